@@ -1,0 +1,117 @@
+/*
+ * dcgpu.h -- C ABI of the GB300 nodal DC-resistivity engine (libdcgpu.so).
+ *
+ * Replaces, for simpeg's 3D nodal DC path, the sparse assembly + direct
+ * factorisation + per-source loops of
+ *   simpeg/electromagnetics/static/resistivity/simulation.py (reference repo).
+ * The system A(sigma) = G^T Me(sigma) G + diag(AvgBC sigma) is never
+ * assembled: it is applied as a matrix-free 7-point nodal stencil and solved
+ * by geometric-multigrid-preconditioned, multi-RHS CG (fp64, or fp32 inner
+ * iterations wrapped in fp64 iterative refinement).
+ *
+ * Conventions
+ *  - All device arrays are caller-owned (any allocator; the Python layer uses
+ *    torch).  Multi-RHS arrays are column-major (N x k) fp64: RHS r occupies
+ *    [r*N, (r+1)*N), the layout of simpeg's Fields "phiSolution" store.
+ *  - Nodes and cells are in Fortran order (x fastest), as in discretize.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Every function returns 0 on success or a DC_ERR_* code; the message of
+ *    the last failure on the calling thread is dc_last_error().
+ *  - A handle may be used from one thread at a time.
+ */
+#ifndef DCGPU_H
+#define DCGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DC_OK 0
+#define DC_ERR_ARG 1           /* bad argument (Python: ValueError/TypeError) */
+#define DC_ERR_CUDA 2          /* CUDA runtime error                          */
+#define DC_ERR_NOT_CONVERGED 3 /* solver hit its iteration limit              */
+#define DC_ERR_BREAKDOWN 4     /* non-positive or non-finite curvature        */
+#define DC_ERR_NOMEM 5         /* workspace too small / allocation failed      */
+#define DC_ERR_STATE 6         /* call out of order (e.g. solve before model)  */
+
+#define DC_MODE_FP64 0   /* plain fp64 MG-PCG                                 */
+#define DC_MODE_MIXED 1  /* fp32 MG-PCG inner solves + fp64 refinement        */
+
+typedef struct dc_handle dc_handle;
+
+typedef struct dc_stats {
+  int iterations;      /* inner PCG iterations summed over refinement sweeps */
+  int outer;           /* refinement sweeps (1 in fp64 mode)                  */
+  int status;          /* DC_OK or DC_ERR_NOT_CONVERGED / DC_ERR_BREAKDOWN    */
+  int n_levels;        /* multigrid levels                                    */
+  double max_rel_res;  /* max over RHS of |b - A x|_2 / |b|_2, fp64          */
+} dc_stats;
+
+/* Mesh + boundary set-up.  Replaces Simulation3DNodal.__init__/setBC
+ * (resistivity/simulation.py:492-501, :573-644).
+ * hx, hy, hz: host cell widths (nx, ny, nz).  bface: host array of
+ * 0.25*alpha_f*area_f for every boundary face, packed by side
+ * [x-lo (ny*nz), x-hi (ny*nz), y-lo (nx*nz), y-hi (nx*nz), z-lo (nx*ny), z-hi (nx*ny)],
+ * each side in Fortran order of its two in-plane cell indices; this is the
+ * diagonal of AvgBC's face weights.  bface == NULL selects the Neumann operator
+ * (no Robin term). */
+int dc_create(int nx, int ny, int nz, const double *hx, const double *hy, const double *hz, const double *bface,
+              dc_handle **out);
+void dc_destroy(dc_handle *h);
+const char *dc_last_error(void);
+
+/* Smoother / hierarchy parameters (before dc_set_model).  Non-positive values keep defaults. */
+int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int coarse_max, int check_every);
+
+/* Number of multigrid levels and nodes of level `lvl`. */
+int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3);
+
+/* Model update: sigma_dev (nC fp64, device).  Builds the per-level stencil
+ * coefficients and the coarsest-level Cholesky.  Replaces getA's MeSigma and
+ * Robin assembly and the solver factorisation (simulation.py:107-108, :523-555). */
+int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream);
+
+/* y = A(sigma) x for k column-major RHS, fp64.  (getA() @ x) */
+int dc_apply(dc_handle *h, const double *x_dev, double *y_dev, int k, void *stream);
+
+/* Workspace needed by dc_solve for k RHS in `mode`. */
+int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes);
+
+/* x = A^-1 b for k column-major RHS.  Replaces `Ainv * RHS`
+ * (simulation.py:111, :181, :245).  Converged when |b - A x| <= rtol |b| per RHS.
+ * inner_rtol / inner_maxit apply to the fp32 inner solves of DC_MODE_MIXED.
+ * ws may be NULL (the handle then allocates and caches its own). */
+int dc_solve(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, double rtol, int maxit,
+             double inner_rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream);
+
+/* out = scale * (dA/dsigma . dsig) u  for k column-major u.  Equals
+ * scale * getADeriv(u, v) with dsig = sigmaDeriv @ v (simulation.py:557-571,
+ * forward): A is linear in sigma, so this is the stencil built from dsig. */
+int dc_dadm_fwd(dc_handle *h, const double *u_dev, const double *dsig_dev, double *out_dev, int k, double scale,
+                void *stream);
+
+/* g = scale * dsig (.) sum_r [ E^T (G u_r (.) G lam_r) + AvgBC^T (u_r (.) lam_r) ]  (nC).
+ * Equals scale * getADeriv(u, lam, adjoint=True) summed over the k pairs
+ * (simulation.py:557-571 adjoint; pde_simulation.py:15-83, :296-321).
+ * dsig_dev may be NULL (derivative with respect to sigma itself). */
+int dc_dadm_adj(dc_handle *h, const double *u_dev, const double *lam_dev, int k, const double *dsig_dev,
+                double scale, double *g_dev, void *stream);
+
+/* Electrode tables (built on the host from trilinear interpolation weights):
+ * y[out_idx[r]] = (accumulate ? y[.] : 0) + scale * sum_{e in row r} w[e] * x[in_idx[e]].
+ * out_idx == NULL means out_idx[r] = r.  Used for receiver projection
+ * (receivers.py:156-244: P u, P^T v) with indices into the column-major arrays. */
+int dc_csr_spmv(int nrows, const long long *rowptr_dev, const long long *in_idx_dev, const double *w_dev,
+                const double *x_dev, const long long *out_idx_dev, double *y_dev, double scale, int accumulate,
+                void *stream);
+
+/* y[idx[e]] = val[e] (indices unique); with y zeroed first this is the source
+ * term q (sources.py:64-88, simulation.py:265-289). */
+int dc_fill_sparse(long long nnz, const long long *idx_dev, const double *val_dev, double *y_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DCGPU_H */

@@ -1,0 +1,831 @@
+// Host orchestration of the nodal DC engine and its C ABI (include/dcgpu.h):
+// multigrid hierarchy set-up, model update, V-cycle, multi-RHS PCG and the
+// fp32/fp64 iterative-refinement driver.
+#include "../../include/dcgpu.h"
+#include "dc_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+namespace dc {
+
+std::string &last_error() {
+  thread_local std::string msg;
+  return msg;
+}
+
+namespace {
+
+int fail(int code, const std::string &msg) {
+  last_error() = msg;
+  return code;
+}
+
+#define CK(expr)                                                                    \
+  do {                                                                              \
+    cudaError_t _e = (expr);                                                        \
+    if (_e != cudaSuccess) return fail(DC_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+template <typename T>
+int dalloc(T **p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(DC_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+template <typename T>
+int upload(T **p, const std::vector<T> &v) {
+  int rc = dalloc(p, v.size());
+  if (rc) return rc;
+  if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Coarse node set of one axis: every second fine node, plus the last one
+// (an odd cell count leaves one single-cell coarse cell at the end).
+Axis1D make_axis(const std::vector<double> &h, bool coarsen) {
+  Axis1D a;
+  const int n = (int)h.size();
+  a.nf = n + 1;
+  std::vector<double> x(n + 1, 0.0);
+  for (int i = 0; i < n; ++i) x[i + 1] = x[i] + h[i];
+  if (coarsen) {
+    for (int i = 0; i <= n; i += 2) a.r_fi.push_back(i);
+    if (a.r_fi.back() != n) a.r_fi.push_back(n);
+  } else {
+    for (int i = 0; i <= n; ++i) a.r_fi.push_back(i);
+  }
+  a.nc = (int)a.r_fi.size();
+  a.pl_idx.assign(a.nf, 0);
+  a.pl_w.assign(a.nf, 1.0);
+  for (int I = 0; I + 1 < a.nc; ++I) {
+    const int f0 = a.r_fi[I], f1 = a.r_fi[I + 1];
+    for (int f = f0; f < f1; ++f) {
+      a.pl_idx[f] = I;
+      a.pl_w[f] = (f == f0) ? 1.0 : (x[f1] - x[f]) / (x[f1] - x[f0]);
+    }
+  }
+  a.pl_idx[n] = a.nc - 1;
+  a.pl_w[n] = 1.0;
+  a.r_wl.assign(a.nc, 0.0);
+  a.r_wr.assign(a.nc, 0.0);
+  for (int I = 0; I < a.nc; ++I) {
+    const int f = a.r_fi[I];
+    if (f - 1 >= 0 && a.pl_idx[f - 1] == I - 1 && a.pl_w[f - 1] < 1.0) a.r_wl[I] = 1.0 - a.pl_w[f - 1];
+    if (f + 1 <= n && a.pl_idx[f + 1] == I && a.pl_w[f + 1] < 1.0) a.r_wr[I] = a.pl_w[f + 1];
+  }
+  return a;
+}
+
+std::vector<double> coarse_widths(const std::vector<double> &h, const Axis1D &a) {
+  std::vector<double> out;
+  for (int I = 0; I + 1 < a.nc; ++I) {
+    double s = 0.0;
+    for (int f = a.r_fi[I]; f < a.r_fi[I + 1]; ++f) s += h[f];
+    out.push_back(s);
+  }
+  return out;
+}
+
+void set_bface_offsets(Level &L) {
+  const long long nyz = (long long)L.ny * L.nz, nxz = (long long)L.nx * L.nz, nxy = (long long)L.nx * L.ny;
+  L.bface_off[0] = 0;
+  L.bface_off[1] = nyz;
+  L.bface_off[2] = 2 * nyz;
+  L.bface_off[3] = 2 * nyz + nxz;
+  L.bface_off[4] = 2 * nyz + 2 * nxz;
+  L.bface_off[5] = 2 * nyz + 2 * nxz + nxy;
+  L.bface_off[6] = 2 * nyz + 2 * nxz + 2 * nxy;
+}
+
+// Aggregate the Robin face weights of a fine level onto the coarse faces they tile.
+std::vector<double> coarse_bface(const Level &f, const Level &c, const Axis1D ax[3]) {
+  std::vector<double> out(c.bface_off[6], 0.0);
+  auto cell_of = [&](int axis, int fine_cell) {
+    const auto &fi = ax[axis].r_fi;
+    int I = (int)(std::upper_bound(fi.begin(), fi.end(), fine_cell) - fi.begin()) - 1;
+    return I;
+  };
+  // x sides: (j, k) in (ny, nz)
+  for (int side = 0; side < 2; ++side)
+    for (int k = 0; k < f.nz; ++k)
+      for (int j = 0; j < f.ny; ++j)
+        out[c.bface_off[side] + cell_of(1, j) + (long long)c.ny * cell_of(2, k)] +=
+            f.bface[f.bface_off[side] + j + (long long)f.ny * k];
+  for (int side = 0; side < 2; ++side)
+    for (int k = 0; k < f.nz; ++k)
+      for (int i = 0; i < f.nx; ++i)
+        out[c.bface_off[2 + side] + cell_of(0, i) + (long long)c.nx * cell_of(2, k)] +=
+            f.bface[f.bface_off[2 + side] + i + (long long)f.nx * k];
+  for (int side = 0; side < 2; ++side)
+    for (int j = 0; j < f.ny; ++j)
+      for (int i = 0; i < f.nx; ++i)
+        out[c.bface_off[4 + side] + cell_of(0, i) + (long long)c.nx * cell_of(1, j)] +=
+            f.bface[f.bface_off[4 + side] + i + (long long)f.nx * j];
+  return out;
+}
+
+void set_dims(Level &L) {
+  L.dims.Nx = L.nx + 1;
+  L.dims.Ny = L.ny + 1;
+  L.dims.Nz = L.nz + 1;
+  L.dims.N = (long long)L.dims.Nx * L.dims.Ny * L.dims.Nz;
+}
+
+struct Cheb {
+  double theta, delta, sigma1;
+};
+Cheb cheb_params(double lmax, double ratio) {
+  const double hi = lmax, lo = lmax / ratio;
+  Cheb c;
+  c.theta = 0.5 * (hi + lo);
+  c.delta = 0.5 * (hi - lo);
+  c.sigma1 = c.theta / c.delta;
+  return c;
+}
+
+}  // namespace
+}  // namespace dc
+
+using namespace dc;
+
+struct dc_handle {
+  int robin = 1;
+  std::vector<Level> lv;
+  int nc = 0;
+  double *d_Ainv64 = nullptr, *d_dense = nullptr, *d_work = nullptr;
+  float *d_Ainv32 = nullptr;
+  int *d_flag = nullptr;
+  unsigned long long *d_lmax = nullptr;
+  bool model_set = false;
+  int nu_pre = 2, nu_post = 2;
+  double cheb_ratio = 6.0;
+  int coarse_max = 600;
+  int check_every = 1;
+  bool built = false;
+  // cached internal workspace
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  // derivative scratch (coefficients of dA/dsigma . dsig, edge products)
+  Level dlev;
+  double *d_P = nullptr, *d_Q = nullptr;
+  // pinned host mailbox for convergence polling
+  int *h_mail = nullptr;
+  double *h_maild = nullptr;
+  cudaEvent_t ev = nullptr;
+};
+
+namespace {
+
+void free_level(Level &L, bool own_geometry) {
+  if (own_geometry) {
+    cudaFree(L.d_h);
+    cudaFree(L.d_bface);
+    cudaFree(L.d_pl_idx);
+    cudaFree(L.d_pl_w);
+    cudaFree(L.d_pl_w32);
+    cudaFree(L.d_r_fi);
+    cudaFree(L.d_r_wl);
+    cudaFree(L.d_r_wr);
+    cudaFree(L.d_r_wl32);
+    cudaFree(L.d_r_wr32);
+    cudaFree(L.d_sigma);
+  }
+  cudaFree(L.d_coef64);
+  cudaFree(L.d_coef32);
+  cudaFree(L.d_invd64);
+  cudaFree(L.d_invd32);
+}
+
+int build_hierarchy(dc_handle *h) {
+  // geometry of every level on the host
+  for (;;) {
+    Level &L = h->lv.back();
+    if (L.dims.N <= h->coarse_max) break;
+    bool cz[3] = {L.nx >= 4, L.ny >= 4, L.nz >= 4};
+    if (!cz[0] && !cz[1] && !cz[2]) break;
+    Level C;
+    const std::vector<double> *hs[3] = {&L.hx, &L.hy, &L.hz};
+    for (int a = 0; a < 3; ++a) L.ax[a] = make_axis(*hs[a], cz[a]);
+    C.hx = coarse_widths(L.hx, L.ax[0]);
+    C.hy = coarse_widths(L.hy, L.ax[1]);
+    C.hz = coarse_widths(L.hz, L.ax[2]);
+    C.nx = (int)C.hx.size();
+    C.ny = (int)C.hy.size();
+    C.nz = (int)C.hz.size();
+    set_dims(C);
+    set_bface_offsets(C);
+    C.bface = coarse_bface(L, C, L.ax);
+    L.has_coarse = true;
+    h->lv.push_back(C);
+  }
+  // upload
+  for (auto &L : h->lv) {
+    std::vector<double> hh(L.hx);
+    hh.insert(hh.end(), L.hy.begin(), L.hy.end());
+    hh.insert(hh.end(), L.hz.begin(), L.hz.end());
+    int rc;
+    if ((rc = upload(&L.d_h, hh))) return rc;
+    if ((rc = upload(&L.d_bface, L.bface))) return rc;
+    const long long nC = (long long)L.nx * L.ny * L.nz;
+    if ((rc = dalloc(&L.d_sigma, nC))) return rc;
+    if ((rc = dalloc(&L.d_coef64, L.dims.N))) return rc;
+    if ((rc = dalloc(&L.d_coef32, L.dims.N))) return rc;
+    if ((rc = dalloc(&L.d_invd64, L.dims.N))) return rc;
+    if ((rc = dalloc(&L.d_invd32, L.dims.N))) return rc;
+    if (L.has_coarse) {
+      std::vector<int> pl, rfi;
+      std::vector<double> pw, rwl, rwr;
+      for (int a = 0; a < 3; ++a) {
+        L.pl_off[a] = (long long)pl.size();
+        L.r_off[a] = (long long)rfi.size();
+        pl.insert(pl.end(), L.ax[a].pl_idx.begin(), L.ax[a].pl_idx.end());
+        pw.insert(pw.end(), L.ax[a].pl_w.begin(), L.ax[a].pl_w.end());
+        rfi.insert(rfi.end(), L.ax[a].r_fi.begin(), L.ax[a].r_fi.end());
+        rwl.insert(rwl.end(), L.ax[a].r_wl.begin(), L.ax[a].r_wl.end());
+        rwr.insert(rwr.end(), L.ax[a].r_wr.begin(), L.ax[a].r_wr.end());
+      }
+      L.pl_off[3] = (long long)pl.size();
+      L.r_off[3] = (long long)rfi.size();
+      std::vector<float> pw32(pw.begin(), pw.end()), rwl32(rwl.begin(), rwl.end()), rwr32(rwr.begin(), rwr.end());
+      if ((rc = upload(&L.d_pl_idx, pl))) return rc;
+      if ((rc = upload(&L.d_pl_w, pw))) return rc;
+      if ((rc = upload(&L.d_pl_w32, pw32))) return rc;
+      if ((rc = upload(&L.d_r_fi, rfi))) return rc;
+      if ((rc = upload(&L.d_r_wl, rwl))) return rc;
+      if ((rc = upload(&L.d_r_wr, rwr))) return rc;
+      if ((rc = upload(&L.d_r_wl32, rwl32))) return rc;
+      if ((rc = upload(&L.d_r_wr32, rwr32))) return rc;
+    }
+  }
+  h->nc = (int)h->lv.back().dims.N;
+  int rc;
+  const size_t nc2 = (size_t)h->nc * h->nc;
+  if ((rc = dalloc(&h->d_Ainv64, nc2))) return rc;
+  if ((rc = dalloc(&h->d_Ainv32, nc2))) return rc;
+  if ((rc = dalloc(&h->d_dense, nc2))) return rc;
+  if ((rc = dalloc(&h->d_work, nc2))) return rc;
+  if ((rc = dalloc(&h->d_flag, 1))) return rc;
+  if ((rc = dalloc(&h->d_lmax, 1))) return rc;
+  h->built = true;
+  return 0;
+}
+
+// ------------------------------------------------------------------ workspace
+struct Carve {
+  char *p;
+  size_t used = 0, cap;
+  template <typename T>
+  T *take(size_t n) {
+    size_t off = (used + 255) & ~size_t(255);
+    used = off + n * sizeof(T) + 0;
+    if (p == nullptr) return nullptr;
+    return reinterpret_cast<T *>(p + off);
+  }
+};
+
+int pick_kb(int k) {
+  // largest KB in {32,16,8,4,2,1} whose padding wastes at most 1/8 of the lanes
+  for (int kb = 32; kb >= 1; kb >>= 1) {
+    const int nb = (k + kb - 1) / kb;
+    if ((long long)(nb * kb - k) * 8 <= (long long)nb * kb) return kb;
+  }
+  return 1;
+}
+
+template <typename T>
+struct MGWork {
+  std::vector<T *> r, z, z2, d, res;
+};
+
+struct Scal {
+  double *part_a, *part_b, *part_c;  // partials (gx * Kp each)
+  double *rz, *rr, *bb, *alpha, *beta, *rr64, *bb64, *maxrel;
+  int *active, *active_out, *n_active, *n_active_out, *status;
+};
+
+template <typename T>
+void carve_mg(Carve &c, const dc_handle *h, int Kp, MGWork<T> &w) {
+  const int L = (int)h->lv.size();
+  w.r.assign(L, nullptr);
+  w.z.assign(L, nullptr);
+  w.z2.assign(L, nullptr);
+  w.d.assign(L, nullptr);
+  w.res.assign(L, nullptr);
+  for (int l = 0; l < L; ++l) {
+    const size_t n = (size_t)h->lv[l].dims.N * Kp;
+    if (l > 0) {
+      w.r[l] = c.take<T>(n);
+      w.z[l] = c.take<T>(n);
+    }
+    if (l + 1 < L || L == 1) {
+      w.z2[l] = c.take<T>(n);
+      w.d[l] = c.take<T>(n);
+      w.res[l] = c.take<T>(n);
+    }
+  }
+}
+
+void carve_scal(Carve &c, int Kp, int gx, Scal &s) {
+  s.part_a = c.take<double>((size_t)gx * Kp);
+  s.part_b = c.take<double>((size_t)gx * Kp);
+  s.part_c = c.take<double>((size_t)gx * Kp);
+  s.rz = c.take<double>(Kp);
+  s.rr = c.take<double>(Kp);
+  s.bb = c.take<double>(Kp);
+  s.alpha = c.take<double>(Kp);
+  s.beta = c.take<double>(Kp);
+  s.rr64 = c.take<double>(Kp);
+  s.bb64 = c.take<double>(Kp);
+  s.maxrel = c.take<double>(1);
+  s.active = c.take<int>(Kp);
+  s.active_out = c.take<int>(Kp);
+  s.n_active = c.take<int>(1);
+  s.n_active_out = c.take<int>(1);
+  s.status = c.take<int>(1);
+}
+
+// Lays out (or, with base == nullptr, sizes) the whole solve workspace.
+struct SolveWS {
+  int KB, nb, Kp, gx;
+  double *B64, *X64, *R64;
+  float *d32, *r32, *p32, *q32, *z32;
+  double *p64, *q64, *z64;
+  MGWork<float> mg32;
+  MGWork<double> mg64;
+  Scal sc;
+  size_t bytes;
+};
+
+void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
+  w.KB = pick_kb(k);
+  w.nb = (k + w.KB - 1) / w.KB;
+  w.Kp = w.nb * w.KB;
+  const long long N = h->lv[0].dims.N;
+  w.gx = node_grid(N, w.KB, w.nb);
+  Carve c{base};
+  const size_t n = (size_t)N * w.Kp;
+  w.B64 = c.take<double>(n);
+  w.X64 = c.take<double>(n);
+  w.R64 = c.take<double>(n);
+  if (mode == DC_MODE_MIXED) {
+    w.d32 = c.take<float>(n);
+    w.r32 = c.take<float>(n);
+    w.p32 = c.take<float>(n);
+    w.q32 = c.take<float>(n);
+    w.z32 = c.take<float>(n);
+    carve_mg(c, h, w.Kp, w.mg32);
+  } else {
+    w.p64 = c.take<double>(n);
+    w.q64 = c.take<double>(n);
+    w.z64 = c.take<double>(n);
+    carve_mg(c, h, w.Kp, w.mg64);
+  }
+  carve_scal(c, w.Kp, w.gx, w.sc);
+  w.bytes = c.used + 256;
+}
+
+// ------------------------------------------------------------------ V-cycle
+template <typename T>
+const T *ainv(const dc_handle *h);
+template <>
+const float *ainv<float>(const dc_handle *h) { return h->d_Ainv32; }
+template <>
+const double *ainv<double>(const dc_handle *h) { return h->d_Ainv64; }
+
+template <typename T, int KB>
+void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int nb, cudaStream_t s) {
+  using O = Ops<T, KB>;
+  const int L = (int)h->lv.size();
+  if (l == L - 1) {
+    if (L == 1) {
+      // single level: plain Chebyshev smoothing as the preconditioner
+    }
+    O::coarse_solve(ainv<T>(h), h->nc, r, z, nb, s);
+    return;
+  }
+  const Level &F = h->lv[l];
+  const Level &C = h->lv[l + 1];
+  const Cheb cp = cheb_params(F.lmax, h->cheb_ratio);
+  const int swaps = (h->nu_pre - 1) + h->nu_post;
+  T *cur = (swaps % 2) ? w.z2[l] : z;
+  T *oth = (swaps % 2) ? z : w.z2[l];
+  // pre-smoothing from zero
+  O::cheb_first(F, r, cur, w.d[l], nb, 1.0 / cp.theta, s);
+  double rho_old = 1.0 / cp.sigma1;
+  for (int it = 1; it < h->nu_pre; ++it) {
+    const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
+    O::cheb_step(F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, s);
+    std::swap(cur, oth);
+    rho_old = rho;
+  }
+  // coarse-grid correction
+  O::residual(F, r, cur, w.res[l], nb, s);
+  O::restrict_(F, C, w.res[l], w.r[l + 1], nb, s);
+  vcycle<T, KB>(h, l + 1, w.r[l + 1], w.z[l + 1], w, nb, s);
+  O::prolong_add(F, C, w.z[l + 1], cur, nb, s);
+  // post-smoothing (same polynomial, nonzero start)
+  O::cheb_step(F, r, cur, oth, w.d[l], nb, 0.0, 1.0 / cp.theta, s);
+  std::swap(cur, oth);
+  rho_old = 1.0 / cp.sigma1;
+  for (int it = 1; it < h->nu_post; ++it) {
+    const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
+    O::cheb_step(F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, s);
+    std::swap(cur, oth);
+    rho_old = rho;
+  }
+  if (cur != z) cudaMemcpyAsync(z, cur, sizeof(T) * F.dims.N * KB * nb, cudaMemcpyDeviceToDevice, s);
+}
+
+// ------------------------------------------------------------------ PCG
+// Solves A x = r0 (x = 0 on entry, r holds r0 and is overwritten by the residual).
+// init_active (nullable): RHS with init_active[r] == 0 are left untouched.
+template <typename T, int KB>
+int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Scal &sc, int nb, int gx,
+        const int *init_active, double tol, int maxit, int *iters, cudaStream_t s) {
+  using O = Ops<T, KB>;
+  const Level &F = h->lv[0];
+  const long long N = F.dims.N;
+  const int Kp = nb * KB;
+  if (init_active)
+    CK(cudaMemcpyAsync(sc.active, init_active, sizeof(int) * Kp, cudaMemcpyDeviceToDevice, s));
+  else {
+    std::vector<int> ones(Kp, 1);
+    CK(cudaMemcpyAsync(sc.active, ones.data(), sizeof(int) * Kp, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemsetAsync(sc.status, 0, sizeof(int), s));
+  O::dot(N, nb, r, r, sc.part_b, gx, s);
+  sum_partials(Kp, KB, gx, sc.part_b, sc.bb, s);
+  vcycle<T, KB>(h, 0, r, z, w, nb, s);
+  O::dot(N, nb, r, z, sc.part_c, gx, s);
+  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol * tol, sc.active, sc.beta, sc.n_active, 1, s);
+  O::copy(N, nb, p, z, s);
+  int it = 0;
+  int since = 0;
+  for (it = 0; it < maxit; ++it) {
+    O::apply(F, p, q, nb, sc.part_a, gx, s);
+    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, s);
+    O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, s);
+    vcycle<T, KB>(h, 0, r, z, w, nb, s);
+    O::dot(N, nb, r, z, sc.part_c, gx, s);
+    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol * tol, sc.active, sc.beta, sc.n_active, 0, s);
+    O::p_update(N, nb, p, z, sc.beta, s);
+    if (++since >= h->check_every || it + 1 == maxit) {
+      since = 0;
+      CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(h->h_mail + 1, sc.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaEventRecord(h->ev, s));
+      CK(cudaEventSynchronize(h->ev));
+      if (h->h_mail[1] != 0) {
+        *iters = it + 1;
+        return fail(DC_ERR_BREAKDOWN, "PCG breakdown: non-positive or non-finite p.Ap");
+      }
+      if (h->h_mail[0] == 0) {
+        ++it;
+        break;
+      }
+    }
+  }
+  *iters = it;
+  // report whether anything is still active
+  CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev, s));
+  CK(cudaEventSynchronize(h->ev));
+  return h->h_mail[0] == 0 ? 0 : DC_ERR_NOT_CONVERGED;
+}
+
+template <int KB>
+int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
+             int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s) {
+  const Level &F = h->lv[0];
+  const long long N = F.dims.N;
+  const int nb = w.nb, Kp = w.Kp, gx = w.gx;
+  pack_colmajor<double>(b, N, k, KB, nb, w.B64, s);
+  CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));
+  int total_it = 0, outer = 0, status = 0;
+  if (mode == DC_MODE_FP64) {
+    CK(cudaMemcpyAsync(w.R64, w.B64, sizeof(double) * N * Kp, cudaMemcpyDeviceToDevice, s));
+    int it = 0;
+    status = pcg<double, KB>(h, w.X64, w.R64, w.p64, w.q64, w.z64, w.mg64, w.sc, nb, gx, nullptr, rtol, maxit, &it, s);
+    if (status == DC_ERR_BREAKDOWN) return status;
+    total_it = it;
+    outer = 1;
+    // true residual
+    ir_residual<KB>(F, w.B64, w.X64, w.R64, (float *)w.p64, nb, w.sc.active, w.sc.part_a, gx, s);
+    sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
+    Ops<double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
+    sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
+    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+  } else {
+    // |b|^2, initial outer flags, r32 = b
+    Ops<double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
+    sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
+    sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
+    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+    pack_colmajor<float>(b, N, k, KB, nb, w.r32, s);
+    const int max_outer = 30;
+    for (outer = 0; outer < max_outer;) {
+      CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaEventRecord(h->ev, s));
+      CK(cudaEventSynchronize(h->ev));
+      if (h->h_mail[0] == 0) break;
+      if (total_it >= maxit) {
+        status = DC_ERR_NOT_CONVERGED;
+        break;
+      }
+      CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
+      int it = 0;
+      int rc = pcg<float, KB>(h, w.d32, w.r32, w.p32, w.q32, w.z32, w.mg32, w.sc, nb, gx, w.sc.active_out,
+                              inner_rtol, std::min(inner_maxit, maxit - total_it), &it, s);
+      total_it += it;
+      if (rc == DC_ERR_BREAKDOWN) return rc;
+      ir_accumulate<KB>(N, nb, w.X64, w.d32, s);
+      ++outer;
+      ir_residual<KB>(F, w.B64, w.X64, w.R64, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, s);
+      sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
+      outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+    }
+    if (outer >= max_outer) status = DC_ERR_NOT_CONVERGED;
+  }
+  unpack_colmajor<double>(w.X64, N, k, KB, x, s);
+  CK(cudaMemcpyAsync(h->h_maild, w.sc.maxrel, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev, s));
+  CK(cudaEventSynchronize(h->ev));
+  if (h->h_mail[0] != 0) status = DC_ERR_NOT_CONVERGED;
+  if (st) {
+    st->iterations = total_it;
+    st->outer = outer;
+    st->status = status;
+    st->n_levels = (int)h->lv.size();
+    st->max_rel_res = h->h_maild[0];
+  }
+  if (status) return fail(status, "solver did not reach the requested tolerance");
+  return 0;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char *dc_last_error(void) { return dc::last_error().c_str(); }
+
+int dc_create(int nx, int ny, int nz, const double *hx, const double *hy, const double *hz, const double *bface,
+              dc_handle **out) {
+  if (!out) return fail(DC_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (nx < 1 || ny < 1 || nz < 1) return fail(DC_ERR_ARG, "cell counts must be positive");
+  if (!hx || !hy || !hz) return fail(DC_ERR_ARG, "cell widths are NULL");
+  const long long N = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+  if (N >= (1LL << 31)) return fail(DC_ERR_ARG, "mesh too large (nodes must fit in int32)");
+  for (int i = 0; i < nx; ++i) if (!(hx[i] > 0) || !std::isfinite(hx[i])) return fail(DC_ERR_ARG, "bad hx");
+  for (int i = 0; i < ny; ++i) if (!(hy[i] > 0) || !std::isfinite(hy[i])) return fail(DC_ERR_ARG, "bad hy");
+  for (int i = 0; i < nz; ++i) if (!(hz[i] > 0) || !std::isfinite(hz[i])) return fail(DC_ERR_ARG, "bad hz");
+  int dev = 0, nsm = 152;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  set_sm_count(nsm);
+  std::unique_ptr<dc_handle> h(new (std::nothrow) dc_handle());
+  if (!h) return fail(DC_ERR_NOMEM, "host allocation failed");
+  h->robin = bface != nullptr;
+  Level L0;
+  L0.nx = nx;
+  L0.ny = ny;
+  L0.nz = nz;
+  L0.hx.assign(hx, hx + nx);
+  L0.hy.assign(hy, hy + ny);
+  L0.hz.assign(hz, hz + nz);
+  set_dims(L0);
+  set_bface_offsets(L0);
+  L0.bface.assign(L0.bface_off[6], 0.0);
+  if (bface) {
+    for (long long i = 0; i < L0.bface_off[6]; ++i) {
+      if (!std::isfinite(bface[i])) return fail(DC_ERR_ARG, "bad Robin face weight");
+      L0.bface[i] = bface[i];
+    }
+  }
+  h->lv.push_back(L0);
+  CK(cudaMallocHost((void **)&h->h_mail, 4 * sizeof(int)));
+  CK(cudaMallocHost((void **)&h->h_maild, 2 * sizeof(double)));
+  CK(cudaEventCreateWithFlags(&h->ev, cudaEventDisableTiming));
+  *out = h.release();
+  return 0;
+}
+
+void dc_destroy(dc_handle *h) {
+  if (!h) return;
+  cudaDeviceSynchronize();
+  for (auto &L : h->lv) free_level(L, true);
+  cudaFree(h->dlev.d_coef64);
+  cudaFree(h->dlev.d_coef32);
+  cudaFree(h->dlev.d_invd64);
+  cudaFree(h->dlev.d_invd32);
+  cudaFree(h->d_P);
+  cudaFree(h->d_Q);
+  cudaFree(h->d_Ainv64);
+  cudaFree(h->d_Ainv32);
+  cudaFree(h->d_dense);
+  cudaFree(h->d_work);
+  cudaFree(h->d_flag);
+  cudaFree(h->d_lmax);
+  cudaFree(h->ws);
+  if (h->h_mail) cudaFreeHost(h->h_mail);
+  if (h->h_maild) cudaFreeHost(h->h_maild);
+  if (h->ev) cudaEventDestroy(h->ev);
+  delete h;
+}
+
+int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int coarse_max, int check_every) {
+  if (!h) return fail(DC_ERR_ARG, "handle is NULL");
+  if (coarse_max > 0 && h->built && coarse_max != h->coarse_max)
+    return fail(DC_ERR_STATE, "coarse_max must be set before the first dc_set_model");
+  if (nu_pre > 0) h->nu_pre = nu_pre;
+  if (nu_post > 0) h->nu_post = nu_post;
+  if (cheb_ratio > 1.0) h->cheb_ratio = cheb_ratio;
+  if (coarse_max > 0) {
+    if (coarse_max > 4096) return fail(DC_ERR_ARG, "coarse_max must be <= 4096");
+    h->coarse_max = coarse_max;
+  }
+  if (check_every > 0) h->check_every = check_every;
+  return 0;
+}
+
+int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3) {
+  if (!h) return fail(DC_ERR_ARG, "handle is NULL");
+  if (!h->built) return fail(DC_ERR_STATE, "hierarchy is built by dc_set_model");
+  if (n_levels) *n_levels = (int)h->lv.size();
+  if (lvl < 0 || lvl >= (int)h->lv.size()) return fail(DC_ERR_ARG, "level out of range");
+  if (nodes) *nodes = h->lv[lvl].dims.N;
+  if (cells3) {
+    cells3[0] = h->lv[lvl].nx;
+    cells3[1] = h->lv[lvl].ny;
+    cells3[2] = h->lv[lvl].nz;
+  }
+  return 0;
+}
+
+int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
+  if (!h || !sigma_dev) return fail(DC_ERR_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->built) {
+    int rc = build_hierarchy(h);
+    if (rc) return rc;
+  }
+  Level &L0 = h->lv[0];
+  const long long nC = (long long)L0.nx * L0.ny * L0.nz;
+  CK(cudaMemcpyAsync(L0.d_sigma, sigma_dev, sizeof(double) * nC, cudaMemcpyDeviceToDevice, s));
+  for (size_t l = 0; l + 1 < h->lv.size(); ++l) coarsen_sigma(h->lv[l], h->lv[l + 1], s);
+  for (auto &L : h->lv) {
+    CK(cudaMemsetAsync(h->d_lmax, 0, sizeof(unsigned long long), s));
+    coef_build(L, h->robin, h->d_lmax, s);
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, h->d_lmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    double lm;
+    std::memcpy(&lm, &bits, sizeof(lm));
+    if (!(lm > 0.0) || !std::isfinite(lm)) return fail(DC_ERR_ARG, "conductivity must be positive and finite");
+    L.lmax = lm;
+  }
+  CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), s));
+  dense_assemble(h->lv.back(), h->d_dense, s);
+  dense_cholesky_inverse(h->d_dense, h->d_work, h->nc, h->d_Ainv64, h->d_Ainv32, h->d_flag, s);
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  if (flag) return fail(DC_ERR_ARG, "coarsest operator is not positive definite (Neumann operator or bad sigma)");
+  h->model_set = true;
+  return 0;
+}
+
+int dc_apply(dc_handle *h, const double *x, double *y, int k, void *stream) {
+  if (!h || !x || !y || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  Ops<double, 1>::apply(h->lv[0], x, y, k, nullptr, 0, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes) {
+  if (!h || !bytes || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
+  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model first");
+  SolveWS w;
+  layout_ws(h, mode, k, nullptr, w);
+  *bytes = w.bytes;
+  return 0;
+}
+
+int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
+             int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream) {
+  if (!h || !b || !x || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
+  if (!(rtol > 0.0) || maxit < 1) return fail(DC_ERR_ARG, "rtol must be > 0 and maxit >= 1");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  if (!(inner_rtol > 0.0)) inner_rtol = 1e-4;
+  if (inner_maxit < 1) inner_maxit = 200;
+  cudaStream_t s = (cudaStream_t)stream;
+  SolveWS w;
+  layout_ws(h, mode, k, nullptr, w);
+  char *base = (char *)ws;
+  if (base) {
+    if (ws_bytes < w.bytes) return fail(DC_ERR_NOMEM, "workspace too small");
+  } else {
+    if (h->ws_bytes < w.bytes) {
+      CK(cudaStreamSynchronize(s));
+      cudaFree(h->ws);
+      h->ws = nullptr;
+      h->ws_bytes = 0;
+      if (cudaMalloc(&h->ws, w.bytes) != cudaSuccess) return fail(DC_ERR_NOMEM, "cannot allocate solve workspace");
+      h->ws_bytes = w.bytes;
+    }
+    base = (char *)h->ws;
+  }
+  base = (char *)(((uintptr_t)base + 255) & ~(uintptr_t)255);
+  layout_ws(h, mode, k, base, w);
+  int rc;
+  switch (w.KB) {
+    case 32: rc = solve_kb<32>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+    case 16: rc = solve_kb<16>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+    case 8: rc = solve_kb<8>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+    case 4: rc = solve_kb<4>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+    case 2: rc = solve_kb<2>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+    default: rc = solve_kb<1>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(DC_ERR_CUDA, std::string("dc_solve: ") + cudaGetErrorString(e));
+  return rc;
+}
+
+static int ensure_dlev(dc_handle *h) {
+  if (h->dlev.d_coef64) return 0;
+  const Level &L0 = h->lv[0];
+  int rc;
+  if ((rc = dalloc(&h->dlev.d_coef64, L0.dims.N))) return rc;
+  if ((rc = dalloc(&h->dlev.d_coef32, L0.dims.N))) return rc;
+  if ((rc = dalloc(&h->dlev.d_invd64, L0.dims.N))) return rc;
+  if ((rc = dalloc(&h->dlev.d_invd32, L0.dims.N))) return rc;
+  if ((rc = dalloc(&h->d_P, 3 * L0.dims.N))) return rc;
+  if ((rc = dalloc(&h->d_Q, L0.dims.N))) return rc;
+  return 0;
+}
+
+int dc_dadm_fwd(dc_handle *h, const double *u, const double *dsig, double *out, int k, double scale, void *stream) {
+  if (!h || !u || !dsig || !out || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model first");
+  int rc = ensure_dlev(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Level D = h->lv[0];  // geometry of level 0, coefficients of dsig
+  D.d_sigma = const_cast<double *>(dsig);
+  D.d_coef64 = h->dlev.d_coef64;
+  D.d_coef32 = h->dlev.d_coef32;
+  D.d_invd64 = h->dlev.d_invd64;
+  D.d_invd32 = h->dlev.d_invd32;
+  coef_build(D, h->robin, h->d_lmax, s);
+  Ops<double, 1>::apply(D, u, out, k, nullptr, 0, s);
+  if (scale != 1.0) scale_vec(D.dims.N * (long long)k, out, scale, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const double *dsig, double scale, double *g,
+                void *stream) {
+  if (!h || !u || !lam || !g || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model first");
+  int rc = ensure_dlev(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Level &L0 = h->lv[0];
+  edge_products(u, lam, k, L0.dims, h->d_P, h->d_Q, s);
+  cell_gradient(L0, h->robin, h->d_P, h->d_Q, dsig, scale, g, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const double *w, const double *x,
+                const long long *out_idx, double *y, double scale, int accumulate, void *stream) {
+  if (nrows < 0) return fail(DC_ERR_ARG, "nrows < 0");
+  if (nrows == 0) return 0;
+  if (!rowptr || !in_idx || !w || !x || !y) return fail(DC_ERR_ARG, "NULL argument");
+  csr_spmv(nrows, rowptr, in_idx, w, x, out_idx, y, scale, accumulate, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_fill_sparse(long long nnz, const long long *idx, const double *val, double *y, void *stream) {
+  if (nnz < 0) return fail(DC_ERR_ARG, "nnz < 0");
+  if (nnz == 0) return 0;
+  if (!idx || !val || !y) return fail(DC_ERR_ARG, "NULL argument");
+  fill_sparse(nnz, idx, val, y, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+}  // extern "C"

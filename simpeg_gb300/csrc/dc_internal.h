@@ -1,0 +1,125 @@
+// Internal declarations of the nodal DC engine (not part of the C ABI).
+//
+// Data layout in HBM
+// ------------------
+// * Node n = i + Nx*(j + Ny*k) (Fortran order, x fastest), as in discretize.
+// * Inside the solver a block of K right-hand sides is stored RHS-interleaved
+//   in blocks of KB: element (node n, rhs r) lives at ((r / KB) * N + n) * KB + r % KB.
+//   With KB = 32 one warp covers one node and 32 RHS, so every stencil load is
+//   one 128-byte (fp32) line and the per-node coefficients are warp-uniform.
+//   For K < 32 a smaller KB (1..16) packs several nodes per warp.  KB = 1 with
+//   K blocks is exactly the column-major (N x K) layout of the C ABI.
+// * The stencil coefficients of a level are one 4-vector per node
+//   {cx, cy, cz, diag}: c* is the coupling to the +x/+y/+z neighbour (zero on
+//   the last node of that axis), diag = sum of the six couplings + Robin term.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace dc {
+
+struct alignas(32) Coef64 { double cx, cy, cz, d; };
+struct alignas(16) Coef32 { float cx, cy, cz, d; };
+
+struct Dims {
+  int Nx, Ny, Nz;  // nodes per axis
+  long long N;     // nodes
+};
+
+// 1D transfer tables between a fine axis (nf nodes) and its coarse axis (nc nodes).
+struct Axis1D {
+  int nf = 0, nc = 0;
+  std::vector<int> pl_idx;      // fine node -> left coarse node
+  std::vector<double> pl_w;     // weight on the left coarse node (1 - w on the right one)
+  std::vector<int> r_fi;        // coarse node -> fine node (also the cell map: coarse cell I = fine cells [fi[I], fi[I+1]))
+  std::vector<double> r_wl, r_wr;  // restriction weights of fine fi-1 and fi+1
+};
+
+struct Level {
+  int nx = 0, ny = 0, nz = 0;  // cells
+  Dims dims{};
+  std::vector<double> hx, hy, hz;
+  std::vector<double> bface;        // host: 0.25*alpha*area, 6 sides packed
+  double *d_h = nullptr;            // device: hx | hy | hz
+  double *d_bface = nullptr;        // device copy of bface
+  long long bface_off[7] = {0};     // xlo, xhi, ylo, yhi, zlo, zhi, end
+  double *d_sigma = nullptr;        // cell conductivity (nC)
+  Coef64 *d_coef64 = nullptr;
+  Coef32 *d_coef32 = nullptr;
+  double *d_invd64 = nullptr;       // 1/diag
+  float *d_invd32 = nullptr;
+  double lmax = 2.0;                // Gershgorin bound of D^-1 A
+  // transfer to the next coarser level (valid when has_coarse)
+  bool has_coarse = false;
+  Axis1D ax[3];
+  int *d_pl_idx = nullptr;
+  double *d_pl_w = nullptr;
+  float *d_pl_w32 = nullptr;
+  int *d_r_fi = nullptr;
+  double *d_r_wl = nullptr, *d_r_wr = nullptr;
+  float *d_r_wl32 = nullptr, *d_r_wr32 = nullptr;
+  long long pl_off[4] = {0}, r_off[4] = {0};
+};
+
+// ---- dc_stencil.cu -----------------------------------------------------------
+void set_sm_count(int n);
+int node_grid(long long nodes, int KB, int nb);
+
+template <typename T, int KB> struct Ops {
+  // y = A x ; if partial: per-block partial sums of x.y
+  static void apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
+  static void residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s);
+  static void cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s);
+  static void cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
+                        cudaStream_t s);
+  static void restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s);
+  static void prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s);
+  static void coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s);
+  static void update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
+                        double *partial, int gx, cudaStream_t s);
+  static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
+  static void p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s);
+  static void copy(long long N, int nb, T *dst, const T *src, cudaStream_t s);
+};
+
+template <int KB>
+void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
+                 const int *active, double *partial, int gx, cudaStream_t s);
+template <int KB>
+void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s);
+
+void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
+               int *status, cudaStream_t s);
+void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
+              const double *bb, double tol2, int *active, double *beta, int *n_active, int first, cudaStream_t s);
+void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s);
+void outer_check(int K, const double *rr, const double *bb, double tol2, int *active, int *n_active, double *maxrel,
+                 cudaStream_t s);
+
+void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s);
+void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s);
+void dense_assemble(const Level &L, double *dense, cudaStream_t s);
+void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, float *Ainv32, int *flag,
+                            cudaStream_t s);
+
+template <typename T>
+void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s);
+template <typename T>
+void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s);
+
+// ---- dc_sens.cu -------------------------------------------------------------
+void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const double *w, const double *x,
+              const long long *out_idx, double *y, double scale, int accumulate, cudaStream_t s);
+void fill_sparse(long long nnz, const long long *idx, const double *val, double *y, cudaStream_t s);
+void scale_vec(long long n, double *y, double a, cudaStream_t s);
+void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s);
+void cell_gradient(const Level &L, int robin, const double *P, const double *Q, const double *dsig, double scale,
+                   double *g, cudaStream_t s);
+
+std::string &last_error();
+
+}  // namespace dc

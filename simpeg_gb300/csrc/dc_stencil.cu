@@ -1,0 +1,848 @@
+// Stencil, multigrid-transfer, PCG-vector and reduction kernels of the nodal
+// DC engine.  Every kernel here is bandwidth-bound except the fp64 stencil,
+// which on this part is bounded by fp64 issue rate (see the design notes).
+//
+// Thread mapping of every "node" kernel: blockDim = 256 = NPB nodes x KB lanes
+// (NPB = 256 / KB); blockIdx.y = RHS block; blockIdx.x strides over node
+// groups.  Lane l of node n in RHS block b touches element (b*N + n)*KB + l,
+// so a warp's loads are contiguous.
+#include "dc_internal.h"
+
+#include <cstdio>
+#include <type_traits>
+
+namespace dc {
+
+namespace {
+
+constexpr int TPB = 256;
+
+__device__ __forceinline__ void node_ijk(int n, const Dims &d, int &i, int &j, int &k) {
+  int nxy = d.Nx * d.Ny;
+  k = n / nxy;
+  int r = n - k * nxy;
+  j = r / d.Nx;
+  i = r - j * d.Nx;
+}
+
+template <typename C> struct CoefT;
+template <> struct CoefT<double> { using type = Coef64; };
+template <> struct CoefT<float> { using type = Coef32; };
+
+// y = (A x) at element t of node (i, j, k).
+template <typename T, int KB>
+__device__ __forceinline__ T stencil_at(const typename CoefT<T>::type *__restrict__ coef,
+                                        const T *__restrict__ x, long long t, int n, int i, int j,
+                                        int k, const Dims &d) {
+  const auto c = coef[n];
+  T acc = c.d * x[t];
+  const long long sx = KB, sy = (long long)d.Nx * KB, sz = (long long)d.Nx * d.Ny * KB;
+  if (i + 1 < d.Nx) acc -= c.cx * x[t + sx];
+  if (i > 0) acc -= coef[n - 1].cx * x[t - sx];
+  if (j + 1 < d.Ny) acc -= c.cy * x[t + sy];
+  if (j > 0) acc -= coef[n - d.Nx].cy * x[t - sy];
+  if (k + 1 < d.Nz) acc -= c.cz * x[t + sz];
+  if (k > 0) acc -= coef[n - d.Nx * d.Ny].cz * x[t - sz];
+  return acc;
+}
+
+// Block-level reduction of one value per thread into per-lane partial sums:
+// partial[(blockIdx.y * gridDim.x + blockIdx.x) * KB + lane].
+template <int KB, typename A>
+__device__ __forceinline__ void block_partial(A v, double *partial) {
+  __shared__ double red[TPB / 32][32];
+#pragma unroll
+  for (int off = 16; off >= KB; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < KB) red[warp][lane] = (double)v;
+  __syncthreads();
+  if (threadIdx.x < KB) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; ++w) s += red[w][threadIdx.x];
+    partial[((long long)blockIdx.y * gridDim.x + blockIdx.x) * KB + threadIdx.x] = s;
+  }
+}
+
+// ---------------------------------------------------------------- stencil ops
+template <typename T, int KB, bool DOT>
+__global__ void __launch_bounds__(TPB) k_apply(const typename CoefT<T>::type *__restrict__ coef,
+                                               const T *__restrict__ x, T *__restrict__ y, Dims d,
+                                               double *__restrict__ partial) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * d.N * KB + lane;
+  T acc = 0;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const long long t = base + (long long)n * KB;
+    T v = stencil_at<T, KB>(coef, x, t, n, i, j, k, d);
+    y[t] = v;
+    if (DOT) acc += v * x[t];
+  }
+  if (DOT) block_partial<KB>(acc, partial);
+}
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_residual(const typename CoefT<T>::type *__restrict__ coef,
+                                                  const T *__restrict__ r, const T *__restrict__ z,
+                                                  T *__restrict__ res, Dims d) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * d.N * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const long long t = base + (long long)n * KB;
+    res[t] = r[t] - stencil_at<T, KB>(coef, z, t, n, i, j, k, d);
+  }
+}
+
+// First Chebyshev step from z = 0: d = c0 * D^-1 r ; z = d.
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, const T *__restrict__ r,
+                                                    T *__restrict__ z, T *__restrict__ dv, Dims d, T c0) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * d.N * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+    const long long t = base + (long long)n * KB;
+    T v = c0 * invd[n] * r[t];
+    z[t] = v;
+    dv[t] = v;
+  }
+}
+
+// Chebyshev step: d = c1 d + c2 D^-1 (r - A zin) ; zout = zin + d.
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_cheb_step(const typename CoefT<T>::type *__restrict__ coef,
+                                                   const T *__restrict__ invd, const T *__restrict__ r,
+                                                   const T *__restrict__ zin, T *__restrict__ zout,
+                                                   T *__restrict__ dv, Dims d, T c1, T c2) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * d.N * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const long long t = base + (long long)n * KB;
+    T res = r[t] - stencil_at<T, KB>(coef, zin, t, n, i, j, k, d);
+    T dn = c1 * dv[t] + c2 * invd[n] * res;
+    dv[t] = dn;
+    zout[t] = zin[t] + dn;
+  }
+}
+
+// ---------------------------------------------------------------- transfers
+struct XferTab {
+  const int *fi;       // coarse node -> fine node, per axis at off[a]
+  const void *wl, *wr; // T weights of fine fi-1 / fi+1
+  const int *pl;       // fine node -> left coarse node
+  const void *pw;      // T weight on pl
+  long long roff[3], poff[3];
+};
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *__restrict__ rc, Dims f,
+                                                  Dims c, XferTab tb) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const T *wl = (const T *)tb.wl, *wr = (const T *)tb.wr;
+  const long long fbase = (long long)blockIdx.y * f.N * KB + lane;
+  const long long cbase = (long long)blockIdx.y * c.N * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < c.N; n += gridDim.x * NPB) {
+    int I, J, K;
+    node_ijk(n, c, I, J, K);
+    const int fx = tb.fi[tb.roff[0] + I], fy = tb.fi[tb.roff[1] + J], fz = tb.fi[tb.roff[2] + K];
+    T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
+    T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
+    T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
+    T acc = 0;
+#pragma unroll
+    for (int cz = 0; cz < 3; ++cz) {
+      if (wz[cz] == (T)0) continue;
+#pragma unroll
+      for (int cy = 0; cy < 3; ++cy) {
+        if (wy[cy] == (T)0) continue;
+        const T wyz = wy[cy] * wz[cz];
+        const long long row = ((long long)(fz + cz - 1) * f.Ny + (fy + cy - 1)) * f.Nx;
+#pragma unroll
+        for (int cx = 0; cx < 3; ++cx) {
+          if (wx[cx] == (T)0) continue;
+          acc += wx[cx] * wyz * res[fbase + (row + fx + cx - 1) * KB];
+        }
+      }
+    }
+    rc[cbase + (long long)n * KB] = acc;
+  }
+}
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T *__restrict__ z, Dims f,
+                                                     Dims c, XferTab tb) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const T *pw = (const T *)tb.pw;
+  const long long fbase = (long long)blockIdx.y * f.N * KB + lane;
+  const long long cbase = (long long)blockIdx.y * c.N * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < f.N; n += gridDim.x * NPB) {
+    int i, j, k;
+    node_ijk(n, f, i, j, k);
+    const int I = tb.pl[tb.poff[0] + i], J = tb.pl[tb.poff[1] + j], K = tb.pl[tb.poff[2] + k];
+    const T ax = pw[tb.poff[0] + i], ay = pw[tb.poff[1] + j], az = pw[tb.poff[2] + k];
+    const T wx[2] = {ax, (T)1 - ax}, wy[2] = {ay, (T)1 - ay}, wz[2] = {az, (T)1 - az};
+    T acc = 0;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      if (wz[b] == (T)0) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        if (wy[a] == (T)0) continue;
+        const T wyz = wy[a] * wz[b];
+        const long long row = ((long long)(K + b) * c.Ny + (J + a)) * c.Nx;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          if (wx[e] == (T)0) continue;
+          acc += wx[e] * wyz * zc[cbase + (row + I + e) * KB];
+        }
+      }
+    }
+    const long long t = fbase + (long long)n * KB;
+    z[t] += acc;
+  }
+}
+
+// z_c = Ainv r_c on the coarsest level (dense, row-major Ainv[nc][nc]).
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, int nc,
+                                                      const T *__restrict__ rc, T *__restrict__ zc) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * nc * KB + lane;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < nc; n += gridDim.x * NPB) {
+    const T *row = Ainv + (long long)n * nc;
+    T acc = 0;
+    for (int m = 0; m < nc; ++m) acc += row[m] * rc[base + (long long)m * KB];
+    zc[base + (long long)n * KB] = acc;
+  }
+}
+
+// ---------------------------------------------------------------- PCG vectors
+// x += a p ; r -= a q ; partial |r|^2   (a per RHS)
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_update_xr(long long N, T *__restrict__ x, T *__restrict__ r,
+                                                   const T *__restrict__ p, const T *__restrict__ q,
+                                                   const double *__restrict__ alpha,
+                                                   double *__restrict__ partial) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * N * KB + lane;
+  const T a = (T)alpha[blockIdx.y * KB + lane];
+  T acc = 0;
+  if (a != (T)0) {
+    for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
+      const long long t = base + n * KB;
+      x[t] += a * p[t];
+      T rv = r[t] - a * q[t];
+      r[t] = rv;
+      acc += rv * rv;
+    }
+  } else {
+    for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
+      T rv = r[base + n * KB];
+      acc += rv * rv;
+    }
+  }
+  block_partial<KB>(acc, partial);
+}
+
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_dot(long long N, const T *__restrict__ a, const T *__restrict__ b,
+                                             double *__restrict__ partial) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * N * KB + lane;
+  T acc = 0;
+  for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
+    const long long t = base + n * KB;
+    acc += a[t] * b[t];
+  }
+  block_partial<KB>(acc, partial);
+}
+
+// p = z + beta p
+template <typename T, int KB>
+__global__ void __launch_bounds__(TPB) k_p_update(long long N, T *__restrict__ p, const T *__restrict__ z,
+                                                  const double *__restrict__ beta) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * N * KB + lane;
+  const T bt = (T)beta[blockIdx.y * KB + lane];
+  for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
+    const long long t = base + n * KB;
+    p[t] = z[t] + bt * p[t];
+  }
+}
+
+// ---------------------------------------------------------------- refinement
+template <int KB>
+__global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ coef, const double *__restrict__ b,
+                                                     const double *__restrict__ x, double *__restrict__ r64,
+                                                     float *__restrict__ r32, Dims d,
+                                                     const int *__restrict__ active, double *__restrict__ partial) {
+  constexpr int NPB = TPB / KB;
+  const int lane = threadIdx.x % KB;
+  const long long base = (long long)blockIdx.y * d.N * KB + lane;
+  const bool act = active[blockIdx.y * KB + lane] != 0;
+  double acc = 0.0;
+  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const long long t = base + (long long)n * KB;
+    double rv = b[t] - stencil_at<double, KB>(coef, x, t, n, i, j, k, d);
+    r64[t] = rv;
+    r32[t] = act ? (float)rv : 0.0f;
+    acc += rv * rv;
+  }
+  block_partial<KB>(acc, partial);
+}
+
+template <int KB>
+__global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total, double *__restrict__ x64,
+                                                       const float *__restrict__ d32) {
+  for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < total; t += (long long)gridDim.x * TPB)
+    x64[t] += (double)d32[t];
+}
+
+// ---------------------------------------------------------------- PCG scalars
+// Partials layout: [nb][gx][KB]; RHS r = b*KB + l.
+__device__ __forceinline__ double sum_partial(const double *p, int gx, int KB, int r) {
+  const int b = r / KB, l = r % KB;
+  const double *q = p + (long long)b * gx * KB + l;
+  double s = 0.0;
+  for (int i = 0; i < gx; ++i) s += q[(long long)i * KB];
+  return s;
+}
+
+__global__ void k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
+                            const double *__restrict__ rz, const int *__restrict__ active,
+                            double *__restrict__ alpha, int *__restrict__ status) {
+  for (int r = threadIdx.x; r < K; r += blockDim.x) {
+    double pq = sum_partial(part_pq, gx, KB, r);
+    double a = 0.0;
+    if (active[r]) {
+      if (!(pq > 0.0) || !isfinite(pq)) {
+        atomicOr(status, 4);  // breakdown / non-finite
+      } else {
+        a = rz[r] / pq;
+      }
+    }
+    alpha[r] = a;
+  }
+}
+
+// rz_new = r.z ; rr = |r|^2 ; active &= rr > tol2*bb ; beta = rz_new/rz_old ; counts active
+__global__ void k_pcg_beta(int K, int KB, int gx, const double *__restrict__ part_rz,
+                           const double *__restrict__ part_rr, double *__restrict__ rz,
+                           double *__restrict__ rr_out, const double *__restrict__ bb, double tol2,
+                           int *__restrict__ active, double *__restrict__ beta, int *__restrict__ n_active,
+                           int first) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int r = threadIdx.x; r < K; r += blockDim.x) {
+    double rzn = sum_partial(part_rz, gx, KB, r);
+    double rr = sum_partial(part_rr, gx, KB, r);
+    rr_out[r] = rr;
+    int act = active[r];
+    if (act && !(rr > tol2 * bb[r])) act = 0;
+    if (act && !isfinite(rr)) act = 0;
+    double bt = 0.0;
+    if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
+    if (act) rz[r] = rzn;
+    beta[r] = first ? 0.0 : bt;
+    active[r] = act;
+    mine += act;
+  }
+  atomicAdd(&cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) *n_active = cnt;
+}
+
+// per-RHS sums of partials into out (used for |b|^2 and the outer residual norms)
+__global__ void k_sum_partials(int K, int KB, int gx, const double *__restrict__ part, double *__restrict__ out) {
+  for (int r = threadIdx.x; r < K; r += blockDim.x) out[r] = sum_partial(part, gx, KB, r);
+}
+
+// outer (refinement) convergence: active = rr > tol2*bb ; counts
+__global__ void k_outer_check(int K, const double *__restrict__ rr, const double *__restrict__ bb, double tol2,
+                              int *__restrict__ active, int *__restrict__ n_active, double *__restrict__ maxrel) {
+  __shared__ int cnt;
+  __shared__ double mx[1024];
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int mine = 0;
+  double m = 0.0;
+  for (int r = threadIdx.x; r < K; r += blockDim.x) {
+    int act = (bb[r] > 0.0) && (rr[r] > tol2 * bb[r]);
+    if (!isfinite(rr[r])) act = 0;
+    active[r] = act;
+    mine += act;
+    if (bb[r] > 0.0) m = fmax(m, sqrt(rr[r] / bb[r]));
+  }
+  atomicAdd(&cnt, mine);
+  mx[threadIdx.x] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int i = 0; i < blockDim.x; ++i) v = fmax(v, mx[i]);
+    *n_active = cnt;
+    *maxrel = v;
+  }
+}
+
+// ---------------------------------------------------------------- coefficients
+__device__ __forceinline__ double sig(const double *s, int nx, int ny, int i, int j, int k) {
+  return s[i + (long long)nx * (j + (long long)ny * k)];
+}
+
+// Coupling of the x-edge (i -> i+1) at node row (j, k): sum over the <= 4 cells
+// (i, j', k') of sigma * hy * hz / (4 hx_i).  Same pattern for y, z.
+__device__ double cpl_x(const double *s, const double *hx, const double *hy, const double *hz, int nx, int ny,
+                        int nz, int i, int j, int k) {
+  double acc = 0.0;
+  for (int b = k - 1; b <= k; ++b) {
+    if (b < 0 || b >= nz) continue;
+    for (int a = j - 1; a <= j; ++a) {
+      if (a < 0 || a >= ny) continue;
+      acc += sig(s, nx, ny, i, a, b) * hy[a] * hz[b];
+    }
+  }
+  return acc / (4.0 * hx[i]);
+}
+__device__ double cpl_y(const double *s, const double *hx, const double *hy, const double *hz, int nx, int ny,
+                        int nz, int i, int j, int k) {
+  double acc = 0.0;
+  for (int b = k - 1; b <= k; ++b) {
+    if (b < 0 || b >= nz) continue;
+    for (int a = i - 1; a <= i; ++a) {
+      if (a < 0 || a >= nx) continue;
+      acc += sig(s, nx, ny, a, j, b) * hx[a] * hz[b];
+    }
+  }
+  return acc / (4.0 * hy[j]);
+}
+__device__ double cpl_z(const double *s, const double *hx, const double *hy, const double *hz, int nx, int ny,
+                        int nz, int i, int j, int k) {
+  double acc = 0.0;
+  for (int b = j - 1; b <= j; ++b) {
+    if (b < 0 || b >= ny) continue;
+    for (int a = i - 1; a <= i; ++a) {
+      if (a < 0 || a >= nx) continue;
+      acc += sig(s, nx, ny, a, b, k) * hx[a] * hy[b];
+    }
+  }
+  return acc / (4.0 * hz[k]);
+}
+
+struct BFace {
+  const double *v;     // 0.25*alpha*area, sides packed
+  long long off[6];    // xlo, xhi, ylo, yhi, zlo, zhi
+};
+
+// Robin diagonal of node (i,j,k): sum over boundary faces f touching the node of bface_f * sigma(cell(f)).
+__device__ double robin_at(const double *s, BFace bf, int nx, int ny, int nz, int i, int j, int k) {
+  double acc = 0.0;
+  if (i == 0 || i == nx) {
+    const double *v = bf.v + bf.off[i == 0 ? 0 : 1];
+    const int ci = (i == 0) ? 0 : nx - 1;
+    for (int b = k - 1; b <= k; ++b) {
+      if (b < 0 || b >= nz) continue;
+      for (int a = j - 1; a <= j; ++a) {
+        if (a < 0 || a >= ny) continue;
+        acc += v[a + (long long)ny * b] * sig(s, nx, ny, ci, a, b);
+      }
+    }
+  }
+  if (j == 0 || j == ny) {
+    const double *v = bf.v + bf.off[j == 0 ? 2 : 3];
+    const int cj = (j == 0) ? 0 : ny - 1;
+    for (int b = k - 1; b <= k; ++b) {
+      if (b < 0 || b >= nz) continue;
+      for (int a = i - 1; a <= i; ++a) {
+        if (a < 0 || a >= nx) continue;
+        acc += v[a + (long long)nx * b] * sig(s, nx, ny, a, cj, b);
+      }
+    }
+  }
+  if (k == 0 || k == nz) {
+    const double *v = bf.v + bf.off[k == 0 ? 4 : 5];
+    const int ck = (k == 0) ? 0 : nz - 1;
+    for (int b = j - 1; b <= j; ++b) {
+      if (b < 0 || b >= ny) continue;
+      for (int a = i - 1; a <= i; ++a) {
+        if (a < 0 || a >= nx) continue;
+        acc += v[a + (long long)nx * b] * sig(s, nx, ny, a, b, ck);
+      }
+    }
+  }
+  return acc;
+}
+
+__global__ void k_coef_build(const double *__restrict__ s, const double *__restrict__ h, int nx, int ny, int nz,
+                             BFace bf, int robin, Coef64 *__restrict__ c64, Coef32 *__restrict__ c32,
+                             double *__restrict__ invd64, float *__restrict__ invd32,
+                             unsigned long long *__restrict__ lmax_bits) {
+  const double *hx = h, *hy = h + nx, *hz = h + nx + ny;
+  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
+  const long long N = (long long)Nx * Ny * Nz;
+  double gmax = 0.0;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(n / ((long long)Nx * Ny));
+    const int r = (int)(n - (long long)k * Nx * Ny);
+    const int j = r / Nx, i = r - j * Nx;
+    const double cxp = (i < nx) ? cpl_x(s, hx, hy, hz, nx, ny, nz, i, j, k) : 0.0;
+    const double cxm = (i > 0) ? cpl_x(s, hx, hy, hz, nx, ny, nz, i - 1, j, k) : 0.0;
+    const double cyp = (j < ny) ? cpl_y(s, hx, hy, hz, nx, ny, nz, i, j, k) : 0.0;
+    const double cym = (j > 0) ? cpl_y(s, hx, hy, hz, nx, ny, nz, i, j - 1, k) : 0.0;
+    const double czp = (k < nz) ? cpl_z(s, hx, hy, hz, nx, ny, nz, i, j, k) : 0.0;
+    const double czm = (k > 0) ? cpl_z(s, hx, hy, hz, nx, ny, nz, i, j, k - 1) : 0.0;
+    const double off = cxp + cxm + cyp + cym + czp + czm;
+    const double rb = robin ? robin_at(s, bf, nx, ny, nz, i, j, k) : 0.0;
+    const double dg = off + rb;
+    Coef64 c;
+    c.cx = cxp; c.cy = cyp; c.cz = czp; c.d = dg;
+    c64[n] = c;
+    Coef32 f;
+    f.cx = (float)cxp; f.cy = (float)cyp; f.cz = (float)czp; f.d = (float)dg;
+    c32[n] = f;
+    const double id = dg > 0.0 ? 1.0 / dg : 0.0;
+    invd64[n] = id;
+    invd32[n] = (float)id;
+    if (dg > 0.0) gmax = fmax(gmax, 1.0 + off / dg);
+  }
+  // positive doubles order like their bit patterns
+  for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(gmax));
+}
+
+// sigma_c = sum(sigma_f V_f) / sum(V_f) over the fine cells of each coarse cell.
+__global__ void k_coarsen_sigma(const double *__restrict__ sf, const double *__restrict__ hf, int fnx, int fny, int fnz,
+                                double *__restrict__ sc, int cnx, int cny, int cnz, const int *__restrict__ fi,
+                                long long o0, long long o1, long long o2) {
+  const double *hx = hf, *hy = hf + fnx, *hz = hf + fnx + fny;
+  const long long nC = (long long)cnx * cny * cnz;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(c / ((long long)cnx * cny));
+    const int r = (int)(c - (long long)K * cnx * cny);
+    const int J = r / cnx, I = r - J * cnx;
+    double sv = 0.0, vv = 0.0;
+    for (int k = fi[o2 + K]; k < fi[o2 + K + 1]; ++k)
+      for (int j = fi[o1 + J]; j < fi[o1 + J + 1]; ++j)
+        for (int i = fi[o0 + I]; i < fi[o0 + I + 1]; ++i) {
+          const double v = hx[i] * hy[j] * hz[k];
+          sv += sf[i + (long long)fnx * (j + (long long)fny * k)] * v;
+          vv += v;
+        }
+    sc[c] = sv / vv;
+  }
+}
+
+// ---------------------------------------------------------------- coarsest level
+__global__ void k_dense_assemble(const Coef64 *__restrict__ coef, Dims d, double *__restrict__ A) {
+  const int N = (int)d.N;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    double *row = A + (long long)n * N;
+    const Coef64 c = coef[n];
+    row[n] = c.d;
+    if (i + 1 < d.Nx) row[n + 1] = -c.cx;
+    if (i > 0) row[n - 1] = -coef[n - 1].cx;
+    if (j + 1 < d.Ny) row[n + d.Nx] = -c.cy;
+    if (j > 0) row[n - d.Nx] = -coef[n - d.Nx].cy;
+    if (k + 1 < d.Nz) row[n + d.Nx * d.Ny] = -c.cz;
+    if (k > 0) row[n - d.Nx * d.Ny] = -coef[n - d.Nx * d.Ny].cz;
+  }
+}
+
+// In-place right-looking Cholesky (lower) of a dense SPD matrix, one CTA.
+__global__ void __launch_bounds__(1024) k_cholesky(double *__restrict__ A, int n, int *__restrict__ flag) {
+  __shared__ double piv;
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      double a = A[(long long)k * n + k];
+      if (!(a > 0.0)) {
+        atomicOr(flag, 1);
+        a = 1.0;
+      }
+      piv = sqrt(a);
+      A[(long long)k * n + k] = piv;
+    }
+    __syncthreads();
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * n + k] /= piv;
+    __syncthreads();
+    const int m = n - k - 1;
+    const long long tot = (long long)m * m;
+    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int ii = k + 1 + (int)(e / m), jj = k + 1 + (int)(e % m);
+      if (jj <= ii) A[(long long)ii * n + jj] -= A[(long long)ii * n + k] * A[(long long)jj * n + k];
+    }
+    __syncthreads();
+  }
+}
+
+// Column j of A^-1 = L^-T L^-1 e_j, one thread per column; writes row-major (symmetric).
+__global__ void k_chol_inverse(const double *__restrict__ L, int n, double *__restrict__ work,
+                               double *__restrict__ Ainv64, float *__restrict__ Ainv32) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double *y = work + (long long)j * n;
+  for (int i = 0; i < n; ++i) y[i] = 0.0;
+  // forward: L y = e_j
+  for (int i = j; i < n; ++i) {
+    double s = (i == j) ? 1.0 : 0.0;
+    for (int m = j; m < i; ++m) s -= L[(long long)i * n + m] * y[m];
+    y[i] = s / L[(long long)i * n + i];
+  }
+  // back: L^T x = y
+  for (int i = n - 1; i >= 0; --i) {
+    double s = y[i];
+    for (int m = i + 1; m < n; ++m) s -= L[(long long)m * n + i] * y[m];
+    y[i] = s / L[(long long)i * n + i];
+  }
+  for (int i = 0; i < n; ++i) {
+    Ainv64[(long long)i * n + j] = y[i];
+    Ainv32[(long long)i * n + j] = (float)y[i];
+  }
+}
+
+// ---------------------------------------------------------------- layout conversion
+template <typename T>
+__global__ void k_pack(const double *__restrict__ src, long long N, int K, int KB, T *__restrict__ dst,
+                       long long total) {
+  // dst element t -> (b, n, l); rhs r = b*KB + l; src[r*N + n]
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int l = (int)(t % KB);
+    const long long bn = t / KB;
+    const long long n = bn % N;
+    const int r = (int)(bn / N) * KB + l;
+    dst[t] = (r < K) ? (T)src[(long long)r * N + n] : (T)0;
+  }
+}
+
+template <typename T>
+__global__ void k_unpack(const T *__restrict__ src, long long N, int K, int KB, double *__restrict__ dst) {
+  const long long total = N * K;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / N);
+    const long long n = e - (long long)r * N;
+    dst[e] = (double)src[((long long)(r / KB) * N + n) * KB + (r % KB)];
+  }
+}
+
+inline int grid_nodes(long long nodes, int KB, int nb, int n_sm) {
+  const long long npb = TPB / KB;
+  long long g = (nodes + npb - 1) / npb;
+  long long cap = (long long)n_sm * 8 / (nb > 0 ? nb : 1);
+  if (cap < 1) cap = 1;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+inline int grid_flat(long long total, int n_sm) {
+  long long g = (total + TPB - 1) / TPB;
+  long long cap = (long long)n_sm * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+int g_n_sm = 152;
+void set_sm_count(int n) { g_n_sm = n > 0 ? n : 152; }
+
+int node_grid(long long nodes, int KB, int nb) { return grid_nodes(nodes, KB, nb, g_n_sm); }
+
+// ------------------------------------------------------------------ launchers
+template <typename T, int KB>
+void Ops<T, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
+  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
+      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
+  dim3 g(partial ? gx : grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
+  if (partial)
+    k_apply<T, KB, true><<<g, TPB, 0, s>>>(coef, x, y, L.dims, partial);
+  else
+    k_apply<T, KB, false><<<g, TPB, 0, s>>>(coef, x, y, L.dims, nullptr);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s) {
+  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
+      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
+  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
+  k_residual<T, KB><<<g, TPB, 0, s>>>(coef, r, z, res, L.dims);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s) {
+  const T *invd = reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
+                                                                              : (const void *)L.d_invd32);
+  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
+  k_cheb_first<T, KB><<<g, TPB, 0, s>>>(invd, r, z, d, L.dims, (T)c0);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
+                           cudaStream_t s) {
+  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
+      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
+  const T *invd = reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
+                                                                              : (const void *)L.d_invd32);
+  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
+  k_cheb_step<T, KB><<<g, TPB, 0, s>>>(coef, invd, r, zin, zout, d, L.dims, (T)c1, (T)c2);
+}
+
+template <typename T>
+static XferTab make_tab(const Level &f) {
+  XferTab tb;
+  const bool dbl = std::is_same<T, double>::value;
+  tb.fi = f.d_r_fi;
+  tb.wl = dbl ? (const void *)f.d_r_wl : (const void *)f.d_r_wl32;
+  tb.wr = dbl ? (const void *)f.d_r_wr : (const void *)f.d_r_wr32;
+  tb.pl = f.d_pl_idx;
+  tb.pw = dbl ? (const void *)f.d_pl_w : (const void *)f.d_pl_w32;
+  for (int a = 0; a < 3; ++a) {
+    tb.roff[a] = f.r_off[a];
+    tb.poff[a] = f.pl_off[a];
+  }
+  return tb;
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s) {
+  dim3 g(grid_nodes(c.dims.N, KB, nb, g_n_sm), nb);
+  k_restrict<T, KB><<<g, TPB, 0, s>>>(res, rc, f.dims, c.dims, make_tab<T>(f));
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s) {
+  dim3 g(grid_nodes(f.dims.N, KB, nb, g_n_sm), nb);
+  k_prolong_add<T, KB><<<g, TPB, 0, s>>>(zc, z, f.dims, c.dims, make_tab<T>(f));
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s) {
+  dim3 g(grid_nodes(nc, KB, nb, g_n_sm), nb);
+  k_coarse_solve<T, KB><<<g, TPB, 0, s>>>(Ainv, nc, rc, zc);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
+                           double *partial, int gx, cudaStream_t s) {
+  k_update_xr<T, KB><<<dim3(gx, nb), TPB, 0, s>>>(N, x, r, p, q, alpha, partial);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s) {
+  k_dot<T, KB><<<dim3(gx, nb), TPB, 0, s>>>(N, a, b, partial);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s) {
+  k_p_update<T, KB><<<dim3(grid_nodes(N, KB, nb, g_n_sm), nb), TPB, 0, s>>>(N, p, z, beta);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::copy(long long N, int nb, T *dst, const T *src, cudaStream_t s) {
+  cudaMemcpyAsync(dst, src, sizeof(T) * N * KB * nb, cudaMemcpyDeviceToDevice, s);
+}
+
+template <int KB>
+void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
+                 const int *active, double *partial, int gx, cudaStream_t s) {
+  k_ir_residual<KB><<<dim3(gx, nb), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, active, partial);
+}
+
+template <int KB>
+void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s) {
+  const long long total = N * KB * nb;
+  k_ir_accumulate<KB><<<grid_flat(total, g_n_sm), TPB, 0, s>>>(total, x64, d32);
+}
+
+void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
+               int *status, cudaStream_t s) {
+  k_pcg_alpha<<<1, 1024, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status);
+}
+
+void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
+              const double *bb, double tol2, int *active, double *beta, int *n_active, int first, cudaStream_t s) {
+  k_pcg_beta<<<1, 1024, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta, n_active, first);
+}
+
+void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s) {
+  k_sum_partials<<<1, 1024, 0, s>>>(K, KB, gx, part, out);
+}
+
+void outer_check(int K, const double *rr, const double *bb, double tol2, int *active, int *n_active,
+                 double *maxrel, cudaStream_t s) {
+  k_outer_check<<<1, 1024, 0, s>>>(K, rr, bb, tol2, active, n_active, maxrel);
+}
+
+void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s) {
+  BFace bf;
+  bf.v = L.d_bface;
+  for (int a = 0; a < 6; ++a) bf.off[a] = L.bface_off[a];
+  k_coef_build<<<grid_flat(L.dims.N, g_n_sm), TPB, 0, s>>>(L.d_sigma, L.d_h, L.nx, L.ny, L.nz, bf, robin,
+                                                            L.d_coef64, L.d_coef32, L.d_invd64, L.d_invd32,
+                                                            d_lmax_bits);
+}
+
+void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s) {
+  const long long nC = (long long)c.nx * c.ny * c.nz;
+  k_coarsen_sigma<<<grid_flat(nC, g_n_sm), TPB, 0, s>>>(f.d_sigma, f.d_h, f.nx, f.ny, f.nz, c.d_sigma, c.nx, c.ny,
+                                                         c.nz, f.d_r_fi, f.r_off[0], f.r_off[1], f.r_off[2]);
+}
+
+void dense_assemble(const Level &L, double *dense, cudaStream_t s) {
+  cudaMemsetAsync(dense, 0, sizeof(double) * L.dims.N * L.dims.N, s);
+  k_dense_assemble<<<grid_flat(L.dims.N, g_n_sm), TPB, 0, s>>>(L.d_coef64, L.dims, dense);
+}
+
+void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, float *Ainv32, int *flag,
+                            cudaStream_t s) {
+  k_cholesky<<<1, 1024, 0, s>>>(dense, n, flag);
+  k_chol_inverse<<<(n + 31) / 32, 32, 0, s>>>(dense, n, work, Ainv64, Ainv32);
+}
+
+template <typename T>
+void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s) {
+  const long long total = N * (long long)KB * nb;
+  k_pack<T><<<grid_flat(total, g_n_sm), TPB, 0, s>>>(src, N, K, KB, dst, total);
+}
+
+template <typename T>
+void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s) {
+  k_unpack<T><<<grid_flat(N * K, g_n_sm), TPB, 0, s>>>(src, N, K, KB, dst);
+}
+
+#define DC_INST(T, KB) template struct Ops<T, KB>;
+DC_INST(float, 1) DC_INST(float, 2) DC_INST(float, 4) DC_INST(float, 8) DC_INST(float, 16) DC_INST(float, 32)
+DC_INST(double, 1) DC_INST(double, 2) DC_INST(double, 4) DC_INST(double, 8) DC_INST(double, 16) DC_INST(double, 32)
+#undef DC_INST
+#define DC_INST_IR(KB)                                                                                       \
+  template void ir_residual<KB>(const Level &, const double *, const double *, double *, float *, int,      \
+                                const int *, double *, int, cudaStream_t);                                  \
+  template void ir_accumulate<KB>(long long, int, double *, const float *, cudaStream_t);
+DC_INST_IR(1) DC_INST_IR(2) DC_INST_IR(4) DC_INST_IR(8) DC_INST_IR(16) DC_INST_IR(32)
+#undef DC_INST_IR
+template void pack_colmajor<float>(const double *, long long, int, int, int, float *, cudaStream_t);
+template void pack_colmajor<double>(const double *, long long, int, int, int, double *, cudaStream_t);
+template void unpack_colmajor<float>(const float *, long long, int, int, double *, cudaStream_t);
+template void unpack_colmajor<double>(const double *, long long, int, int, double *, cudaStream_t);
+
+}  // namespace dc

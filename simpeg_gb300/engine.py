@@ -1,0 +1,186 @@
+"""Python handle over the CUDA nodal-DC engine (``include/dcgpu.h``).
+
+Device memory is torch-owned: every array passed in is a CUDA ``torch.Tensor``
+(float64, contiguous).  Multi-RHS arrays have shape ``(k, nN)`` -- i.e. the
+column-major ``(nN, k)`` layout of simpeg's ``Fields`` store.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+
+MODES = {"fp64": _lib.DC_MODE_FP64, "mixed": _lib.DC_MODE_MIXED}
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _dev64(t, shape=None, name="array"):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch tensor")
+    if not t.is_cuda or t.dtype != torch.float64:
+        raise TypeError(f"{name} must be a CUDA float64 tensor")
+    if not t.is_contiguous():
+        t = t.contiguous()
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    return t
+
+
+class SolveInfo:
+    def __init__(self, st):
+        self.iterations = st.iterations
+        self.outer = st.outer
+        self.status = st.status
+        self.n_levels = st.n_levels
+        self.max_rel_res = st.max_rel_res
+
+    def __repr__(self):
+        return (f"SolveInfo(iterations={self.iterations}, outer={self.outer}, status={self.status}, "
+                f"levels={self.n_levels}, max_rel_res={self.max_rel_res:.3e})")
+
+
+class DCEngine:
+    """One mesh + boundary condition on the GPU; model-dependent state after :meth:`set_model`.
+
+    Parameters
+    ----------
+    h : three arrays of cell widths (nx, ny, nz)
+    bface : packed Robin face weights (``boundary.robin_face_weights``) or None (Neumann)
+    """
+
+    def __init__(self, h, bface=None, nu_pre=2, nu_post=2, cheb_ratio=6.0, coarse_max=600, check_every=1):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the DC engine needs a CUDA device")
+        L = lib()
+        hx, hy, hz = [np.ascontiguousarray(w, dtype=np.float64) for w in h]
+        self.shape_cells = (hx.size, hy.size, hz.size)
+        self.nN = (hx.size + 1) * (hy.size + 1) * (hz.size + 1)
+        self.nC = hx.size * hy.size * hz.size
+        dp = C.POINTER(C.c_double)
+        bf = None
+        if bface is not None:
+            bf = np.ascontiguousarray(bface, dtype=np.float64)
+            nx, ny, nz = self.shape_cells
+            if bf.size != 2 * (ny * nz + nx * nz + nx * ny):
+                raise ValueError("bface has the wrong length")
+        self._h = C.c_void_p()
+        check(L.dc_create(hx.size, hy.size, hz.size, hx.ctypes.data_as(dp), hy.ctypes.data_as(dp),
+                          hz.ctypes.data_as(dp), bf.ctypes.data_as(dp) if bf is not None else None,
+                          C.byref(self._h)))
+        check(L.dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
+        self.robin = bface is not None
+        self._ws = {}
+        self._model_set = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().dc_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    # ------------------------------------------------------------------
+    def set_params(self, nu_pre=0, nu_post=0, cheb_ratio=0.0, coarse_max=0, check_every=0):
+        check(lib().dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
+
+    def set_model(self, sigma):
+        sigma = _dev64(sigma, (self.nC,), "sigma")
+        check(lib().dc_set_model(self._h, _ptr(sigma), _stream()))
+        self._model_set = True
+
+    def levels(self):
+        n = C.c_int()
+        out = []
+        nodes = C.c_longlong()
+        cells = (C.c_int * 3)()
+        check(lib().dc_level_info(self._h, 0, C.byref(n), C.byref(nodes), cells))
+        for l in range(n.value):
+            check(lib().dc_level_info(self._h, l, None, C.byref(nodes), cells))
+            out.append((tuple(cells), nodes.value))
+        return out
+
+    def apply(self, x):
+        x = _dev64(x, None, "x")
+        x2 = x.reshape(-1, self.nN)
+        y = torch.empty_like(x2)
+        check(lib().dc_apply(self._h, _ptr(x2), _ptr(y), x2.shape[0], _stream()))
+        return y.reshape(x.shape)
+
+    def workspace_bytes(self, k, mode="mixed"):
+        b = C.c_size_t()
+        check(lib().dc_solve_workspace_bytes(self._h, MODES[mode], int(k), C.byref(b)))
+        return b.value
+
+    def solve(self, b, mode="mixed", rtol=1e-9, maxit=2000, inner_rtol=1e-4, inner_maxit=200, ws=None,
+              raise_on_fail=True):
+        """x = A^-1 b for b of shape (k, nN) or (nN,). Returns (x, SolveInfo)."""
+        b = _dev64(b, None, "b")
+        b2 = b.reshape(-1, self.nN)
+        k = b2.shape[0]
+        x = torch.empty_like(b2)
+        st = _lib.dc_stats()
+        if ws is None:
+            need = self.workspace_bytes(k, mode)
+            key = (mode,)
+            cur = self._ws.get(key)
+            if cur is None or cur.numel() < need:
+                self._ws[key] = cur = torch.empty(need, dtype=torch.uint8, device=b.device)
+            ws = cur
+        rc = lib().dc_solve(self._h, MODES[mode], _ptr(b2), _ptr(x), k, float(rtol), int(maxit), float(inner_rtol),
+                            int(inner_maxit), _ptr(ws), ws.numel(), C.byref(st), _stream())
+        info = SolveInfo(st)
+        if rc != 0 and (raise_on_fail or rc != _lib.DC_ERR_NOT_CONVERGED):
+            check(rc)
+        return x.reshape(b.shape), info
+
+    def release_workspace(self):
+        self._ws.clear()
+
+    def dadm_fwd(self, u, dsig, scale=1.0):
+        u = _dev64(u, None, "u")
+        u2 = u.reshape(-1, self.nN)
+        dsig = _dev64(dsig, (self.nC,), "dsig")
+        out = torch.empty_like(u2)
+        check(lib().dc_dadm_fwd(self._h, _ptr(u2), _ptr(dsig), _ptr(out), u2.shape[0], float(scale), _stream()))
+        return out.reshape(u.shape)
+
+    def dadm_adj(self, u, lam, dsig=None, scale=1.0):
+        u = _dev64(u, None, "u").reshape(-1, self.nN)
+        lam = _dev64(lam, None, "lam").reshape(-1, self.nN)
+        if u.shape != lam.shape:
+            raise ValueError("u and lam must have the same shape")
+        if dsig is not None:
+            dsig = _dev64(dsig, (self.nC,), "dsig")
+        g = torch.empty(self.nC, dtype=torch.float64, device=u.device)
+        check(lib().dc_dadm_adj(self._h, _ptr(u), _ptr(lam), u.shape[0], _ptr(dsig), float(scale), _ptr(g),
+                                _stream()))
+        return g
+
+
+def csr_spmv(rowptr, idx, w, x, y, out_idx=None, scale=1.0, accumulate=False):
+    nrows = rowptr.numel() - 1
+    check(lib().dc_csr_spmv(nrows, _ptr(rowptr), _ptr(idx), _ptr(w), _ptr(x), _ptr(out_idx), _ptr(y), float(scale),
+                            int(bool(accumulate)), _stream()))
+    return y
+
+
+def fill_sparse(idx, val, y):
+    check(lib().dc_fill_sparse(idx.numel(), _ptr(idx), _ptr(val), _ptr(y), _stream()))
+    return y

@@ -1,0 +1,151 @@
+"""DC receivers: potential (Pole) and potential-difference (Dipole) data.
+
+Mirrors ``simpeg/electromagnetics/static/resistivity/receivers.py``:
+``BaseRx.eval``/``evalDeriv`` (``:156-244``) project the nodal potential with
+``P`` (``Dipole.getP`` = interp(M) - interp(N), ``:379-424``; ``Pole.getP`` =
+interp(M), ``:461-498``) and divide by the geometric factor for
+``data_type="apparent_resistivity"``.  On the GPU path ``P`` is never formed;
+the projection is an electrode gather (see ``electrodes.py``).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = ["BaseRx", "Pole", "Dipole"]
+
+_VOLT = ("volt", "potential", "potentials", "v", "voltage", "voltages")
+_APPRES = (
+    "apparent_resistivity",
+    "apparent resistivity",
+    "appresistivity",
+    "apparentresistivity",
+    "apparent-resistivity",
+)
+_APPCHG = (
+    "apparent_chargeability",
+    "apparent chargeability",
+    "appchargeability",
+    "apparentchargeability",
+    "apparent-chargeability",
+)
+
+
+def _loc2d(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        a = a[None, :]
+    if a.ndim != 2:
+        raise ValueError("locations must be (n, dim)")
+    return a
+
+
+class BaseRx:
+    def __init__(self, locations, data_type="volt", orientation=None, projField="phi",
+                 storeProjections=False):
+        self.locations = locations
+        self.data_type = data_type
+        if orientation is not None:
+            raise NotImplementedError("only potential (phi) receivers are on the GPU path")
+        self.orientation = None
+        if projField != "phi":
+            raise NotImplementedError("only projField='phi' is on the GPU path")
+        self.projField = "phi"
+        self.storeProjections = storeProjections
+        self._geometric_factor = {}
+
+    @property
+    def data_type(self):
+        return self._data_type
+
+    @data_type.setter
+    def data_type(self, var):
+        v = str(var).lower()
+        if v in _VOLT:
+            self._data_type = "volt"
+        elif v in _APPRES:
+            self._data_type = "apparent_resistivity"
+        elif v in _APPCHG:
+            self._data_type = "apparent_chargeability"
+        else:
+            raise ValueError(f"data_type {var!r} not in volt / apparent_resistivity / apparent_chargeability")
+
+    @property
+    def geometric_factor(self):
+        return self._geometric_factor
+
+
+class Pole(BaseRx):
+    """Potential at electrode M."""
+
+    def __init__(self, locations, **kwargs):
+        super().__init__(locations=locations, **kwargs)
+
+    @property
+    def locations(self):
+        return self._locations
+
+    @locations.setter
+    def locations(self, value):
+        self._locations = _loc2d(value)
+
+    @property
+    def nD(self):
+        return self._locations.shape[0]
+
+    @property
+    def locations_m(self):
+        return self._locations
+
+    @property
+    def locations_n(self):
+        return None
+
+
+class Dipole(BaseRx):
+    """Potential difference between electrodes M and N."""
+
+    def __init__(self, locations_m=None, locations_n=None, locations=None, **kwargs):
+        if locations_m is not None or locations_n is not None:
+            if locations_n is None or locations_m is None:
+                raise ValueError("For a dipole receiver both locations_m and locations_n must be set")
+            if locations is not None:
+                raise ValueError(
+                    "Cannot set both locations and locations_m, locations_n. Please provide "
+                    "either locations=(locations_m, locations_n) or both locations_m, locations_n"
+                )
+            locations = [locations_m, locations_n]
+        if locations is None:
+            raise AttributeError("Receiver cannot be instantiated without assigning 'locations'.")
+        kwargs.pop("threshold", None)
+        super().__init__(locations=locations, **kwargs)
+
+    @property
+    def locations(self):
+        return self._locations
+
+    @locations.setter
+    def locations(self, locs):
+        if len(locs) != 2:
+            raise ValueError(
+                "locations must be a list or tuple of length 2: [locations_m, locations_n]. "
+                f"The input locations has length {len(locs)}"
+            )
+        m, n = _loc2d(locs[0]), _loc2d(locs[1])
+        if m.shape != n.shape:
+            raise ValueError(
+                f"locations_m (shape: {m.shape}) and locations_n (shape: {n.shape}) need to be the same size"
+            )
+        self._locations = [m, n]
+
+    @property
+    def locations_m(self):
+        return self._locations[0]
+
+    @property
+    def locations_n(self):
+        return self._locations[1]
+
+    @property
+    def nD(self):
+        return self._locations[0].shape[0]

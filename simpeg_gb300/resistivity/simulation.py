@@ -1,0 +1,389 @@
+"""GPU ``Simulation3DNodal``: simpeg's nodal DC forward/sensitivity API on the CUDA engine.
+
+Drop-in for ``simpeg.electromagnetics.static.resistivity.Simulation3DNodal``
+(``simpeg/electromagnetics/static/resistivity/simulation.py:20-319,483-670``):
+same constructor arguments, same ``fields / dpred / Jvec / Jtvec / getJ /
+getJtJdiag`` signatures and data ordering.  The difference is underneath: A
+is never assembled or factored; every solve is one multi-RHS call of the
+matrix-free multigrid-PCG engine (``include/dcgpu.h``), sources and receivers
+are GPU gathers/scatters of precomputed electrode tables, and ``getADeriv``
+is a stencil (forward) or an edge-product reduction (adjoint) kernel.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from ..engine import DCEngine, csr_spmv, fill_sparse
+from ..maps import IdentityMap, ReciprocalMap, ComboMap
+from .boundary import robin_face_weights
+from .electrodes import SurveyTables
+from .fields import Fields3DNodal
+from .survey import Survey
+from .utils import mini_pole_pole
+
+__all__ = ["Simulation3DNodal"]
+
+
+def _is_tensor_mesh(mesh):
+    return hasattr(mesh, "h") and len(mesh.h) == 3 and hasattr(mesh, "origin")
+
+
+class Simulation3DNodal:
+    """3D nodal DC problem on a tensor mesh, solved on the GPU.
+
+    Extra keyword arguments (not in the reference) select the arithmetic:
+    ``precision`` ("mixed": fp32 multigrid-PCG inner solves wrapped in fp64
+    iterative refinement; "fp64": plain fp64 multigrid-PCG), ``rtol`` (relative
+    residual of every solve, default 1e-10) and ``device``.
+    """
+
+    _solutionType = "phiSolution"
+    _formulation = "EB"
+
+    def __init__(self, mesh, survey=None, bc_type="Robin", sigma=None, sigmaMap=None, rho=None, rhoMap=None,
+                 solver=None, solver_opts=None, storeJ=False, miniaturize=False, surface_faces=None,
+                 precision="mixed", rtol=1e-10, maxit=5000, device=None, engine_opts=None, verbose=False,
+                 counter=None, **kwargs):
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {sorted(kwargs)}")
+        if not _is_tensor_mesh(mesh):
+            raise NotImplementedError("the GPU nodal simulation supports 3D tensor meshes only")
+        if getattr(mesh, "_meshType", "TENSOR").upper() != "TENSOR":
+            raise NotImplementedError(f"mesh type {mesh._meshType} is not supported")
+        self.mesh = mesh
+        self.survey = survey
+        self.storeJ = bool(storeJ)
+        self.verbose = verbose
+        self.counter = counter
+        self.solver = solver
+        self.solver_opts = {} if solver_opts is None else dict(solver_opts)
+        if bc_type == "Mixed":
+            bc_type = "Robin"
+        if bc_type == "Dirichlet":
+            raise ValueError("Dirichlet conditions are not supported in the Nodal formulation")
+        if bc_type not in ("Robin", "Neumann"):
+            raise ValueError(f"bc_type must be Neumann, Robin or Mixed, not {bc_type!r}")
+        if bc_type == "Neumann":
+            raise NotImplementedError(
+                "Neumann (row-0 pinned, non-symmetric) A is not supported by the GPU PCG path; use Robin")
+        self.bc_type = bc_type
+        self.surface_faces = surface_faces
+        if precision not in ("mixed", "fp64"):
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        self.precision = precision
+        self.rtol = float(self.solver_opts.get("rtol", rtol))
+        self.maxit = int(self.solver_opts.get("maxiter", maxit))
+        self.device = torch.device(device if device is not None else "cuda")
+        # physical property / map (props.Invertible + Reciprocal semantics)
+        self._sigma = None if sigma is None else np.asarray(sigma, dtype=np.float64)
+        self._rho = None if rho is None else np.asarray(rho, dtype=np.float64)
+        self.sigmaMap = sigmaMap
+        self.rhoMap = rhoMap
+        self._model = None
+        self._miniaturize = bool(miniaturize)
+        self._mini_survey = None
+        if self._miniaturize:
+            self._dipoles, self._invs, self._mini_survey = mini_pole_pole(self.survey)
+        eo = dict(engine_opts or {})
+        bface = robin_face_weights(mesh, surface_faces)
+        self.engine = DCEngine(mesh.h, bface, **eo)
+        self.nN = self.engine.nN
+        self.nC = self.engine.nC
+        self._tables = None
+        self._clear()
+
+    # ------------------------------------------------------------ properties
+    @property
+    def survey(self):
+        if self._survey is None:
+            raise AttributeError("Simulation must have a survey")
+        return self._survey
+
+    @survey.setter
+    def survey(self, value):
+        self._survey = value
+        self._tables = None
+
+    @property
+    def sigmaMap(self):
+        if self._sigmaMap is not None:
+            return self._sigmaMap
+        if self._rhoMap is not None:
+            return ComboMap([ReciprocalMap(), self._rhoMap])
+        return None
+
+    @sigmaMap.setter
+    def sigmaMap(self, value):
+        self._sigmaMap = value
+
+    @property
+    def rhoMap(self):
+        return self._rhoMap
+
+    @rhoMap.setter
+    def rhoMap(self, value):
+        self._rhoMap = value
+
+    @property
+    def model(self):
+        return self._model
+
+    @model.setter
+    def model(self, m):
+        if m is None:
+            self._model = None
+            self._clear()
+            return
+        m = np.asarray(m, dtype=np.float64).ravel()
+        nP = getattr(self.sigmaMap, "nP", "*") if self.sigmaMap is not None else "*"
+        if isinstance(nP, (int, np.integer)) and m.size != nP:
+            raise ValueError(f"model must have {nP} parameters, got {m.size}")
+        if self._model is not None and self._model.shape == m.shape and np.array_equal(self._model, m):
+            return
+        self._model = m.copy()
+        self._clear()
+
+    def _clear(self):
+        self._sigma_dev = None
+        self._f_cache = None
+        self._Jmatrix = None
+        self._gtgdiag = None
+
+    @property
+    def sigma(self):
+        if self._sigma is not None:
+            return self._sigma
+        if self._rho is not None:
+            return 1.0 / self._rho
+        if self.sigmaMap is None:
+            raise AttributeError("Neither a value nor mapping for sigma/rho has been set")
+        if self._model is None:
+            raise AttributeError("A `model` is required for physical property sigma")
+        return self.sigmaMap * self._model
+
+    @property
+    def rho(self):
+        return 1.0 / self.sigma
+
+    def _sigma_deriv(self):
+        """Diagonal of d sigma / d m as an array, or a sparse matrix for general maps."""
+        mp = self.sigmaMap
+        if mp is None:
+            return None
+        if hasattr(mp, "diag_deriv"):
+            return mp.diag_deriv(self._model)
+        D = mp.deriv(self._model)
+        if sp.issparse(D):
+            D = D.tocsr()
+            if D.shape[0] == D.shape[1] and D.nnz == np.count_nonzero(D.diagonal()):
+                return np.asarray(D.diagonal(), dtype=np.float64)
+        return D
+
+    @property
+    def sigmaDeriv(self):
+        d = self._sigma_deriv()
+        if d is None:
+            return None
+        return sp.diags(d) if isinstance(d, np.ndarray) else d
+
+    def _active_survey(self):
+        return self._mini_survey if self._mini_survey is not None else self.survey
+
+    def _get_tables(self):
+        if self._tables is None:
+            t = SurveyTables(self.mesh, self._active_survey().source_list, self.nN)
+            dev = self.device
+            self._tables = t
+            self._tq = dict(
+                q_idx=torch.from_numpy(t.q_idx).to(dev), q_val=torch.from_numpy(t.q_val).to(dev),
+                P_ptr=torch.from_numpy(t.P_ptr).to(dev), P_idx=torch.from_numpy(t.P_idx).to(dev),
+                P_w=torch.from_numpy(t.P_w).to(dev), PT_ptr=torch.from_numpy(t.PT_ptr).to(dev),
+                PT_idx=torch.from_numpy(t.PT_idx).to(dev), PT_w=torch.from_numpy(t.PT_w).to(dev),
+                PT_out=torch.from_numpy(t.PT_out).to(dev),
+            )
+        return self._tables, self._tq
+
+    # ------------------------------------------------------------ device state
+    def _ensure_model(self):
+        if self._sigma_dev is None:
+            s = self.sigma
+            if s.size != self.nC:
+                raise NotImplementedError(
+                    "Anisotropic conductivity is not supported for Robin boundary conditions")
+            if np.any(~np.isfinite(s)) or np.any(s <= 0):
+                raise ValueError("conductivity must be positive and finite")
+            self._sigma_dev = torch.from_numpy(np.ascontiguousarray(s)).to(self.device)
+            self.engine.set_model(self._sigma_dev)
+        return self._sigma_dev
+
+    def _solve(self, B):
+        X, info = self.engine.solve(B, mode=self.precision, rtol=self.rtol, maxit=self.maxit)
+        self.last_solve_info = info
+        return X
+
+    def getRHS(self):
+        """Source term q as a device tensor (nSrc, nN) == column-major (nN, nSrc)."""
+        t, tq = self._get_tables()
+        Q = torch.zeros(t.nSrc, self.nN, dtype=torch.float64, device=self.device)
+        fill_sparse(tq["q_idx"], tq["q_val"], Q.view(-1))
+        return Q
+
+    getSourceTerm = getRHS
+
+    # ------------------------------------------------------------ forward
+    def fields(self, m=None, calcJ=True):
+        if m is not None:
+            self.model = m
+        self._ensure_model()
+        Q = self.getRHS()
+        U = self._solve(Q)
+        f = Fields3DNodal(self, U)
+        self._f_cache = f
+        return f
+
+    def _gather(self, U):
+        t, tq = self._get_tables()
+        d = torch.empty(t.nD, dtype=torch.float64, device=self.device)
+        csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U.reshape(-1), d)
+        return d
+
+    def dpred(self, m=None, f=None):
+        if f is None:
+            if m is None:
+                m = self.model
+            f = self.fields(m)
+        d = self._gather(f.phi_dev).cpu().numpy()
+        return self._mini_survey_data(d)
+
+    def residual(self, m, dobs, f=None):
+        return self.dpred(m, f=f) - np.asarray(dobs)
+
+    def make_synthetic_data(self, m, relative_error=0.0, noise_floor=0.0, f=None, add_noise=False, random_seed=None):
+        from ..data import SyntheticData
+
+        dclean = self.dpred(m, f=f)
+        dobs = dclean.copy()
+        if add_noise:
+            rng = np.random.default_rng(random_seed)
+            std = np.sqrt((relative_error * np.abs(dclean)) ** 2 + noise_floor ** 2)
+            dobs = dclean + rng.standard_normal(dclean.size) * std
+        return SyntheticData(self.survey, dobs=dobs, dclean=dclean, relative_error=relative_error,
+                             noise_floor=noise_floor)
+
+    # ------------------------------------------------------------ sensitivities
+    def _fields_for(self, m, f):
+        if f is None:
+            if self._f_cache is not None and m is not None and self._model is not None and \
+                    np.array_equal(np.asarray(m, dtype=np.float64).ravel(), self._model):
+                return self._f_cache
+            return self.fields(m)
+        return f
+
+    def _dsig_dev(self, v):
+        d = self._sigma_deriv()
+        v = np.asarray(v, dtype=np.float64).ravel()
+        if d is None:
+            raise AttributeError("a sigmaMap (or rhoMap) is needed for sensitivities")
+        dv = d * v if isinstance(d, np.ndarray) else np.asarray(d @ v).ravel()
+        return torch.from_numpy(np.ascontiguousarray(dv)).to(self.device)
+
+    def Jvec(self, m, v, f=None):
+        f = self._fields_for(m, f)
+        self.model = m
+        self._ensure_model()
+        if self.storeJ:
+            return self.getJ(m, f=f).dot(v)
+        dsig = self._dsig_dev(v)
+        R = self.engine.dadm_fwd(f.phi_dev, dsig, scale=-1.0)
+        dU = self._solve(R)
+        return self._mini_survey_data(self._gather(dU).cpu().numpy())
+
+    def _scatterT(self, v):
+        t, tq = self._get_tables()
+        vd = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(self.device)
+        PTv = torch.zeros(t.nSrc, self.nN, dtype=torch.float64, device=self.device)
+        csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], vd, PTv.view(-1), out_idx=tq["PT_out"])
+        return PTv
+
+    def _map_adjoint(self, g_sigma):
+        d = self._sigma_deriv()
+        if isinstance(d, np.ndarray):
+            return d * g_sigma
+        return np.asarray(d.T @ g_sigma).ravel()
+
+    def Jtvec(self, m, v, f=None):
+        f = self._fields_for(m, f)
+        self.model = m
+        self._ensure_model()
+        if hasattr(v, "dobs"):
+            v = v.dobs
+        if self.storeJ:
+            return np.asarray(self.getJ(m, f=f).T.dot(v))
+        v = self._mini_survey_dataT(np.asarray(v, dtype=np.float64))
+        PTv = self._scatterT(v)
+        Lam = self._solve(PTv)
+        g = self.engine.dadm_adj(f.phi_dev, Lam, None, scale=-1.0).cpu().numpy()
+        return self._map_adjoint(g)
+
+    def getJ(self, m, f=None):
+        """Full sensitivity (nD, nP): one adjoint solve per datum, batched."""
+        self.model = m
+        if self._Jmatrix is not None:
+            return self._Jmatrix
+        f = self._fields_for(m, f)
+        self._ensure_model()
+        t, tq = self._get_tables()
+        nD = t.nD
+        J = np.zeros((nD, self.nC))
+        PT = t.P.T.tocsc()
+        owner = t.owner
+        chunk = max(1, min(nD, 256))
+        for s0 in range(0, nD, chunk):
+            s1 = min(nD, s0 + chunk)
+            cols = PT[:, s0:s1].tocoo()
+            # each datum's P row lives in one source's block: fold to (k, nN)
+            B = np.zeros((s1 - s0, self.nN))
+            np.add.at(B, (cols.col, cols.row % self.nN), cols.data)
+            Lam = self._solve(torch.from_numpy(B).to(self.device))
+            for i in range(s1 - s0):
+                s = int(owner[s0 + i])
+                g = self.engine.dadm_adj(f.phi_dev[s:s + 1], Lam[i:i + 1], None, scale=-1.0)
+                J[s0 + i] = self._map_adjoint(g.cpu().numpy())
+        J = self._mini_J(J)
+        self._Jmatrix = J
+        return J
+
+    def getJtJdiag(self, m, W=None, f=None):
+        if self._gtgdiag is None:
+            J = self.getJ(m, f=f)
+            w = np.ones(J.shape[0]) if W is None else np.asarray(W.diagonal()) ** 2
+            self._gtgdiag = (w[:, None] * J * J).sum(axis=0)
+        return self._gtgdiag
+
+    # ------------------------------------------------------------ miniaturize
+    def _mini_survey_data(self, d_mini):
+        if self._mini_survey is None:
+            return d_mini
+        out = d_mini[self._invs[0]]
+        out[self._dipoles[0]] -= d_mini[self._invs[1]]
+        out[self._dipoles[1]] -= d_mini[self._invs[2]]
+        out[self._dipoles[0] & self._dipoles[1]] += d_mini[self._invs[3]]
+        return out
+
+    def _mini_survey_dataT(self, v):
+        if self._mini_survey is None:
+            return v
+        out = np.zeros(self._mini_survey.nD)
+        np.add.at(out, self._invs[0], v)
+        np.subtract.at(out, self._invs[1], v[self._dipoles[0]])
+        np.subtract.at(out, self._invs[2], v[self._dipoles[1]])
+        np.add.at(out, self._invs[3], v[self._dipoles[0] & self._dipoles[1]])
+        return out
+
+    def _mini_J(self, J):
+        if self._mini_survey is None:
+            return J
+        return self._mini_survey_data(J)

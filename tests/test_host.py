@@ -1,0 +1,187 @@
+"""Host-side logic of the product (no GPU): geometry, electrode tables,
+boundary weights, miniaturisation and the C-ABI library surface."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.dc3d import OracleDC3DNodal
+from oracle.operators import MeshOps
+from simpeg_gb300 import maps
+from simpeg_gb300.mesh import TensorMesh, unpack_widths
+from simpeg_gb300.resistivity import receivers, sources
+from simpeg_gb300.resistivity.boundary import robin_face_weights
+from simpeg_gb300.resistivity.electrodes import SurveyTables, interpolation_matrix
+from simpeg_gb300.resistivity.survey import Survey, geometric_factor
+from simpeg_gb300.resistivity.utils import mini_pole_pole
+from simpeg_gb300.workloads import block_model_survey
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_unpack_widths_padding():
+    w = unpack_widths([(25.0, 3, -1.3), (25.0, 2), (25.0, 2, 1.3)])
+    np.testing.assert_allclose(w, [25 * 1.3**3, 25 * 1.3**2, 25 * 1.3, 25, 25, 25 * 1.3, 25 * 1.3**2])
+    m = TensorMesh([[(10.0, 4)], [(10.0, 2)], [(5.0, 2)]], origin="CCN")
+    np.testing.assert_allclose(m.origin, [-20.0, -10.0, -10.0])
+    assert m.n_nodes == 5 * 3 * 3
+    np.testing.assert_allclose(m.nodes[1], [-10.0, -10.0, -10.0])
+
+
+def _mesh():
+    return TensorMesh([[(5.0, 2, -1.3), (5.0, 6), (5.0, 2, 1.3)], [(5.0, 7)], [(5.0, 2, -1.3), (5.0, 4)]], origin="CCN")
+
+
+@pytest.mark.parametrize("pts", [
+    np.array([[0.0, 0.0, 0.0]]),                      # on a node
+    np.array([[1.3, -2.2, -3.7], [2.5, 2.5, -2.5]]),  # inside cells, on a midpoint
+    None,                                              # last node on each axis
+])
+def test_interpolation_bit_exact_vs_oracle(pts):
+    mesh = _mesh()
+    if pts is None:
+        pts = np.array([[mesh.nodes_x[-1], mesh.nodes_y[-1], mesh.nodes_z[-1]],
+                        [mesh.nodes_x[0], mesh.nodes_y[0], mesh.nodes_z[0]]])
+    P = interpolation_matrix(mesh, pts)
+    Q = MeshOps(mesh.h, mesh.origin).interpolation_matrix(pts)
+    P.sum_duplicates()
+    Q.sum_duplicates()
+    assert (P != Q).nnz == 0  # identical indices and identical weights
+
+
+def test_points_outside_mesh_raise():
+    mesh = _mesh()
+    with pytest.raises(ValueError):
+        interpolation_matrix(mesh, np.array([[1e4, 0.0, 0.0]]))
+
+
+def test_robin_weights_match_oracle_AvgBC():
+    mesh = _mesh()
+    rng = np.random.default_rng(0)
+    sigma = 10 ** rng.uniform(-3, -1, mesh.n_cells)
+    o = OracleDC3DNodal(mesh, Survey([sources.Pole([], np.r_[0.0, 0.0, 0.0])]), sigma=sigma)
+    ref = o.AvgBC @ sigma
+    bw = robin_face_weights(mesh)
+    # rebuild the Robin diagonal from the packed per-side weights
+    nx, ny, nz = mesh.shape_cells
+    Nx, Ny = nx + 1, ny + 1
+    s3 = sigma.reshape(nx, ny, nz, order="F")
+    out = np.zeros(mesh.n_nodes)
+    off = 0
+
+    def add(face_w, cell_sig, nodes4):
+        for n in nodes4:
+            np.add.at(out, n, face_w * cell_sig)
+
+    sides = []
+    for side, i in ((0, 0), (1, nx)):
+        J, K = np.meshgrid(np.arange(ny), np.arange(nz), indexing="ij")
+        J, K = J.ravel(order="F"), K.ravel(order="F")
+        w = bw[off:off + J.size]; off += J.size
+        cs = s3[0 if side == 0 else nx - 1, J, K]
+        nodes4 = [i + Nx * (J + Ny * K), i + Nx * (J + 1 + Ny * K), i + Nx * (J + Ny * (K + 1)), i + Nx * (J + 1 + Ny * (K + 1))]
+        sides.append((w, cs, nodes4))
+    for side, j in ((0, 0), (1, ny)):
+        I, K = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+        I, K = I.ravel(order="F"), K.ravel(order="F")
+        w = bw[off:off + I.size]; off += I.size
+        cs = s3[I, 0 if side == 0 else ny - 1, K]
+        nodes4 = [I + Nx * (j + Ny * K), I + 1 + Nx * (j + Ny * K), I + Nx * (j + Ny * (K + 1)), I + 1 + Nx * (j + Ny * (K + 1))]
+        sides.append((w, cs, nodes4))
+    for side, k in ((0, 0), (1, nz)):
+        I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        I, J = I.ravel(order="F"), J.ravel(order="F")
+        w = bw[off:off + I.size]; off += I.size
+        cs = s3[I, J, 0 if side == 0 else nz - 1]
+        nodes4 = [I + Nx * (J + Ny * k), I + 1 + Nx * (J + Ny * k), I + Nx * (J + 1 + Ny * k), I + 1 + Nx * (J + 1 + Ny * k)]
+        sides.append((w, cs, nodes4))
+    assert off == bw.size
+    for w, cs, nodes4 in sides:
+        add(w, cs, nodes4)
+    np.testing.assert_allclose(out, ref, rtol=1e-13, atol=1e-16)
+    # top faces carry no Robin weight
+    assert np.all(bw[-nx * ny:] == 0.0)
+
+
+def test_survey_tables_match_oracle_projection():
+    mesh, sigma, survey, _ = block_model_survey(seed=0)
+    t = SurveyTables(mesh, survey.source_list, mesh.n_nodes)
+    o = OracleDC3DNodal(mesh, survey, sigma=sigma)
+    # source term
+    q = np.zeros(mesh.n_nodes * survey.nSrc)
+    q[t.q_idx] = t.q_val
+    np.testing.assert_array_equal(q.reshape(survey.nSrc, -1).T, o.getRHS())
+    # receiver projection: each datum row restricted to its source block
+    row = 0
+    for s, P, fac in o._projections():
+        blk = t.P[row:row + P.shape[0], s * mesh.n_nodes:(s + 1) * mesh.n_nodes]
+        assert (blk != P).nnz == 0
+        row += P.shape[0]
+    assert t.nD == survey.nD == 300
+    # the transpose table is the exact transpose
+    PT = np.zeros((t.P.shape[1], t.nD))
+    for r, o_idx in enumerate(t.PT_out):
+        for e in range(t.PT_ptr[r], t.PT_ptr[r + 1]):
+            PT[o_idx, t.PT_idx[e]] += t.PT_w[e]
+    np.testing.assert_array_equal(PT, t.P.T.toarray())
+
+
+def test_survey_slices_and_geometric_factor():
+    a, b = np.r_[-10.0, 0, 0], np.r_[10.0, 0, 0]
+    M = np.array([[30.0, 0, 0], [40.0, 0, 0]])
+    N = np.array([[40.0, 0, 0], [50.0, 0, 0]])
+    rx = receivers.Dipole(M, N, data_type="apparent_resistivity")
+    rx2 = receivers.Pole(M)
+    s1 = sources.Dipole([rx], a, b)
+    s2 = sources.Pole([rx2], a)
+    sv = Survey([s1, s2])
+    sl = sv.get_all_slices()
+    assert sl[s1, rx] == slice(0, 2) and sl[s2, rx2] == slice(2, 4) and sv.nD == 4
+    g = geometric_factor(sv)
+    am, bm, an, bn = 40.0, 20.0, 50.0, 30.0
+    assert np.isclose(g[0], (1 / am - 1 / bm - 1 / an + 1 / bn) / (2 * np.pi))
+    assert np.isclose(g[2], (1 / 40.0) / (2 * np.pi))
+    sv.set_geometric_factor()
+    np.testing.assert_allclose(rx.geometric_factor[s1], g[:2])
+
+
+def test_mini_pole_pole_reassembles_dipole_data():
+    mesh, sigma, survey, _ = block_model_survey(seed=0)
+    dipoles, invs, mini = mini_pole_pole(survey)
+    o = OracleDC3DNodal(mesh, survey, sigma=sigma)
+    d_full = o.dpred()
+    om = OracleDC3DNodal(mesh, mini, sigma=sigma)
+    dm = om.dpred()
+    out = dm[invs[0]]
+    out[dipoles[0]] -= dm[invs[1]]
+    out[dipoles[1]] -= dm[invs[2]]
+    out[dipoles[0] & dipoles[1]] += dm[invs[3]]
+    np.testing.assert_allclose(out, d_full, rtol=1e-9, atol=1e-12 * np.abs(d_full).max())
+    assert mini.nSrc < 4 * survey.nD
+
+
+def test_maps_derivatives():
+    m = np.array([0.1, -0.3, 2.0])
+    e = maps.ExpMap(nP=3)
+    np.testing.assert_allclose(e * m, np.exp(m))
+    np.testing.assert_allclose(e.deriv(m).diagonal(), np.exp(m))
+    c = maps.ComboMap([maps.ReciprocalMap(), maps.ExpMap(nP=3)])
+    np.testing.assert_allclose(c * m, np.exp(-m))
+    np.testing.assert_allclose(c.diag_deriv(m), -np.exp(-m))
+
+
+def test_library_exports_every_declared_symbol():
+    """The C ABI in include/dcgpu.h is exported by libdcgpu.so (no compute call)."""
+    from simpeg_gb300 import _lib
+
+    header = (ROOT / "include" / "dcgpu.h").read_text()
+    declared = set(re.findall(r"^\s*(?:int|void|const char \*)\s*(dc_\w+)\s*\(", header, re.M))
+    assert declared, "no declarations parsed"
+    L = _lib.lib()
+    for name in sorted(declared):
+        assert hasattr(L, name), name
+        assert ctypes.cast(getattr(L, name), ctypes.c_void_p).value
+    assert declared == set(_lib.declared_symbols())

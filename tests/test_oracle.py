@@ -1,0 +1,175 @@
+"""Pins of the CPU oracle against the reference's own test recipes (no GPU).
+
+The reference has no golden vectors for this path; its DC tests pin the
+physics with an analytic half-space (tests/em/static/test_DC_analytic.py),
+the adjoint identity and Taylor derivative order
+(tests/em/static/test_DC_jvecjtvecadj.py), custom-surface equality
+(tests/em/static/test_DC_Boundaries.py) and source-chunk equality
+(tests/meta/test_meta_sim.py).  The same recipes are applied here to the
+oracle.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import analytic
+from oracle.dc3d import OracleDC3DNodal
+from oracle.operators import MeshOps
+from simpeg_gb300 import maps
+from simpeg_gb300.mesh import TensorMesh
+from simpeg_gb300.resistivity import receivers, sources
+from simpeg_gb300.resistivity.survey import Survey
+
+
+def _analytic_setup():
+    cs = 25.0
+    npad = 7
+    hx = [(cs, npad, -1.3), (cs, 21), (cs, npad, 1.3)]
+    hz = [(cs, npad, -1.3), (cs, 20)]
+    mesh = TensorMesh([hx, hx, hz], origin="CCN")
+    x = mesh.cell_centers_x[(mesh.cell_centers_x > -100) & (mesh.cell_centers_x < 100)]
+    y = mesh.cell_centers_y[(mesh.cell_centers_y > -100) & (mesh.cell_centers_y < 100)]
+    A = np.r_[-200.0, 0.0, 0.0]
+    B = np.r_[200.0, 0.0, 0.0]
+    M = TensorMesh._ndgrid(x - 25.0, y, np.r_[0.0])
+    N = TensorMesh._ndgrid(x + 25.0, y, np.r_[0.0])
+    ana = analytic.pole_dipole(A, M, N, 1e-2, earth_type="halfspace") - analytic.pole_dipole(
+        B, M, N, 1e-2, earth_type="halfspace")
+    rx = receivers.Dipole(M, N)
+    src = sources.Dipole([rx], A, B)
+    return mesh, Survey([src]), ana
+
+
+@pytest.mark.slow
+def test_analytic_halfspace_robin():
+    """tests/em/static/test_DC_analytic.py:69-81: rms relative error < 5 %."""
+    mesh, survey, ana = _analytic_setup()
+    o = OracleDC3DNodal(mesh, survey, sigma=np.full(mesh.n_cells, 1e-2), bc_type="Robin")
+    d = o.dpred()
+    err = np.sqrt((((d - ana) / ana) ** 2).sum() / survey.nD)
+    assert err < 0.05, err
+
+
+def _small_problem(seed=0, rho=False):
+    mesh = TensorMesh([[(10.0, 3, -1.3), (10.0, 8), (10.0, 3, 1.3)], [(10.0, 3, -1.3), (10.0, 6), (10.0, 3, 1.3)],
+                       [(10.0, 3, -1.3), (10.0, 5)]], origin="CCN")
+    xs = np.arange(-30.0, 31.0, 10.0)
+    srcs = []
+    for i in range(3):
+        M = np.c_[xs[3:6], np.zeros(3), np.zeros(3)]
+        N = np.c_[xs[4:7], np.zeros(3), np.zeros(3)]
+        srcs.append(sources.Dipole([receivers.Dipole(M, N)], np.r_[xs[i], 0, 0], np.r_[xs[i] - 10, 0, 0]))
+    srcs.append(sources.Pole([receivers.Pole(np.c_[xs[:4], np.full(4, 10.0), np.zeros(4)])], np.r_[20.0, 10.0, 0.0]))
+    survey = Survey(srcs)
+    rng = np.random.default_rng(seed)
+    m = np.log(10 ** rng.uniform(-2.5, -1.5, mesh.n_cells))
+    return mesh, survey, m
+
+
+def test_adjoint_identity():
+    """tests/em/static/test_DC_jvecjtvecadj.py:264-274: |w.Jv - v.Jtw| < 1e-8."""
+    mesh, survey, m = _small_problem()
+    o = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
+    o.set_model(m)
+    f = o.fields()
+    rng = np.random.default_rng(42)
+    v = rng.uniform(size=mesh.n_cells)
+    w = rng.uniform(size=survey.nD)
+    wJv = w @ o.Jvec(m, v, f=f)
+    vJtw = v @ o.Jtvec(m, w, f=f)
+    assert abs(wJv - vJtw) < 1e-8 * max(1.0, abs(wJv)), (wJv, vJtw)
+
+
+def test_taylor_derivative_order():
+    """discretize.tests.check_derivative recipe: second-order Taylor decay."""
+    mesh, survey, m = _small_problem(seed=1)
+    o = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
+    o.set_model(m)
+    f = o.fields()
+    d0 = o.dpred(f=f)
+    rng = np.random.default_rng(562)
+    dm = rng.standard_normal(mesh.n_cells) * 0.1
+    Jdm = o.Jvec(m, dm, f=f)
+    e1, e2 = [], []
+    hs = [1e-1, 1e-2, 1e-3]
+    for h in hs:
+        o.set_model(m + h * dm)
+        dh = o.dpred()
+        e1.append(np.linalg.norm(dh - d0))
+        e2.append(np.linalg.norm(dh - d0 - h * Jdm))
+    order1 = np.log10(e1[0] / e1[-1]) / 2
+    order2 = np.log10(e2[0] / e2[-1]) / 2
+    assert order1 > 0.9 and order2 > 1.8, (order1, order2)
+
+
+def test_custom_surface_faces_equal_default():
+    """tests/em/static/test_DC_Boundaries.py:35-50: explicit top faces == default."""
+    mesh = TensorMesh([8, 9, 10])
+    ops = MeshOps(mesh.h, mesh.origin)
+    bf = ops.boundary_faces()
+    top = bf["centers"][:, -1] == bf["centers"][:, -1].max()
+    src = sources.Pole([], np.r_[0.5, 0.5, 1.0])
+    sigma = np.full(mesh.n_cells, 0.1)
+    o1 = OracleDC3DNodal(mesh, Survey([src]), sigma=sigma)
+    o2 = OracleDC3DNodal(mesh, Survey([src]), sigma=sigma, surface_faces=top)
+    np.testing.assert_equal(o1.fields(), o2.fields())
+
+
+def test_source_chunks_equal_full():
+    """tests/meta/test_meta_sim.py:12-100: chunked sources reproduce the full simulation."""
+    mesh = TensorMesh([16, 16, 16], origin="CCN")
+    rx_locs = np.mgrid[-0.25:0.25:5j, -0.25:0.25:5j, 0:1:1j].reshape(3, -1).T
+    src_locs = np.mgrid[-0.5:0.5:10j, 0:1:1j, 0:1:1j].reshape(3, -1).T
+    src_list = [sources.Pole([receivers.Pole(rx_locs)], loc) for loc in src_locs]
+    m = np.arange(mesh.n_cells) / mesh.n_cells + 0.1
+    full = OracleDC3DNodal(mesh, Survey(src_list), sigma_map=maps.IdentityMap(mesh))
+    full.set_model(m)
+    ff = full.fields()
+    d_full = full.dpred(f=ff)
+    rng = np.random.default_rng(0)
+    u = rng.random(mesh.n_cells)
+    v = rng.random(d_full.size)
+    jv_full = full.Jvec(m, u, f=ff)
+    jtv_full = full.Jtvec(m, v, f=ff)
+    d_parts, jv_parts, jtv_sum, start = [], [], 0, 0
+    for i in range(0, len(src_list), 3):
+        sub = OracleDC3DNodal(mesh, Survey(src_list[i:i + 3]), sigma_map=maps.IdentityMap(mesh))
+        sub.set_model(m)
+        fs = sub.fields()
+        d = sub.dpred(f=fs)
+        d_parts.append(d)
+        jv_parts.append(sub.Jvec(m, u, f=fs))
+        jtv_sum = jtv_sum + sub.Jtvec(m, v[start:start + d.size], f=fs)
+        start += d.size
+    np.testing.assert_allclose(np.hstack(d_parts), d_full)
+    np.testing.assert_allclose(np.hstack(jv_parts), jv_full)
+    np.testing.assert_allclose(jtv_sum, jtv_full, rtol=1e-7, atol=1e-12 * np.abs(jtv_full).max())
+
+
+def test_jtj_diag_matches_full_J():
+    mesh, survey, m = _small_problem(seed=3)
+    o = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
+    o.set_model(m)
+    f = o.fields()
+    J = o.getJ(m, f=f)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(mesh.n_cells)
+    np.testing.assert_allclose(J @ v, o.Jvec(m, v, f=f), rtol=1e-8, atol=1e-14)
+    diag = o.getJtJdiag(m, f=f)
+    np.testing.assert_allclose(diag, (J * J).sum(axis=0), rtol=1e-12)
+
+
+def test_operator_hand_checked_2x1x1():
+    """A on a 2x1x1-cell mesh written out by hand (Neumann part)."""
+    mesh = TensorMesh([[1.0, 2.0], [1.0], [1.0]])
+    o = OracleDC3DNodal(mesh, Survey([sources.Pole([], np.r_[0.0, 0.0, 0.0])]), sigma=np.array([1.0, 3.0]),
+                        bc_type="Neumann")
+    G = o.G
+    Me = o.E @ np.array([1.0, 3.0])
+    # x-edges of cell 0 carry sigma*V/4 = 1*1/4; of cell 1: 3*2/4
+    np.testing.assert_allclose(Me[:8], [0.25, 1.5] * 4)
+    A = (G.T @ np.diag(Me) @ G)
+    # coupling between nodes 0 and 1 along x: -Me/hx^2
+    assert np.isclose(A[0, 1], -0.25)
+    assert np.isclose(A[1, 2], -1.5 / 4.0)
+    np.testing.assert_allclose(np.asarray(A.sum(axis=1)).ravel(), 0.0, atol=1e-14)
