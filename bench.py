@@ -1,0 +1,381 @@
+"""Benchmark: source-solves/s and Jtvec/s of the 1M-cell nodal DC workload.
+
+Workload (seeded, synthetic): TensorMesh 128x128x64 cells (1,081,665 nodes),
+5 m core cells, 8 padding cells at x1.3 on each horizontal side and at the
+bottom, log10 sigma a Gaussian random field (mean -2, std 0.5, correlation
+10 cells), 256 pole sources on a 16x16 surface grid, 40 dipole receivers each
+(10,240 data).  Every solve runs to a relative residual of 1e-9.
+
+One step = one forward pass of all 256 sources (multi-RHS solve + receiver
+gather).  ``value`` is device-resident throughput (inputs in HBM) of the
+mixed-precision path (fp32 multigrid-PCG inner solves + fp64 refinement);
+``e2e`` is the same through the public API ``Simulation3DNodal.dpred(m)`` with
+the model on the host and the data copied back every step.  The fp64 plain
+PCG and Jtvec throughputs, relative errors against an fp64 solve at 1e-13,
+the fine-level stencil roofline and the CPU baseline ride along in the line.
+
+``--impl reference`` times the reference's CPU path restated in ``oracle/``
+(scipy assembly of A = G^T Me G + Robin diagonal, then a SciPy solve) on the
+host cores: SuperLU (the reference's default solver) does not fit in memory at
+this size, so each step solves one source with SciPy CG + Jacobi (the
+reference's iterative-solver plug-in path) to the same 1e-9 tolerance.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "source-solves/s + Jtvec/s, 1M-cell DC3D: mixed vs FP64 plain on GB300 @<=1e-6 err"
+RTOL = 1e-9
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
+    return ap.parse_args()
+
+
+def _dist_init(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+
+    dist.init_process_group("nccl")
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def _workload(n_side):
+    from simpeg_gb300 import workloads
+
+    return workloads.scale_forward(seed=1, n_side=n_side)
+
+
+def _config(mesh, survey):
+    return {
+        "workload": "dc3d_nodal_forward_1M",
+        "mesh_cells": list(mesh.shape_cells),
+        "nodes": int(mesh.n_nodes),
+        "sources": int(survey.nSrc),
+        "data": int(survey.nD),
+        "rtol": RTOL,
+        "l2": "inputs larger than L2 (fields 2.2 GB fp64)",
+        "parallelism": "replicas",
+    }
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _cpu_baseline(mesh, sigma, survey):
+    """The oracle (CPU restatement of the reference path) on one source, SciPy CG + Jacobi to 1e-9."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    from oracle.dc3d import OracleDC3DNodal
+    from simpeg_gb300.resistivity.survey import Survey
+
+    t0 = time.perf_counter()
+    o = OracleDC3DNodal(mesh, Survey(survey.source_list[:1]), sigma=sigma, solver="cg", cg_rtol=RTOL)
+    A = o.getA()
+    q = o.getRHS()[:, 0]
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    x, info = spla.cg(A, q, rtol=RTOL, atol=0.0, M=sp.diags(1.0 / A.diagonal()), maxiter=20000)
+    t_solve = time.perf_counter() - t0
+    d = o.dpred(f=x[:, None])
+    return {
+        "value": 1.0 / t_solve,
+        "unit": "source-solves/s",
+        "cores": 1,
+        "kind": "port",
+        "sample": (f"1 of {survey.nSrc} sources: oracle assembly ({t_setup:.1f} s, excluded) + SciPy CG/Jacobi "
+                   f"to rtol {RTOL:g} ({t_solve:.1f} s, info={info}); SuperLU does not fit at this size"),
+        "_x": x, "_d": d,
+    }
+
+
+def run_reference(args):
+    rank, world, dist = _dist_init(args.gpus)
+    if rank != 0:
+        return
+    mesh, sigma, survey = _workload(args.n_side)
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the CPU path has no warm-up state worth priming beyond the first assembly
+    last = None
+    for _ in range(args.steps):
+        last = _cpu_baseline(mesh, sigma, survey)
+        vals.append(last["value"])
+    v = statistics.median(vals)
+    cb = {k: last[k] for k in ("unit", "cores", "kind", "sample")}
+    cb["value"] = v
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "source-solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": _config(mesh, survey), "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "source-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _traffic_per_unit():
+    """DRAM bytes per (node x RHS) of the fine-level fp32 stencil step from the committed ncu summary."""
+    p = ROOT / "profiles" / "cheb_step_fp32_dc3d.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_node_rhs:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    rank, world, dist = _dist_init(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from simpeg_gb300 import maps
+    from simpeg_gb300.engine import csr_spmv, kernel_launches, padded_rhs
+    from simpeg_gb300.resistivity import Simulation3DNodal
+
+    mesh, sigma, survey = _workload(args.n_side)
+    m = np.log(sigma)
+    K = survey.nSrc
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+    sim.model = m
+    sim._ensure_model()
+    eng = sim.engine
+    t, tq = sim._get_tables()
+    Q = sim.getRHS()
+    d_out = torch.empty(t.nD, dtype=torch.float64, device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def fwd(mode):
+        U, info = eng.solve(Q, mode=mode, rtol=RTOL)
+        csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U.view(-1), d_out)
+        return U, info
+
+    rng = np.random.default_rng(5)
+    v_host = rng.standard_normal(t.nD)
+    v_dev = torch.from_numpy(v_host).to(dev)
+
+    def jtvec(mode, U):
+        PTv = torch.zeros(K, mesh.n_nodes, dtype=torch.float64, device=dev)
+        csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], v_dev, PTv.view(-1), out_idx=tq["PT_out"])
+        Lam, _ = eng.solve(PTv, mode=mode, rtol=RTOL)
+        return eng.dadm_adj(U, Lam, None, scale=-1.0)
+
+    def timed(fn, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record()
+        out = None
+        for _ in range(steps):
+            out = fn()
+        e1.record()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            tt = torch.tensor([ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, out
+
+    # ---- warm-up (also allocates the solver workspaces)
+    for _ in range(args.warmup):
+        U, info = fwd("mixed")
+    jtvec("mixed", U)
+    torch.cuda.synchronize()
+
+    # ---- headline: mixed forward, device resident
+    n0 = kernel_launches()
+    eng.stencil_timing(True)
+    with Clocks(local) as clk:
+        ms_mixed, (U_mixed, info_mixed) = timed(lambda: fwd("mixed"), args.steps)
+    st_ms, st_n, st_bytes = eng.stencil_timing(False)
+    launches = kernel_launches() - n0
+    clocks = clk.summary()
+    d_mixed = d_out.cpu().numpy()
+
+    # ---- Jtvec (mixed), fp64 forward and Jtvec
+    ms_jt_mixed, g_mixed = timed(lambda: jtvec("mixed", U_mixed), args.steps)
+    g_mixed = g_mixed.cpu().numpy()
+    fwd("fp64")
+    ms_fp64, (U64, info64) = timed(lambda: fwd("fp64"), args.steps)
+    ms_jt_fp64, _ = timed(lambda: jtvec("fp64", U64), args.steps)
+
+    # ---- accuracy against an fp64 solve at 1e-13 (the oracle at this size)
+    U_ref, _ = eng.solve(Q, mode="fp64", rtol=1e-13)
+    csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U_ref.view(-1), d_out)
+    d_ref = d_out.cpu().numpy()
+    PTv = torch.zeros(K, mesh.n_nodes, dtype=torch.float64, device=dev)
+    csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], v_dev, PTv.view(-1), out_idx=tq["PT_out"])
+    Lam_ref, _ = eng.solve(PTv, mode="fp64", rtol=1e-13)
+    g_ref = eng.dadm_adj(U_ref, Lam_ref, None, scale=-1.0).cpu().numpy()
+    del Lam_ref, PTv
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    err = {"dpred": rel(d_mixed, d_ref), "jtvec_sigma": rel(g_mixed, g_ref)}
+
+    # ---- end to end through the public API: host model in, host data out
+    m2 = m + 1e-3 * rng.standard_normal(m.size)
+    models = [m, m2]
+    sim.dpred(m2)
+    e2e_steps = args.steps
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        dd = sim.dpred(models[i % 2])
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        tt = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    h2d = int(mesh.n_cells * 8)
+    d2h = int(t.nD * 8)
+
+    value = world * K * args.steps / (ms_mixed / 1e3)
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (st_bytes / st_n) / (st_ms / st_n * 1e-3) / 1e9 if st_n else None
+    tpu = _traffic_per_unit()
+    traffic = tpu * mesh.n_nodes * padded_rhs(K) if tpu is not None else None
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "source-solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner / f64 refinement",
+        "data": "synthetic (seeded Gaussian random field, 16x16 pole grid)",
+        "config": _config(mesh, survey),
+        "jtvec_per_s": world * args.steps / (ms_jt_mixed / 1e3),
+        "fp64_plain": {
+            "source_solves_per_s": world * K * args.steps / (ms_fp64 / 1e3),
+            "jtvec_per_s": world * args.steps / (ms_jt_fp64 / 1e3),
+            "iterations": info64.iterations,
+        },
+        "speedup_vs_fp64": {"forward": ms_fp64 / ms_mixed, "jtvec": ms_jt_fp64 / ms_jt_mixed},
+        "mixed_solve": {"inner_iterations": info_mixed.iterations, "outer": info_mixed.outer,
+                        "max_rel_res": info_mixed.max_rel_res, "levels": info_mixed.n_levels},
+        "rel_err_vs_fp64_1e-13": err,
+        "e2e": {"value": world * K * e2e_steps / e2e_s, "unit": "source-solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "Simulation3DNodal.dpred(m): host model -> exp -> H2D -> set_model -> solve -> gather -> D2H"},
+        "roofline": {
+            "kernel": "k_cheb_step<float,32> (fine-level Chebyshev stencil step)",
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "traffic": traffic,
+            "launches_timed": st_n,
+            "alg_bytes_per_launch": (st_bytes / st_n) if st_n else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback",
+        },
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = _cpu_baseline(mesh, sigma, survey)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -111,6 +111,18 @@ int dc_csr_spmv(int nrows, const long long *rowptr_dev, const long long *in_idx_
  * term q (sources.py:64-88, simulation.py:265-289). */
 int dc_fill_sparse(long long nnz, const long long *idx_dev, const double *val_dev, double *y_dev, void *stream);
 
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (all handles, all threads).  Instrumentation; no reference counterpart. */
+long long dc_kernel_launches(void);
+
+/* Event timing of the fine-level fp32 Chebyshev/stencil launches of h.
+ * enable = 1: start recording (up to 4096 launches); enable = 0: stop and
+ * return the summed device time, the number of timed launches and their
+ * algorithmic bytes (N*(20*K + 20): read z, r, d, write d, z in fp32 plus
+ * 16-byte coefficients and the 4-byte inverse diagonal per node).
+ * Instrumentation; no reference counterpart. */
+int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *launches, double *alg_bytes);
+
 #ifdef __cplusplus
 }
 #endif

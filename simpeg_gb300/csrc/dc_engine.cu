@@ -135,6 +135,8 @@ void set_dims(Level &L) {
   L.dims.Ny = L.ny + 1;
   L.dims.Nz = L.nz + 1;
   L.dims.N = (long long)L.dims.Nx * L.dims.Ny * L.dims.Nz;
+  L.dims.mx = div_magic((unsigned)L.dims.Nx);
+  L.dims.mxy = div_magic((unsigned)(L.dims.Nx * L.dims.Ny));
 }
 
 struct Cheb {
@@ -163,9 +165,9 @@ struct dc_handle {
   int *d_flag = nullptr;
   unsigned long long *d_lmax = nullptr;
   bool model_set = false;
-  int nu_pre = 2, nu_post = 2;
-  double cheb_ratio = 6.0;
-  int coarse_max = 600;
+  int nu_pre = 3, nu_post = 3;
+  double cheb_ratio = 30.0;
+  int coarse_max = 200;
   int check_every = 1;
   bool built = false;
   // cached internal workspace
@@ -178,6 +180,11 @@ struct dc_handle {
   int *h_mail = nullptr;
   double *h_maild = nullptr;
   cudaEvent_t ev = nullptr;
+  // optional timing of the fine-level fp32 Chebyshev stencil launches
+  bool prof = false;
+  std::vector<cudaEvent_t> prof_ev;  // start/stop pairs
+  int prof_used = 0;
+  double prof_bytes = 0.0;
 };
 
 namespace {
@@ -305,7 +312,7 @@ struct MGWork {
 
 struct Scal {
   double *part_a, *part_b, *part_c;  // partials (gx * Kp each)
-  double *rz, *rr, *bb, *alpha, *beta, *rr64, *bb64, *maxrel;
+  double *rz, *rr, *bb, *alpha, *beta, *rr64, *bb64, *maxrel, *tol2;
   int *active, *active_out, *n_active, *n_active_out, *status;
 };
 
@@ -343,6 +350,7 @@ void carve_scal(Carve &c, int Kp, int gx, Scal &s) {
   s.rr64 = c.take<double>(Kp);
   s.bb64 = c.take<double>(Kp);
   s.maxrel = c.take<double>(1);
+  s.tol2 = c.take<double>(Kp);
   s.active = c.take<int>(Kp);
   s.active_out = c.take<int>(Kp);
   s.n_active = c.take<int>(1);
@@ -398,29 +406,53 @@ const float *ainv<float>(const dc_handle *h) { return h->d_Ainv32; }
 template <>
 const double *ainv<double>(const dc_handle *h) { return h->d_Ainv64; }
 
+// Chebyshev step; the fine-level fp32 launches are bracketed by events when
+// stencil timing is on (dc_stencil_timing).
 template <typename T, int KB>
-void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int nb, cudaStream_t s) {
+void timed_cheb(const dc_handle *hc, int l, const Level &F, const T *r, const T *zin, T *zout, T *d, int nb,
+                double c1, double c2, double *partial, int gx, cudaStream_t s) {
+  dc_handle *h = const_cast<dc_handle *>(hc);
+  const bool rec = h->prof && l == 0 && sizeof(T) == 4 && h->prof_used + 2 <= (int)h->prof_ev.size();
+  if (rec) cudaEventRecord(h->prof_ev[h->prof_used], s);
+  Ops<T, KB>::cheb_step(F, r, zin, zout, d, nb, c1, c2, partial, gx, s);
+  if (rec) {
+    cudaEventRecord(h->prof_ev[h->prof_used + 1], s);
+    h->prof_used += 2;
+    h->prof_bytes += (double)F.dims.N * (20.0 * KB * nb + 20.0);
+  }
+}
+
+// Buffer that receives the first pre-smoothing step of level l, chosen so that
+// after (nu_pre - 1) + nu_post ping-pong swaps the result lands in z.
+template <typename T>
+T *first_buffer(const dc_handle *h, int l, T *z, const MGWork<T> &w) {
+  const int swaps = (h->nu_pre - 1) + h->nu_post;
+  return (swaps % 2) ? w.z2[l] : z;
+}
+
+// One V-cycle z = M r from level l.  If `pre_done`, the first Chebyshev step
+// (z1 = d = D^-1 r / theta into first_buffer) was already applied by the caller.
+// If `dot_partial`, the last smoothing step also emits per-block partials of r.z.
+template <typename T, int KB>
+void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int nb, cudaStream_t s,
+            bool pre_done = false, double *dot_partial = nullptr, int gx = 0) {
   using O = Ops<T, KB>;
   const int L = (int)h->lv.size();
   if (l == L - 1) {
-    if (L == 1) {
-      // single level: plain Chebyshev smoothing as the preconditioner
-    }
     O::coarse_solve(ainv<T>(h), h->nc, r, z, nb, s);
     return;
   }
   const Level &F = h->lv[l];
   const Level &C = h->lv[l + 1];
   const Cheb cp = cheb_params(F.lmax, h->cheb_ratio);
-  const int swaps = (h->nu_pre - 1) + h->nu_post;
-  T *cur = (swaps % 2) ? w.z2[l] : z;
-  T *oth = (swaps % 2) ? z : w.z2[l];
+  T *cur = first_buffer(h, l, z, w);
+  T *oth = (cur == z) ? w.z2[l] : z;
   // pre-smoothing from zero
-  O::cheb_first(F, r, cur, w.d[l], nb, 1.0 / cp.theta, s);
+  if (!pre_done) O::cheb_first(F, r, cur, w.d[l], nb, 1.0 / cp.theta, s);
   double rho_old = 1.0 / cp.sigma1;
   for (int it = 1; it < h->nu_pre; ++it) {
     const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
-    O::cheb_step(F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, s);
+    timed_cheb<T, KB>(h, l, F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, nullptr, 0, s);
     std::swap(cur, oth);
     rho_old = rho;
   }
@@ -430,14 +462,21 @@ void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int
   vcycle<T, KB>(h, l + 1, w.r[l + 1], w.z[l + 1], w, nb, s);
   O::prolong_add(F, C, w.z[l + 1], cur, nb, s);
   // post-smoothing (same polynomial, nonzero start)
-  O::cheb_step(F, r, cur, oth, w.d[l], nb, 0.0, 1.0 / cp.theta, s);
-  std::swap(cur, oth);
-  rho_old = 1.0 / cp.sigma1;
-  for (int it = 1; it < h->nu_post; ++it) {
-    const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
-    O::cheb_step(F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, s);
+  for (int it = 0; it < h->nu_post; ++it) {
+    double c1, c2;
+    if (it == 0) {
+      c1 = 0.0;
+      c2 = 1.0 / cp.theta;
+      rho_old = 1.0 / cp.sigma1;
+    } else {
+      const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
+      c1 = rho * rho_old;
+      c2 = 2.0 * rho / cp.delta;
+      rho_old = rho;
+    }
+    const bool last = it + 1 == h->nu_post;
+    timed_cheb<T, KB>(h, l, F, r, cur, oth, w.d[l], nb, c1, c2, last ? dot_partial : nullptr, gx, s);
     std::swap(cur, oth);
-    rho_old = rho;
   }
   if (cur != z) cudaMemcpyAsync(z, cur, sizeof(T) * F.dims.N * KB * nb, cudaMemcpyDeviceToDevice, s);
 }
@@ -447,33 +486,39 @@ void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int
 // init_active (nullable): RHS with init_active[r] == 0 are left untouched.
 template <typename T, int KB>
 int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Scal &sc, int nb, int gx,
-        const int *init_active, double tol, int maxit, int *iters, cudaStream_t s) {
+        const int *init_active, const double *tol2, int maxit, int *iters, cudaStream_t s) {
   using O = Ops<T, KB>;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
   const int Kp = nb * KB;
+  const bool fused = h->lv.size() > 1;
   if (init_active)
     CK(cudaMemcpyAsync(sc.active, init_active, sizeof(int) * Kp, cudaMemcpyDeviceToDevice, s));
-  else {
-    std::vector<int> ones(Kp, 1);
-    CK(cudaMemcpyAsync(sc.active, ones.data(), sizeof(int) * Kp, cudaMemcpyHostToDevice, s));
-  }
+  else
+    fill_int(sc.active, Kp, 1, s);
   CK(cudaMemsetAsync(sc.status, 0, sizeof(int), s));
   O::dot(N, nb, r, r, sc.part_b, gx, s);
   sum_partials(Kp, KB, gx, sc.part_b, sc.bb, s);
-  vcycle<T, KB>(h, 0, r, z, w, nb, s);
-  O::dot(N, nb, r, z, sc.part_c, gx, s);
-  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol * tol, sc.active, sc.beta, sc.n_active, 1, s);
+  vcycle<T, KB>(h, 0, r, z, w, nb, s, false, sc.part_c, gx);
+  if (!fused) O::dot(N, nb, r, z, sc.part_c, gx, s);
+  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 1, s);
   O::copy(N, nb, p, z, s);
+  const Cheb cp0 = cheb_params(F.lmax, h->cheb_ratio);
+  T *z1 = fused ? first_buffer(h, 0, z, w) : nullptr;
   int it = 0;
   int since = 0;
   for (it = 0; it < maxit; ++it) {
     O::apply(F, p, q, nb, sc.part_a, gx, s);
     pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, s);
-    O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, s);
-    vcycle<T, KB>(h, 0, r, z, w, nb, s);
-    O::dot(N, nb, r, z, sc.part_c, gx, s);
-    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol * tol, sc.active, sc.beta, sc.n_active, 0, s);
+    if (fused) {
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, 1.0 / cp0.theta, z1, w.d[0], s);
+      vcycle<T, KB>(h, 0, r, z, w, nb, s, true, sc.part_c, gx);
+    } else {
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, s);
+      vcycle<T, KB>(h, 0, r, z, w, nb, s);
+      O::dot(N, nb, r, z, sc.part_c, gx, s);
+    }
+    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 0, s);
     O::p_update(N, nb, p, z, sc.beta, s);
     if (++since >= h->check_every || it + 1 == maxit) {
       since = 0;
@@ -492,12 +537,14 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
     }
   }
   *iters = it;
-  // report whether anything is still active
   CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));
   CK(cudaEventSynchronize(h->ev));
   return h->h_mail[0] == 0 ? 0 : DC_ERR_NOT_CONVERGED;
 }
+
+// Inner solves aim at 0.3x the remaining outer gap (squared: 0.09).
+constexpr double kSafety2 = 0.09;
 
 template <int KB>
 int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
@@ -511,7 +558,9 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
   if (mode == DC_MODE_FP64) {
     CK(cudaMemcpyAsync(w.R64, w.B64, sizeof(double) * N * Kp, cudaMemcpyDeviceToDevice, s));
     int it = 0;
-    status = pcg<double, KB>(h, w.X64, w.R64, w.p64, w.q64, w.z64, w.mg64, w.sc, nb, gx, nullptr, rtol, maxit, &it, s);
+    fill_double(w.sc.tol2, Kp, rtol * rtol, s);
+    status = pcg<double, KB>(h, w.X64, w.R64, w.p64, w.q64, w.z64, w.mg64, w.sc, nb, gx, nullptr, w.sc.tol2, maxit,
+                             &it, s);
     if (status == DC_ERR_BREAKDOWN) return status;
     total_it = it;
     outer = 1;
@@ -520,13 +569,15 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
     Ops<double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
-    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, nullptr,
+                0.0, 0.0, s);
   } else {
     // |b|^2, initial outer flags, r32 = b
     Ops<double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
-    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+    outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
+                inner_rtol * inner_rtol, kSafety2, s);
     pack_colmajor<float>(b, N, k, KB, nb, w.r32, s);
     const int max_outer = 30;
     for (outer = 0; outer < max_outer;) {
@@ -541,14 +592,15 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
       int it = 0;
       int rc = pcg<float, KB>(h, w.d32, w.r32, w.p32, w.q32, w.z32, w.mg32, w.sc, nb, gx, w.sc.active_out,
-                              inner_rtol, std::min(inner_maxit, maxit - total_it), &it, s);
+                              w.sc.tol2, std::min(inner_maxit, maxit - total_it), &it, s);
       total_it += it;
       if (rc == DC_ERR_BREAKDOWN) return rc;
       ir_accumulate<KB>(N, nb, w.X64, w.d32, s);
       ++outer;
       ir_residual<KB>(F, w.B64, w.X64, w.R64, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, s);
       sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
-      outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, s);
+      outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel,
+                  w.sc.tol2, inner_rtol * inner_rtol, kSafety2, s);
     }
     if (outer >= max_outer) status = DC_ERR_NOT_CONVERGED;
   }
@@ -638,6 +690,7 @@ void dc_destroy(dc_handle *h) {
   if (h->h_mail) cudaFreeHost(h->h_mail);
   if (h->h_maild) cudaFreeHost(h->h_maild);
   if (h->ev) cudaEventDestroy(h->ev);
+  for (auto &e : h->prof_ev) cudaEventDestroy(e);
   delete h;
 }
 
@@ -806,6 +859,34 @@ int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const d
   edge_products(u, lam, k, L0.dims, h->d_P, h->d_Q, s);
   cell_gradient(L0, h->robin, h->d_P, h->d_Q, dsig, scale, g, s);
   CK(cudaGetLastError());
+  return 0;
+}
+
+long long dc_kernel_launches(void) { return dc::launch_counter(); }
+
+int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *launches, double *alg_bytes) {
+  if (!h) return fail(DC_ERR_ARG, "handle is NULL");
+  if (enable) {
+    if (h->prof_ev.empty()) {
+      h->prof_ev.resize(8192);
+      for (auto &e : h->prof_ev) CK(cudaEventCreate(&e));
+    }
+    h->prof_used = 0;
+    h->prof_bytes = 0.0;
+    h->prof = true;
+    return 0;
+  }
+  h->prof = false;
+  double tot = 0.0;
+  for (int i = 0; i + 1 < h->prof_used; i += 2) {
+    CK(cudaEventSynchronize(h->prof_ev[i + 1]));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, h->prof_ev[i], h->prof_ev[i + 1]));
+    tot += ms;
+  }
+  if (total_ms) *total_ms = tot;
+  if (launches) *launches = h->prof_used / 2;
+  if (alg_bytes) *alg_bytes = h->prof_bytes;
   return 0;
 }
 

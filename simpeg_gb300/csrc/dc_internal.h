@@ -26,9 +26,13 @@ struct alignas(32) Coef64 { double cx, cy, cz, d; };
 struct alignas(16) Coef32 { float cx, cy, cz, d; };
 
 struct Dims {
-  int Nx, Ny, Nz;  // nodes per axis
-  long long N;     // nodes
+  int Nx, Ny, Nz;    // nodes per axis
+  long long N;       // nodes
+  unsigned mx, mxy;  // division magic for Nx and Nx*Ny (see fast_div in dc_stencil.cu)
 };
+
+// floor(2^32 / d) + 1: with q = umulhi(n, m), floor(n / d) is q or q - 1 for 0 <= n < 2^31, d >= 2.
+inline unsigned div_magic(unsigned d) { return (unsigned)(0x100000000ull / d + 1ull); }
 
 // 1D transfer tables between a fine axis (nf nodes) and its coarse axis (nc nodes).
 struct Axis1D {
@@ -65,6 +69,14 @@ struct Level {
   long long pl_off[4] = {0}, r_off[4] = {0};
 };
 
+// Every kernel launch of the engine passes its grid through count_launch(),
+// which counts launches for dc_kernel_launches().
+long long &launch_counter();
+inline dim3 count_launch(dim3 g) {
+  ++launch_counter();
+  return g;
+}
+
 // ---- dc_stencil.cu -----------------------------------------------------------
 void set_sm_count(int n);
 int node_grid(long long nodes, int KB, int nb);
@@ -74,13 +86,15 @@ template <typename T, int KB> struct Ops {
   static void apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
   static void residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s);
   static void cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s);
+  // with partial: also per-block partials of r . zout
   static void cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
-                        cudaStream_t s);
+                        double *partial, int gx, cudaStream_t s);
   static void restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s);
   static void prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s);
   static void coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s);
+  // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = d = c0 D^-1 r on that level.
   static void update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                        double *partial, int gx, cudaStream_t s);
+                        double *partial, int gx, const Level *smooth, double c0, T *z, T *d, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
   static void p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s);
   static void copy(long long N, int nb, T *dst, const T *src, cudaStream_t s);
@@ -92,13 +106,16 @@ void ir_residual(const Level &L, const double *b, const double *x, double *r64, 
 template <int KB>
 void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s);
 
+void fill_int(int *a, int n, int v, cudaStream_t s);
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
                int *status, cudaStream_t s);
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
-              const double *bb, double tol2, int *active, double *beta, int *n_active, int first, cudaStream_t s);
+              const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
+              cudaStream_t s);
 void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s);
-void outer_check(int K, const double *rr, const double *bb, double tol2, int *active, int *n_active, double *maxrel,
-                 cudaStream_t s);
+void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
+                 double *maxrel, double *inner_tol2, double inner_floor2, double safety2, cudaStream_t s);
+void fill_double(double *a, int n, double v, cudaStream_t s);
 
 void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s);
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s);

@@ -124,27 +124,27 @@ extern int g_n_sm;
 void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const double *w, const double *x,
               const long long *out_idx, double *y, double scale, int accumulate, cudaStream_t s) {
   if (nrows <= 0) return;
-  k_csr_spmv<<<grid_flat(nrows, g_n_sm), TPB, 0, s>>>(nrows, rowptr, in_idx, w, x, out_idx, y, scale, accumulate);
+  k_csr_spmv<<<count_launch(grid_flat(nrows, g_n_sm)), TPB, 0, s>>>(nrows, rowptr, in_idx, w, x, out_idx, y, scale, accumulate);
 }
 
 void fill_sparse(long long nnz, const long long *idx, const double *val, double *y, cudaStream_t s) {
   if (nnz <= 0) return;
-  k_fill_sparse<<<grid_flat(nnz, g_n_sm), TPB, 0, s>>>(nnz, idx, val, y);
+  k_fill_sparse<<<count_launch(grid_flat(nnz, g_n_sm)), TPB, 0, s>>>(nnz, idx, val, y);
 }
 
 void scale_vec(long long n, double *y, double a, cudaStream_t s) {
   if (n <= 0) return;
-  k_scale<<<grid_flat(n, g_n_sm), TPB, 0, s>>>(n, y, a);
+  k_scale<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(n, y, a);
 }
 
 void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s) {
-  k_edge_products<<<grid_flat(d.N, g_n_sm), TPB, 0, s>>>(u, l, K, d, P, Q);
+  k_edge_products<<<count_launch(grid_flat(d.N, g_n_sm)), TPB, 0, s>>>(u, l, K, d, P, Q);
 }
 
 void cell_gradient(const Level &L, int robin, const double *P, const double *Q, const double *dsig, double scale,
                    double *g, cudaStream_t s) {
   const long long nC = (long long)L.nx * L.ny * L.nz;
-  k_cell_gradient<<<grid_flat(nC, g_n_sm), TPB, 0, s>>>(
+  k_cell_gradient<<<count_launch(grid_flat(nC, g_n_sm)), TPB, 0, s>>>(
       P, Q, L.d_h, L.nx, L.ny, L.nz, robin ? L.d_bface : nullptr, L.bface_off[0], L.bface_off[1], L.bface_off[2],
       L.bface_off[3], L.bface_off[4], L.bface_off[5], dsig, scale, g);
 }

@@ -17,11 +17,18 @@ namespace {
 
 constexpr int TPB = 256;
 
+// floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
+__device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
+  unsigned q = __umulhi((unsigned)n, m);
+  q -= (q * (unsigned)d > (unsigned)n) ? 1u : 0u;
+  return (int)q;
+}
+
 __device__ __forceinline__ void node_ijk(int n, const Dims &d, int &i, int &j, int &k) {
-  int nxy = d.Nx * d.Ny;
-  k = n / nxy;
-  int r = n - k * nxy;
-  j = r / d.Nx;
+  const int nxy = d.Nx * d.Ny;
+  k = fast_div(n, nxy, d.mxy);
+  const int r = n - k * nxy;
+  j = fast_div(r, d.Nx, d.mx);
   i = r - j * d.Nx;
 }
 
@@ -29,73 +36,127 @@ template <typename C> struct CoefT;
 template <> struct CoefT<double> { using type = Coef64; };
 template <> struct CoefT<float> { using type = Coef32; };
 
-// y = (A x) at element t of node (i, j, k).
+// Vector width per thread: 16-byte accesses (4 fp32 / 2 fp64 RHS lanes of one node).
+template <typename T, int KB> struct VWidth {
+  static constexpr int v = (sizeof(T) == 4) ? (KB >= 4 ? 4 : KB) : (KB >= 2 ? 2 : 1);
+};
+
+template <typename T, int W> struct alignas(sizeof(T) * W) Vec {
+  T a[W];
+};
+
+template <typename T, int W>
+__device__ __forceinline__ Vec<T, W> ldv(const T *p) {
+  return *reinterpret_cast<const Vec<T, W> *>(p);
+}
+template <typename T, int W>
+__device__ __forceinline__ void stv(T *p, const Vec<T, W> &v) {
+  *reinterpret_cast<Vec<T, W> *>(p) = v;
+}
+
+// Per-thread geometry of the "node x lane-group" mapping.  LPN threads share
+// one node (each owning W consecutive RHS lanes); blockIdx.y is the RHS block.
+template <typename T, int KB> struct Map {
+  static constexpr int W = VWidth<T, KB>::v;
+  static constexpr int LPN = KB / W;  // threads per node
+};
+
 template <typename T, int KB>
-__device__ __forceinline__ T stencil_at(const typename CoefT<T>::type *__restrict__ coef,
-                                        const T *__restrict__ x, long long t, int n, int i, int j,
-                                        int k, const Dims &d) {
+__device__ __forceinline__ const typename CoefT<T>::type *coef_of(const void *c) {
+  return reinterpret_cast<const typename CoefT<T>::type *>(c);
+}
+
+// (A x) for the W lanes at element t of node n = (i, j, k).
+template <typename T, int KB, int W>
+__device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *__restrict__ coef,
+                                                  const T *__restrict__ x, long long t, int n, int i, int j, int k,
+                                                  const Dims &d) {
   const auto c = coef[n];
-  T acc = c.d * x[t];
+  Vec<T, W> acc = ldv<T, W>(x + t);
+#pragma unroll
+  for (int e = 0; e < W; ++e) acc.a[e] *= c.d;
   const long long sx = KB, sy = (long long)d.Nx * KB, sz = (long long)d.Nx * d.Ny * KB;
-  if (i + 1 < d.Nx) acc -= c.cx * x[t + sx];
-  if (i > 0) acc -= coef[n - 1].cx * x[t - sx];
-  if (j + 1 < d.Ny) acc -= c.cy * x[t + sy];
-  if (j > 0) acc -= coef[n - d.Nx].cy * x[t - sy];
-  if (k + 1 < d.Nz) acc -= c.cz * x[t + sz];
-  if (k > 0) acc -= coef[n - d.Nx * d.Ny].cz * x[t - sz];
+  auto sub = [&](T w, long long off) {
+    const Vec<T, W> v = ldv<T, W>(x + t + off);
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc.a[e] -= w * v.a[e];
+  };
+  if (i + 1 < d.Nx) sub(c.cx, sx);
+  if (i > 0) sub(coef[n - 1].cx, -sx);
+  if (j + 1 < d.Ny) sub(c.cy, sy);
+  if (j > 0) sub(coef[n - d.Nx].cy, -sy);
+  if (k + 1 < d.Nz) sub(c.cz, sz);
+  if (k > 0) sub(coef[n - d.Nx * d.Ny].cz, -sz);
   return acc;
 }
 
-// Block-level reduction of one value per thread into per-lane partial sums:
-// partial[(blockIdx.y * gridDim.x + blockIdx.x) * KB + lane].
-template <int KB, typename A>
-__device__ __forceinline__ void block_partial(A v, double *partial) {
-  __shared__ double red[TPB / 32][32];
+// Block reduction of W per-thread sums (lanes q*W .. q*W+W-1 of the RHS block)
+// into partial[(blockIdx.y * gridDim.x + blockIdx.x) * KB + lane].
+template <int KB, int W, int LPN, typename A>
+__device__ __forceinline__ void block_partial(A (&v)[W], double *partial) {
+  __shared__ double red[TPB / 32][32][W];
 #pragma unroll
-  for (int off = 16; off >= KB; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  for (int e = 0; e < W; ++e) {
+#pragma unroll
+    for (int off = 16; off >= LPN; off >>= 1) v[e] += __shfl_xor_sync(0xffffffffu, v[e], off);
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane < KB) red[warp][lane] = (double)v;
+  if (lane < LPN) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) red[warp][lane][e] = (double)v[e];
+  }
   __syncthreads();
   if (threadIdx.x < KB) {
+    const int q = threadIdx.x / W, e = threadIdx.x % W;
     double s = 0.0;
 #pragma unroll
-    for (int w = 0; w < TPB / 32; ++w) s += red[w][threadIdx.x];
+    for (int w = 0; w < TPB / 32; ++w) s += red[w][q][e];
     partial[((long long)blockIdx.y * gridDim.x + blockIdx.x) * KB + threadIdx.x] = s;
   }
 }
 
+#define NODE_LOOP(NNODES)                                                                  \
+  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;                                  \
+  const int q = threadIdx.x % LPN;                                                         \
+  const long long stride = (long long)gridDim.x * TPB;                                     \
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g / LPN < (NNODES); g += stride)
+
 // ---------------------------------------------------------------- stencil ops
 template <typename T, int KB, bool DOT>
-__global__ void __launch_bounds__(TPB) k_apply(const typename CoefT<T>::type *__restrict__ coef,
-                                               const T *__restrict__ x, T *__restrict__ y, Dims d,
-                                               double *__restrict__ partial) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * d.N * KB + lane;
-  T acc = 0;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
+                                               T *__restrict__ y, Dims d, double *__restrict__ partial) {
+  const auto *coef = coef_of<T, KB>(cf);
+  T acc[Map<T, KB>::W] = {};
+  NODE_LOOP(d.N) {
+    const int n = (int)(g / LPN);
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = base + (long long)n * KB;
-    T v = stencil_at<T, KB>(coef, x, t, n, i, j, k, d);
-    y[t] = v;
-    if (DOT) acc += v * x[t];
+    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+    const Vec<T, W> v = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
+    stv<T, W>(y + t, v);
+    if (DOT) {
+      const Vec<T, W> xv = ldv<T, W>(x + t);
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
+    }
   }
-  if (DOT) block_partial<KB>(acc, partial);
+  if (DOT) block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
 }
 
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_residual(const typename CoefT<T>::type *__restrict__ coef,
-                                                  const T *__restrict__ r, const T *__restrict__ z,
-                                                  T *__restrict__ res, Dims d) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * d.N * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+__global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, const T *__restrict__ r,
+                                                  const T *__restrict__ z, T *__restrict__ res, Dims d) {
+  const auto *coef = coef_of<T, KB>(cf);
+  NODE_LOOP(d.N) {
+    const int n = (int)(g / LPN);
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = base + (long long)n * KB;
-    res[t] = r[t] - stencil_at<T, KB>(coef, z, t, n, i, j, k, d);
+    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, z, t, n, i, j, k, d);
+    Vec<T, W> rv = ldv<T, W>(r + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) rv.a[e] -= az.a[e];
+    stv<T, W>(res + t, rv);
   }
 }
 
@@ -103,62 +164,74 @@ __global__ void __launch_bounds__(TPB) k_residual(const typename CoefT<T>::type 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, const T *__restrict__ r,
                                                     T *__restrict__ z, T *__restrict__ dv, Dims d, T c0) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * d.N * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
-    const long long t = base + (long long)n * KB;
-    T v = c0 * invd[n] * r[t];
-    z[t] = v;
-    dv[t] = v;
+  NODE_LOOP(d.N) {
+    const int n = (int)(g / LPN);
+    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+    const T s = c0 * invd[n];
+    Vec<T, W> v = ldv<T, W>(r + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) v.a[e] *= s;
+    stv<T, W>(z + t, v);
+    stv<T, W>(dv + t, v);
   }
 }
 
-// Chebyshev step: d = c1 d + c2 D^-1 (r - A zin) ; zout = zin + d.
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_cheb_step(const typename CoefT<T>::type *__restrict__ coef,
-                                                   const T *__restrict__ invd, const T *__restrict__ r,
-                                                   const T *__restrict__ zin, T *__restrict__ zout,
-                                                   T *__restrict__ dv, Dims d, T c1, T c2) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * d.N * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+// Chebyshev step: d = c1 d + c2 D^-1 (r - A zin) ; zout = zin + d.  With DOT,
+// also per-block partials of r . zout (the PCG's r.z after the V-cycle).
+template <typename T, int KB, bool DOT>
+__global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
+                                                   const T *__restrict__ r, const T *__restrict__ zin,
+                                                   T *__restrict__ zout, T *__restrict__ dv, Dims d, T c1, T c2,
+                                                   double *__restrict__ partial) {
+  const auto *coef = coef_of<T, KB>(cf);
+  T acc[Map<T, KB>::W] = {};
+  NODE_LOOP(d.N) {
+    const int n = (int)(g / LPN);
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = base + (long long)n * KB;
-    T res = r[t] - stencil_at<T, KB>(coef, zin, t, n, i, j, k, d);
-    T dn = c1 * dv[t] + c2 * invd[n] * res;
-    dv[t] = dn;
-    zout[t] = zin[t] + dn;
+    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, zin, t, n, i, j, k, d);
+    const Vec<T, W> rv = ldv<T, W>(r + t);
+    Vec<T, W> dd = ldv<T, W>(dv + t);
+    Vec<T, W> zo = ldv<T, W>(zin + t);
+    const T s = c2 * invd[n];
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      dd.a[e] = c1 * dd.a[e] + s * (rv.a[e] - az.a[e]);
+      zo.a[e] += dd.a[e];
+      if (DOT) acc[e] += rv.a[e] * zo.a[e];
+    }
+    stv<T, W>(dv + t, dd);
+    stv<T, W>(zout + t, zo);
   }
+  if (DOT) block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
 }
 
 // ---------------------------------------------------------------- transfers
 struct XferTab {
-  const int *fi;       // coarse node -> fine node, per axis at off[a]
-  const void *wl, *wr; // T weights of fine fi-1 / fi+1
-  const int *pl;       // fine node -> left coarse node
-  const void *pw;      // T weight on pl
+  const int *fi;        // coarse node -> fine node, per axis at roff[a]
+  const void *wl, *wr;  // T weights of fine fi-1 / fi+1
+  const int *pl;        // fine node -> left coarse node, per axis at poff[a]
+  const void *pw;       // T weight on pl
   long long roff[3], poff[3];
 };
 
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *__restrict__ rc, Dims f,
-                                                  Dims c, XferTab tb) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
+__global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *__restrict__ rc, Dims f, Dims c,
+                                                  XferTab tb) {
   const T *wl = (const T *)tb.wl, *wr = (const T *)tb.wr;
-  const long long fbase = (long long)blockIdx.y * f.N * KB + lane;
-  const long long cbase = (long long)blockIdx.y * c.N * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < c.N; n += gridDim.x * NPB) {
+  NODE_LOOP(c.N) {
+    const int n = (int)(g / LPN);
     int I, J, K;
     node_ijk(n, c, I, J, K);
     const int fx = tb.fi[tb.roff[0] + I], fy = tb.fi[tb.roff[1] + J], fz = tb.fi[tb.roff[2] + K];
-    T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
-    T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
-    T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
-    T acc = 0;
+    const T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
+    const T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
+    const T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
+    const long long fb = (long long)blockIdx.y * f.N * KB + q * W;
+    Vec<T, W> acc;
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc.a[e] = 0;
 #pragma unroll
     for (int cz = 0; cz < 3; ++cz) {
       if (wz[cz] == (T)0) continue;
@@ -170,29 +243,31 @@ __global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *
 #pragma unroll
         for (int cx = 0; cx < 3; ++cx) {
           if (wx[cx] == (T)0) continue;
-          acc += wx[cx] * wyz * res[fbase + (row + fx + cx - 1) * KB];
+          const T w = wx[cx] * wyz;
+          const Vec<T, W> v = ldv<T, W>(res + fb + (row + fx + cx - 1) * KB);
+#pragma unroll
+          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
         }
       }
     }
-    rc[cbase + (long long)n * KB] = acc;
+    stv<T, W>(rc + ((long long)blockIdx.y * c.N + n) * KB + q * W, acc);
   }
 }
 
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T *__restrict__ z, Dims f,
-                                                     Dims c, XferTab tb) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
+__global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T *__restrict__ z, Dims f, Dims c,
+                                                     XferTab tb) {
   const T *pw = (const T *)tb.pw;
-  const long long fbase = (long long)blockIdx.y * f.N * KB + lane;
-  const long long cbase = (long long)blockIdx.y * c.N * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < f.N; n += gridDim.x * NPB) {
+  NODE_LOOP(f.N) {
+    const int n = (int)(g / LPN);
     int i, j, k;
     node_ijk(n, f, i, j, k);
     const int I = tb.pl[tb.poff[0] + i], J = tb.pl[tb.poff[1] + j], K = tb.pl[tb.poff[2] + k];
     const T ax = pw[tb.poff[0] + i], ay = pw[tb.poff[1] + j], az = pw[tb.poff[2] + k];
     const T wx[2] = {ax, (T)1 - ax}, wy[2] = {ay, (T)1 - ay}, wz[2] = {az, (T)1 - az};
-    T acc = 0;
+    const long long cb = (long long)blockIdx.y * c.N * KB + q * W;
+    const long long t = ((long long)blockIdx.y * f.N + n) * KB + q * W;
+    Vec<T, W> acc = ldv<T, W>(z + t);
 #pragma unroll
     for (int b = 0; b < 2; ++b) {
       if (wz[b] == (T)0) continue;
@@ -202,86 +277,114 @@ __global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T
         const T wyz = wy[a] * wz[b];
         const long long row = ((long long)(K + b) * c.Ny + (J + a)) * c.Nx;
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          if (wx[e] == (T)0) continue;
-          acc += wx[e] * wyz * zc[cbase + (row + I + e) * KB];
+        for (int e2 = 0; e2 < 2; ++e2) {
+          if (wx[e2] == (T)0) continue;
+          const T w = wx[e2] * wyz;
+          const Vec<T, W> v = ldv<T, W>(zc + cb + (row + I + e2) * KB);
+#pragma unroll
+          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
         }
       }
     }
-    const long long t = fbase + (long long)n * KB;
-    z[t] += acc;
+    stv<T, W>(z + t, acc);
   }
 }
 
 // z_c = Ainv r_c on the coarsest level (dense, row-major Ainv[nc][nc]).
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, int nc,
-                                                      const T *__restrict__ rc, T *__restrict__ zc) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * nc * KB + lane;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < nc; n += gridDim.x * NPB) {
+__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, int nc, const T *__restrict__ rc,
+                                                      T *__restrict__ zc) {
+  NODE_LOOP(nc) {
+    const int n = (int)(g / LPN);
     const T *row = Ainv + (long long)n * nc;
-    T acc = 0;
-    for (int m = 0; m < nc; ++m) acc += row[m] * rc[base + (long long)m * KB];
-    zc[base + (long long)n * KB] = acc;
+    const long long b = (long long)blockIdx.y * nc * KB + q * W;
+    Vec<T, W> acc;
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc.a[e] = 0;
+    for (int m = 0; m < nc; ++m) {
+      const T w = row[m];
+      const Vec<T, W> v = ldv<T, W>(rc + b + (long long)m * KB);
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
+    }
+    stv<T, W>(zc + b + (long long)n * KB, acc);
   }
 }
 
 // ---------------------------------------------------------------- PCG vectors
-// x += a p ; r -= a q ; partial |r|^2   (a per RHS)
-template <typename T, int KB>
+// x += a p ; r -= a q ; partial |r|^2 (a per RHS).  With SMOOTH, also the first
+// Chebyshev step of the fine level on the new residual: z = d = c0 D^-1 r.
+template <typename T, int KB, bool SMOOTH>
 __global__ void __launch_bounds__(TPB) k_update_xr(long long N, T *__restrict__ x, T *__restrict__ r,
-                                                   const T *__restrict__ p, const T *__restrict__ q,
-                                                   const double *__restrict__ alpha,
-                                                   double *__restrict__ partial) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * N * KB + lane;
-  const T a = (T)alpha[blockIdx.y * KB + lane];
-  T acc = 0;
-  if (a != (T)0) {
-    for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
-      const long long t = base + n * KB;
-      x[t] += a * p[t];
-      T rv = r[t] - a * q[t];
-      r[t] = rv;
-      acc += rv * rv;
+                                                   const T *__restrict__ p, const T *__restrict__ qv,
+                                                   const double *__restrict__ alpha, double *__restrict__ partial,
+                                                   const T *__restrict__ invd, T *__restrict__ z, T *__restrict__ dv,
+                                                   T c0) {
+  constexpr int Wc = Map<T, KB>::W;
+  T acc[Wc] = {};
+  T a[Wc];
+  {
+    const int qq = threadIdx.x % Map<T, KB>::LPN;
+#pragma unroll
+    for (int e = 0; e < Wc; ++e) a[e] = (T)alpha[blockIdx.y * KB + qq * Wc + e];
+  }
+  NODE_LOOP(N) {
+    const long long n = g / LPN;
+    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
+    Vec<T, W> xv = ldv<T, W>(x + t), rv = ldv<T, W>(r + t);
+    const Vec<T, W> pv = ldv<T, W>(p + t), qq = ldv<T, W>(qv + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      xv.a[e] += a[e] * pv.a[e];
+      rv.a[e] -= a[e] * qq.a[e];
+      acc[e] += rv.a[e] * rv.a[e];
     }
-  } else {
-    for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
-      T rv = r[base + n * KB];
-      acc += rv * rv;
+    stv<T, W>(x + t, xv);
+    stv<T, W>(r + t, rv);
+    if (SMOOTH) {
+      const T s = c0 * invd[n];
+#pragma unroll
+      for (int e = 0; e < W; ++e) rv.a[e] *= s;
+      stv<T, W>(z + t, rv);
+      stv<T, W>(dv + t, rv);
     }
   }
-  block_partial<KB>(acc, partial);
+  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
 }
 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_dot(long long N, const T *__restrict__ a, const T *__restrict__ b,
                                              double *__restrict__ partial) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * N * KB + lane;
-  T acc = 0;
-  for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
-    const long long t = base + n * KB;
-    acc += a[t] * b[t];
+  T acc[Map<T, KB>::W] = {};
+  NODE_LOOP(N) {
+    const long long n = g / LPN;
+    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
+    const Vec<T, W> av = ldv<T, W>(a + t), bv = ldv<T, W>(b + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] += av.a[e] * bv.a[e];
   }
-  block_partial<KB>(acc, partial);
+  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
 }
 
 // p = z + beta p
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_p_update(long long N, T *__restrict__ p, const T *__restrict__ z,
                                                   const double *__restrict__ beta) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * N * KB + lane;
-  const T bt = (T)beta[blockIdx.y * KB + lane];
-  for (long long n = blockIdx.x * NPB + threadIdx.x / KB; n < N; n += (long long)gridDim.x * NPB) {
-    const long long t = base + n * KB;
-    p[t] = z[t] + bt * p[t];
+  constexpr int Wc = Map<T, KB>::W;
+  T bt[Wc];
+  {
+    const int qq = threadIdx.x % Map<T, KB>::LPN;
+#pragma unroll
+    for (int e = 0; e < Wc; ++e) bt[e] = (T)beta[blockIdx.y * KB + qq * Wc + e];
+  }
+  NODE_LOOP(N) {
+    const long long n = g / LPN;
+    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
+    Vec<T, W> pv = ldv<T, W>(p + t);
+    const Vec<T, W> zv = ldv<T, W>(z + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + bt[e] * pv.a[e];
+    stv<T, W>(p + t, pv);
   }
 }
 
@@ -289,96 +392,138 @@ __global__ void __launch_bounds__(TPB) k_p_update(long long N, T *__restrict__ p
 template <int KB>
 __global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ coef, const double *__restrict__ b,
                                                      const double *__restrict__ x, double *__restrict__ r64,
-                                                     float *__restrict__ r32, Dims d,
-                                                     const int *__restrict__ active, double *__restrict__ partial) {
-  constexpr int NPB = TPB / KB;
-  const int lane = threadIdx.x % KB;
-  const long long base = (long long)blockIdx.y * d.N * KB + lane;
-  const bool act = active[blockIdx.y * KB + lane] != 0;
-  double acc = 0.0;
-  for (int n = blockIdx.x * NPB + threadIdx.x / KB; n < d.N; n += gridDim.x * NPB) {
+                                                     float *__restrict__ r32, Dims d, const int *__restrict__ active,
+                                                     double *__restrict__ partial) {
+  using T = double;
+  constexpr int Wc = Map<T, KB>::W;
+  double acc[Wc] = {};
+  bool act[Wc];
+  {
+    const int qq = threadIdx.x % Map<T, KB>::LPN;
+#pragma unroll
+    for (int e = 0; e < Wc; ++e) act[e] = active[blockIdx.y * KB + qq * Wc + e] != 0;
+  }
+  NODE_LOOP(d.N) {
+    const int n = (int)(g / LPN);
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = base + (long long)n * KB;
-    double rv = b[t] - stencil_at<double, KB>(coef, x, t, n, i, j, k, d);
-    r64[t] = rv;
-    r32[t] = act ? (float)rv : 0.0f;
-    acc += rv * rv;
+    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+    const Vec<T, W> ax = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
+    Vec<T, W> rv = ldv<T, W>(b + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      rv.a[e] -= ax.a[e];
+      acc[e] += rv.a[e] * rv.a[e];
+      r32[t + e] = act[e] ? (float)rv.a[e] : 0.0f;
+    }
+    stv<T, W>(r64 + t, rv);
   }
-  block_partial<KB>(acc, partial);
+  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
 }
 
-template <int KB>
-__global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total, double *__restrict__ x64,
+__global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total4, double *__restrict__ x64,
                                                        const float *__restrict__ d32) {
-  for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < total; t += (long long)gridDim.x * TPB)
+  // total4 = number of 4-element groups (the blocked arrays are padded to KB >= 1 lanes; tail handled by caller)
+  for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < total4; t += (long long)gridDim.x * TPB) {
+    const float4 dv = reinterpret_cast<const float4 *>(d32)[t];
+    double2 a = reinterpret_cast<double2 *>(x64)[2 * t], b = reinterpret_cast<double2 *>(x64)[2 * t + 1];
+    a.x += dv.x;
+    a.y += dv.y;
+    b.x += dv.z;
+    b.y += dv.w;
+    reinterpret_cast<double2 *>(x64)[2 * t] = a;
+    reinterpret_cast<double2 *>(x64)[2 * t + 1] = b;
+  }
+}
+
+__global__ void k_fill_int(int *__restrict__ a, int n, int v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
+}
+
+__global__ void k_ir_accumulate_tail(long long start, long long total, double *__restrict__ x64,
+                                     const float *__restrict__ d32) {
+  for (long long t = start + (long long)blockIdx.x * TPB + threadIdx.x; t < total; t += (long long)gridDim.x * TPB)
     x64[t] += (double)d32[t];
 }
 
 // ---------------------------------------------------------------- PCG scalars
-// Partials layout: [nb][gx][KB]; RHS r = b*KB + l.
-__device__ __forceinline__ double sum_partial(const double *p, int gx, int KB, int r) {
+// Partials layout: [nb][gx][KB]; RHS r = b*KB + l.  One warp reduces one RHS
+// (lanes stride over the gx block partials), so the scalar kernels cost a few
+// microseconds regardless of K.  Fixed lane order keeps the sums deterministic.
+__device__ __forceinline__ double warp_sum_partial(const double *p, int gx, int KB, int r) {
   const int b = r / KB, l = r % KB;
   const double *q = p + (long long)b * gx * KB + l;
+  const int lane = threadIdx.x & 31;
   double s = 0.0;
-  for (int i = 0; i < gx; ++i) s += q[(long long)i * KB];
+  for (int i = lane; i < gx; i += 32) s += q[(long long)i * KB];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
+
+#define WARP_RHS_LOOP(K) for (int r = threadIdx.x >> 5; r < (K); r += (blockDim.x >> 5))
 
 __global__ void k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
                             const double *__restrict__ rz, const int *__restrict__ active,
                             double *__restrict__ alpha, int *__restrict__ status) {
-  for (int r = threadIdx.x; r < K; r += blockDim.x) {
-    double pq = sum_partial(part_pq, gx, KB, r);
-    double a = 0.0;
-    if (active[r]) {
-      if (!(pq > 0.0) || !isfinite(pq)) {
-        atomicOr(status, 4);  // breakdown / non-finite
-      } else {
-        a = rz[r] / pq;
+  WARP_RHS_LOOP(K) {
+    const double pq = warp_sum_partial(part_pq, gx, KB, r);
+    if ((threadIdx.x & 31) == 0) {
+      double a = 0.0;
+      if (active[r]) {
+        if (!(pq > 0.0) || !isfinite(pq))
+          atomicOr(status, 4);  // breakdown / non-finite
+        else
+          a = rz[r] / pq;
       }
+      alpha[r] = a;
     }
-    alpha[r] = a;
   }
 }
 
-// rz_new = r.z ; rr = |r|^2 ; active &= rr > tol2*bb ; beta = rz_new/rz_old ; counts active
+// rz_new = r.z ; rr = |r|^2 ; active &= rr > tol2[r]*bb ; beta = rz_new/rz_old ; counts active
 __global__ void k_pcg_beta(int K, int KB, int gx, const double *__restrict__ part_rz,
                            const double *__restrict__ part_rr, double *__restrict__ rz,
-                           double *__restrict__ rr_out, const double *__restrict__ bb, double tol2,
-                           int *__restrict__ active, double *__restrict__ beta, int *__restrict__ n_active,
-                           int first) {
+                           double *__restrict__ rr_out, const double *__restrict__ bb, const double *__restrict__ tol2,
+                           int *__restrict__ active, double *__restrict__ beta, int *__restrict__ n_active, int first) {
   __shared__ int cnt;
   if (threadIdx.x == 0) cnt = 0;
   __syncthreads();
-  int mine = 0;
-  for (int r = threadIdx.x; r < K; r += blockDim.x) {
-    double rzn = sum_partial(part_rz, gx, KB, r);
-    double rr = sum_partial(part_rr, gx, KB, r);
-    rr_out[r] = rr;
-    int act = active[r];
-    if (act && !(rr > tol2 * bb[r])) act = 0;
-    if (act && !isfinite(rr)) act = 0;
-    double bt = 0.0;
-    if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
-    if (act) rz[r] = rzn;
-    beta[r] = first ? 0.0 : bt;
-    active[r] = act;
-    mine += act;
+  WARP_RHS_LOOP(K) {
+    const double rzn = warp_sum_partial(part_rz, gx, KB, r);
+    const double rr = warp_sum_partial(part_rr, gx, KB, r);
+    if ((threadIdx.x & 31) == 0) {
+      rr_out[r] = rr;
+      int act = active[r];
+      if (act && !(rr > tol2[r] * bb[r])) act = 0;
+      if (act && !isfinite(rr)) act = 0;
+      double bt = 0.0;
+      if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
+      if (act) rz[r] = rzn;
+      beta[r] = first ? 0.0 : bt;
+      active[r] = act;
+      if (act) atomicAdd(&cnt, 1);
+    }
   }
-  atomicAdd(&cnt, mine);
   __syncthreads();
   if (threadIdx.x == 0) *n_active = cnt;
 }
 
 // per-RHS sums of partials into out (used for |b|^2 and the outer residual norms)
 __global__ void k_sum_partials(int K, int KB, int gx, const double *__restrict__ part, double *__restrict__ out) {
-  for (int r = threadIdx.x; r < K; r += blockDim.x) out[r] = sum_partial(part, gx, KB, r);
+  WARP_RHS_LOOP(K) {
+    const double v = warp_sum_partial(part, gx, KB, r);
+    if ((threadIdx.x & 31) == 0) out[r] = v;
+  }
 }
 
-// outer (refinement) convergence: active = rr > tol2*bb ; counts
-__global__ void k_outer_check(int K, const double *__restrict__ rr, const double *__restrict__ bb, double tol2,
-                              int *__restrict__ active, int *__restrict__ n_active, double *__restrict__ maxrel) {
+// Outer (refinement) convergence: active = rr > rtol2*bb ; counts ; max relative residual.
+// Also the per-RHS tolerance of the next inner solve: the inner solve only has
+// to close the remaining gap (with a factor `safety`), but never asks for less
+// than a floor of inner_tol2 (what fp32 iterations can deliver).
+__global__ void k_outer_check(int K, const double *__restrict__ rr, const double *__restrict__ bb, double rtol2,
+                              int *__restrict__ active, int *__restrict__ n_active, double *__restrict__ maxrel,
+                              double *__restrict__ inner_tol2, double inner_floor2, double safety2) {
   __shared__ int cnt;
   __shared__ double mx[1024];
   if (threadIdx.x == 0) cnt = 0;
@@ -386,11 +531,15 @@ __global__ void k_outer_check(int K, const double *__restrict__ rr, const double
   int mine = 0;
   double m = 0.0;
   for (int r = threadIdx.x; r < K; r += blockDim.x) {
-    int act = (bb[r] > 0.0) && (rr[r] > tol2 * bb[r]);
+    int act = (bb[r] > 0.0) && (rr[r] > rtol2 * bb[r]);
     if (!isfinite(rr[r])) act = 0;
     active[r] = act;
     mine += act;
     if (bb[r] > 0.0) m = fmax(m, sqrt(rr[r] / bb[r]));
+    if (inner_tol2) {
+      double t = (rr[r] > 0.0) ? safety2 * rtol2 * bb[r] / rr[r] : 1.0;
+      inner_tol2[r] = fmin(fmax(t, inner_floor2), 0.25);
+    }
   }
   atomicAdd(&cnt, mine);
   mx[threadIdx.x] = m;
@@ -401,6 +550,10 @@ __global__ void k_outer_check(int K, const double *__restrict__ rr, const double
     *n_active = cnt;
     *maxrel = v;
   }
+}
+
+__global__ void k_fill_double(double *__restrict__ a, int n, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
 }
 
 // ---------------------------------------------------------------- coefficients
@@ -568,9 +721,11 @@ __global__ void k_dense_assemble(const Coef64 *__restrict__ coef, Dims d, double
   }
 }
 
-// In-place right-looking Cholesky (lower) of a dense SPD matrix, one CTA.
+// In-place right-looking Cholesky (lower) of a dense SPD matrix, one CTA:
+// warps own rows of the trailing update, lanes own columns.
 __global__ void __launch_bounds__(1024) k_cholesky(double *__restrict__ A, int n, int *__restrict__ flag) {
   __shared__ double piv;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
       double a = A[(long long)k * n + k];
@@ -584,36 +739,43 @@ __global__ void __launch_bounds__(1024) k_cholesky(double *__restrict__ A, int n
     __syncthreads();
     for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * n + k] /= piv;
     __syncthreads();
-    const int m = n - k - 1;
-    const long long tot = (long long)m * m;
-    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
-      const int ii = k + 1 + (int)(e / m), jj = k + 1 + (int)(e % m);
-      if (jj <= ii) A[(long long)ii * n + jj] -= A[(long long)ii * n + k] * A[(long long)jj * n + k];
+    for (int i = k + 1 + warp; i < n; i += nw) {
+      const double lik = A[(long long)i * n + k];
+      for (int j = k + 1 + lane; j <= i; j += 32) A[(long long)i * n + j] -= lik * A[(long long)j * n + k];
     }
     __syncthreads();
   }
 }
 
-// Column j of A^-1 = L^-T L^-1 e_j, one thread per column; writes row-major (symmetric).
+// Column j of A^-1 = L^-T L^-1 e_j, one warp per column (lanes split the dot
+// products); writes row-major (the inverse is symmetric).
 __global__ void k_chol_inverse(const double *__restrict__ L, int n, double *__restrict__ work,
                                double *__restrict__ Ainv64, float *__restrict__ Ainv32) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (j >= n) return;
   double *y = work + (long long)j * n;
-  for (int i = 0; i < n; ++i) y[i] = 0.0;
-  // forward: L y = e_j
+  for (int i = lane; i < n; i += 32) y[i] = 0.0;
+  __syncwarp();
+  // forward: L y = e_j  (y_i = 0 for i < j)
   for (int i = j; i < n; ++i) {
-    double s = (i == j) ? 1.0 : 0.0;
-    for (int m = j; m < i; ++m) s -= L[(long long)i * n + m] * y[m];
-    y[i] = s / L[(long long)i * n + i];
+    double s = 0.0;
+    for (int m = j + lane; m < i; m += 32) s += L[(long long)i * n + m] * y[m];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) y[i] = ((i == j ? 1.0 : 0.0) - s) / L[(long long)i * n + i];
+    __syncwarp();
   }
   // back: L^T x = y
   for (int i = n - 1; i >= 0; --i) {
-    double s = y[i];
-    for (int m = i + 1; m < n; ++m) s -= L[(long long)m * n + i] * y[m];
-    y[i] = s / L[(long long)i * n + i];
+    double s = 0.0;
+    for (int m = i + 1 + lane; m < n; m += 32) s += L[(long long)m * n + i] * y[m];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) y[i] = (y[i] - s) / L[(long long)i * n + i];
+    __syncwarp();
   }
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += 32) {
     Ainv64[(long long)i * n + j] = y[i];
     Ainv32[(long long)i * n + j] = (float)y[i];
   }
@@ -643,8 +805,8 @@ __global__ void k_unpack(const T *__restrict__ src, long long N, int K, int KB, 
   }
 }
 
-inline int grid_nodes(long long nodes, int KB, int nb, int n_sm) {
-  const long long npb = TPB / KB;
+inline int grid_nodes(long long nodes, int LPN, int nb, int n_sm) {
+  const long long npb = TPB / LPN;
   long long g = (nodes + npb - 1) / npb;
   long long cap = (long long)n_sm * 8 / (nb > 0 ? nb : 1);
   if (cap < 1) cap = 1;
@@ -664,47 +826,57 @@ inline int grid_flat(long long total, int n_sm) {
 }  // namespace
 
 int g_n_sm = 152;
+long long &launch_counter() {
+  static long long c = 0;
+  return c;
+}
 void set_sm_count(int n) { g_n_sm = n > 0 ? n : 152; }
 
-int node_grid(long long nodes, int KB, int nb) { return grid_nodes(nodes, KB, nb, g_n_sm); }
+int node_grid(long long nodes, int KB, int nb) {
+  const int W = KB >= 4 ? 4 : KB;
+  return grid_nodes(nodes, KB / W, nb, g_n_sm);
+}
 
 // ------------------------------------------------------------------ launchers
+template <typename T>
+static const void *coef_ptr(const Level &L) {
+  return std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32;
+}
+template <typename T>
+static const T *invd_ptr(const Level &L) {
+  return reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
+                                                                    : (const void *)L.d_invd32);
+}
+
+#define GRID(NODES) dim3(grid_nodes((NODES), Map<T, KB>::LPN, nb, g_n_sm), nb)
+
 template <typename T, int KB>
 void Ops<T, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
-  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
-      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
-  dim3 g(partial ? gx : grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
   if (partial)
-    k_apply<T, KB, true><<<g, TPB, 0, s>>>(coef, x, y, L.dims, partial);
+    k_apply<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, partial);
   else
-    k_apply<T, KB, false><<<g, TPB, 0, s>>>(coef, x, y, L.dims, nullptr);
+    k_apply<T, KB, false><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nullptr);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s) {
-  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
-      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
-  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
-  k_residual<T, KB><<<g, TPB, 0, s>>>(coef, r, z, res, L.dims);
+  k_residual<T, KB><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), r, z, res, L.dims);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s) {
-  const T *invd = reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
-                                                                              : (const void *)L.d_invd32);
-  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
-  k_cheb_first<T, KB><<<g, TPB, 0, s>>>(invd, r, z, d, L.dims, (T)c0);
+  k_cheb_first<T, KB><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(invd_ptr<T>(L), r, z, d, L.dims, (T)c0);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
-                           cudaStream_t s) {
-  const auto *coef = reinterpret_cast<const typename CoefT<T>::type *>(
-      std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32);
-  const T *invd = reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
-                                                                              : (const void *)L.d_invd32);
-  dim3 g(grid_nodes(L.dims.N, KB, nb, g_n_sm), nb);
-  k_cheb_step<T, KB><<<g, TPB, 0, s>>>(coef, invd, r, zin, zout, d, L.dims, (T)c1, (T)c2);
+                           double *partial, int gx, cudaStream_t s) {
+  if (partial)
+    k_cheb_step<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, d, L.dims,
+                                                          (T)c1, (T)c2, partial);
+  else
+    k_cheb_step<T, KB, false><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, d,
+                                                             L.dims, (T)c1, (T)c2, nullptr);
 }
 
 template <typename T>
@@ -725,36 +897,38 @@ static XferTab make_tab(const Level &f) {
 
 template <typename T, int KB>
 void Ops<T, KB>::restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s) {
-  dim3 g(grid_nodes(c.dims.N, KB, nb, g_n_sm), nb);
-  k_restrict<T, KB><<<g, TPB, 0, s>>>(res, rc, f.dims, c.dims, make_tab<T>(f));
+  k_restrict<T, KB><<<count_launch(GRID(c.dims.N)), TPB, 0, s>>>(res, rc, f.dims, c.dims, make_tab<T>(f));
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s) {
-  dim3 g(grid_nodes(f.dims.N, KB, nb, g_n_sm), nb);
-  k_prolong_add<T, KB><<<g, TPB, 0, s>>>(zc, z, f.dims, c.dims, make_tab<T>(f));
+  k_prolong_add<T, KB><<<count_launch(GRID(f.dims.N)), TPB, 0, s>>>(zc, z, f.dims, c.dims, make_tab<T>(f));
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s) {
-  dim3 g(grid_nodes(nc, KB, nb, g_n_sm), nb);
-  k_coarse_solve<T, KB><<<g, TPB, 0, s>>>(Ainv, nc, rc, zc);
+  k_coarse_solve<T, KB><<<count_launch(GRID(nc)), TPB, 0, s>>>(Ainv, nc, rc, zc);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                           double *partial, int gx, cudaStream_t s) {
-  k_update_xr<T, KB><<<dim3(gx, nb), TPB, 0, s>>>(N, x, r, p, q, alpha, partial);
+                           double *partial, int gx, const Level *smooth, double c0, T *z, T *d, cudaStream_t s) {
+  if (smooth)
+    k_update_xr<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, x, r, p, q, alpha, partial, invd_ptr<T>(*smooth), z, d,
+                                                         (T)c0);
+  else
+    k_update_xr<T, KB, false><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, x, r, p, q, alpha, partial, nullptr, nullptr, nullptr,
+                                                          (T)0);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s) {
-  k_dot<T, KB><<<dim3(gx, nb), TPB, 0, s>>>(N, a, b, partial);
+  k_dot<T, KB><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, a, b, partial);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s) {
-  k_p_update<T, KB><<<dim3(grid_nodes(N, KB, nb, g_n_sm), nb), TPB, 0, s>>>(N, p, z, beta);
+  k_p_update<T, KB><<<count_launch(GRID(N)), TPB, 0, s>>>(N, p, z, beta);
 }
 
 template <typename T, int KB>
@@ -765,69 +939,80 @@ void Ops<T, KB>::copy(long long N, int nb, T *dst, const T *src, cudaStream_t s)
 template <int KB>
 void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
                  const int *active, double *partial, int gx, cudaStream_t s) {
-  k_ir_residual<KB><<<dim3(gx, nb), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, active, partial);
+  k_ir_residual<KB><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, active, partial);
 }
 
 template <int KB>
 void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s) {
   const long long total = N * KB * nb;
-  k_ir_accumulate<KB><<<grid_flat(total, g_n_sm), TPB, 0, s>>>(total, x64, d32);
+  const long long t4 = total / 4;
+  if (t4 > 0) k_ir_accumulate<<<count_launch(grid_flat(t4, g_n_sm)), TPB, 0, s>>>(t4, x64, d32);
+  if (t4 * 4 < total) k_ir_accumulate_tail<<<count_launch(1), TPB, 0, s>>>(t4 * 4, total, x64, d32);
+}
+
+void fill_int(int *a, int n, int v, cudaStream_t s) {
+  if (n > 0) k_fill_int<<<count_launch((n + TPB - 1) / TPB), TPB, 0, s>>>(a, n, v);
 }
 
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
                int *status, cudaStream_t s) {
-  k_pcg_alpha<<<1, 1024, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status);
+  k_pcg_alpha<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status);
 }
 
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
-              const double *bb, double tol2, int *active, double *beta, int *n_active, int first, cudaStream_t s) {
-  k_pcg_beta<<<1, 1024, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta, n_active, first);
+              const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
+              cudaStream_t s) {
+  k_pcg_beta<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta, n_active, first);
 }
 
 void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s) {
-  k_sum_partials<<<1, 1024, 0, s>>>(K, KB, gx, part, out);
+  k_sum_partials<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part, out);
 }
 
-void outer_check(int K, const double *rr, const double *bb, double tol2, int *active, int *n_active,
-                 double *maxrel, cudaStream_t s) {
-  k_outer_check<<<1, 1024, 0, s>>>(K, rr, bb, tol2, active, n_active, maxrel);
+void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
+                 double *maxrel, double *inner_tol2, double inner_floor2, double safety2, cudaStream_t s) {
+  k_outer_check<<<count_launch(1), 1024, 0, s>>>(K, rr, bb, rtol2, active, n_active, maxrel, inner_tol2, inner_floor2, safety2);
+}
+
+void fill_double(double *a, int n, double v, cudaStream_t s) {
+  if (n > 0) k_fill_double<<<count_launch((n + TPB - 1) / TPB), TPB, 0, s>>>(a, n, v);
 }
 
 void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s) {
   BFace bf;
   bf.v = L.d_bface;
   for (int a = 0; a < 6; ++a) bf.off[a] = L.bface_off[a];
-  k_coef_build<<<grid_flat(L.dims.N, g_n_sm), TPB, 0, s>>>(L.d_sigma, L.d_h, L.nx, L.ny, L.nz, bf, robin,
+  k_coef_build<<<count_launch(grid_flat(L.dims.N, g_n_sm)), TPB, 0, s>>>(L.d_sigma, L.d_h, L.nx, L.ny, L.nz, bf, robin,
                                                             L.d_coef64, L.d_coef32, L.d_invd64, L.d_invd32,
                                                             d_lmax_bits);
 }
 
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s) {
   const long long nC = (long long)c.nx * c.ny * c.nz;
-  k_coarsen_sigma<<<grid_flat(nC, g_n_sm), TPB, 0, s>>>(f.d_sigma, f.d_h, f.nx, f.ny, f.nz, c.d_sigma, c.nx, c.ny,
+  k_coarsen_sigma<<<count_launch(grid_flat(nC, g_n_sm)), TPB, 0, s>>>(f.d_sigma, f.d_h, f.nx, f.ny, f.nz, c.d_sigma, c.nx, c.ny,
                                                          c.nz, f.d_r_fi, f.r_off[0], f.r_off[1], f.r_off[2]);
 }
 
 void dense_assemble(const Level &L, double *dense, cudaStream_t s) {
   cudaMemsetAsync(dense, 0, sizeof(double) * L.dims.N * L.dims.N, s);
-  k_dense_assemble<<<grid_flat(L.dims.N, g_n_sm), TPB, 0, s>>>(L.d_coef64, L.dims, dense);
+  k_dense_assemble<<<count_launch(grid_flat(L.dims.N, g_n_sm)), TPB, 0, s>>>(L.d_coef64, L.dims, dense);
 }
 
 void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, float *Ainv32, int *flag,
                             cudaStream_t s) {
-  k_cholesky<<<1, 1024, 0, s>>>(dense, n, flag);
-  k_chol_inverse<<<(n + 31) / 32, 32, 0, s>>>(dense, n, work, Ainv64, Ainv32);
+  k_cholesky<<<count_launch(1), 1024, 0, s>>>(dense, n, flag);
+  k_chol_inverse<<<count_launch((n * 32 + 255) / 256), 256, 0, s>>>(dense, n, work, Ainv64, Ainv32);
 }
 
 template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s) {
   const long long total = N * (long long)KB * nb;
-  k_pack<T><<<grid_flat(total, g_n_sm), TPB, 0, s>>>(src, N, K, KB, dst, total);
+  k_pack<T><<<count_launch(grid_flat(total, g_n_sm)), TPB, 0, s>>>(src, N, K, KB, dst, total);
 }
 
 template <typename T>
 void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s) {
-  k_unpack<T><<<grid_flat(N * K, g_n_sm), TPB, 0, s>>>(src, N, K, KB, dst);
+  k_unpack<T><<<count_launch(grid_flat(N * K, g_n_sm)), TPB, 0, s>>>(src, N, K, KB, dst);
 }
 
 #define DC_INST(T, KB) template struct Ops<T, KB>;

@@ -60,7 +60,7 @@ class DCEngine:
     bface : packed Robin face weights (``boundary.robin_face_weights``) or None (Neumann)
     """
 
-    def __init__(self, h, bface=None, nu_pre=2, nu_post=2, cheb_ratio=6.0, coarse_max=600, check_every=1):
+    def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1):
         if not torch.cuda.is_available():
             raise RuntimeError("the DC engine needs a CUDA device")
         L = lib()
@@ -150,6 +150,14 @@ class DCEngine:
             check(rc)
         return x.reshape(b.shape), info
 
+    def stencil_timing(self, enable):
+        """Start (True) or stop (False) event timing of the fine-level fp32 stencil launches.
+
+        Stopping returns (total_ms, launches, algorithmic_bytes)."""
+        ms, n, b = C.c_double(), C.c_longlong(), C.c_double()
+        check(lib().dc_stencil_timing(self._h, 1 if enable else 0, C.byref(ms), C.byref(n), C.byref(b)))
+        return (ms.value, n.value, b.value) if not enable else None
+
     def release_workspace(self):
         self._ws.clear()
 
@@ -172,6 +180,20 @@ class DCEngine:
         check(lib().dc_dadm_adj(self._h, _ptr(u), _ptr(lam), u.shape[0], _ptr(dsig), float(scale), _ptr(g),
                                 _stream()))
         return g
+
+
+def padded_rhs(k):
+    """RHS count the engine pads k to (blocks of KB lanes, at most 1/8 of them idle)."""
+    for kb in (32, 16, 8, 4, 2, 1):
+        nb = (k + kb - 1) // kb
+        if (nb * kb - k) * 8 <= nb * kb:
+            return nb * kb
+    return k
+
+
+def kernel_launches():
+    """Kernels launched by libdcgpu.so so far (process-wide)."""
+    return int(lib().dc_kernel_launches())
 
 
 def csr_spmv(rowptr, idx, w, x, y, out_idx=None, scale=1.0, accumulate=False):

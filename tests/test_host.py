@@ -178,7 +178,7 @@ def test_library_exports_every_declared_symbol():
     from simpeg_gb300 import _lib
 
     header = (ROOT / "include" / "dcgpu.h").read_text()
-    declared = set(re.findall(r"^\s*(?:int|void|const char \*)\s*(dc_\w+)\s*\(", header, re.M))
+    declared = set(re.findall(r"^\s*(?:int|void|long long|const char \*)\s*(dc_\w+)\s*\(", header, re.M))
     assert declared, "no declarations parsed"
     L = _lib.lib()
     for name in sorted(declared):

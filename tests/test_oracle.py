@@ -173,3 +173,22 @@ def test_operator_hand_checked_2x1x1():
     assert np.isclose(A[0, 1], -0.25)
     assert np.isclose(A[1, 2], -1.5 / 4.0)
     np.testing.assert_allclose(np.asarray(A.sum(axis=1)).ravel(), 0.0, atol=1e-14)
+
+
+def test_oracle_reproduces_golden_fixture():
+    """tests/golden/block_model_oracle.npz (made by tests/golden/make_golden.py) still holds."""
+    import os
+
+    from simpeg_gb300.workloads import block_model_survey
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "block_model_oracle.npz"))
+    mesh, sigma, survey, blocks = block_model_survey(seed=0)
+    np.testing.assert_array_equal(np.log(sigma), g["m"])
+    np.testing.assert_array_equal(np.array(blocks), g["blocks"])
+    o = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
+    o.set_model(g["m"])
+    f = o.fields()
+    np.testing.assert_allclose(o.dpred(f=f), g["dpred"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(o.Jvec(g["m"], g["v"], f=f), g["jvec"], rtol=1e-9, atol=1e-12 * np.abs(g["jvec"]).max())
+    np.testing.assert_allclose(o.Jtvec(g["m"], g["w"], f=f), g["jtvec"], rtol=1e-9,
+                               atol=1e-12 * np.abs(g["jtvec"]).max())
