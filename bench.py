@@ -47,6 +47,7 @@ def _args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
+    ap.add_argument("--sources", type=int, default=0, help="use only the first N sources (profiling runs)")
     return ap.parse_args()
 
 
@@ -59,10 +60,14 @@ def _dist_init(n):
     return dist.get_rank(), dist.get_world_size(), dist
 
 
-def _workload(n_side):
+def _workload(n_side, n_sources=0):
     from simpeg_gb300 import workloads
+    from simpeg_gb300.resistivity.survey import Survey
 
-    return workloads.scale_forward(seed=1, n_side=n_side)
+    mesh, sigma, survey = workloads.scale_forward(seed=1, n_side=n_side)
+    if n_sources:
+        survey = Survey(survey.source_list[:n_sources])
+    return mesh, sigma, survey
 
 
 def _config(mesh, survey):
@@ -160,7 +165,7 @@ def run_reference(args):
     rank, world, dist = _dist_init(args.gpus)
     if rank != 0:
         return
-    mesh, sigma, survey = _workload(args.n_side)
+    mesh, sigma, survey = _workload(args.n_side, args.sources)
     vals = []
     for _ in range(args.warmup):
         pass  # the CPU path has no warm-up state worth priming beyond the first assembly
@@ -208,7 +213,7 @@ def run_gb300(args):
     from simpeg_gb300.engine import csr_spmv, kernel_launches, padded_rhs
     from simpeg_gb300.resistivity import Simulation3DNodal
 
-    mesh, sigma, survey = _workload(args.n_side)
+    mesh, sigma, survey = _workload(args.n_side, args.sources)
     m = np.log(sigma)
     K = survey.nSrc
     sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
