@@ -111,6 +111,26 @@ int dc_csr_spmv(int nrows, const long long *rowptr_dev, const long long *in_idx_
  * term q (sources.py:64-88, simulation.py:265-289). */
 int dc_fill_sparse(long long nnz, const long long *idx_dev, const double *val_dev, double *y_dev, void *stream);
 
+/* Allocation-free variant of dc_dadm_adj.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory when they need the
+ * adjoint model derivative -- a host framework that has reserved the GPU's
+ * memory for its own pool, or a caller that must not take the implicit device
+ * synchronisation of cudaMalloc/cudaFree -- while dc_dadm_adj allocates its
+ * scratch through the handle on first use.  Needs no handle: h_dev holds the
+ * cell widths hx|hy|hz (nx+ny+nz doubles) and bface_dev the packed Robin face
+ * weights of dc_create (NULL: no Robin term), both on the device.  Computes
+ * exactly what dc_dadm_adj computes.  Scratch: a file-scope device array of
+ * 4*DC_NOALLOC_MAX_NODES doubles (36.6 MiB) held by every GPU that loads the
+ * library until exit; meshes with more nodes are rejected with DC_ERR_ARG.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race.  Calls no
+ * cudaMalloc, cudaFree or other allocating routine. */
+#define DC_NOALLOC_MAX_NODES 1200000
+int dc_dadm_adj_noalloc(int nx, int ny, int nz, const double *h_dev, const double *bface_dev, const double *u_dev,
+                        const double *lam_dev, int k, const double *dsig_dev, double scale, double *g_dev,
+                        void *stream);
+
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */
 long long dc_kernel_launches(void);
