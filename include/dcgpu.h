@@ -111,6 +111,33 @@ int dc_csr_spmv(int nrows, const long long *rowptr_dev, const long long *in_idx_
  * term q (sources.py:64-88, simulation.py:265-289). */
 int dc_fill_sparse(long long nnz, const long long *idx_dev, const double *val_dev, double *y_dev, void *stream);
 
+/* diag(J^T W^T W J) for the model map's diagonal derivative dsig (nC; NULL: w.r.t.
+ * sigma), without forming J.  Replaces getJ + the row loop of getJtJdiag
+ * (resistivity/simulation.py:115-154).  phi: column-major (N x nE) pole
+ * solutions A^-1 q_k of the survey's nE unique electrodes (from dc_solve).
+ * Datum d uses source electrodes sa[d], sb[d] (-1: none) with currents
+ * ia[d], ib[d], receiver electrodes rm[d], rn[d] (-1: none) with weights
+ * wm[d], wn[d] (interpolation/apparent-resistivity factors absorbed), and
+ * w2[d] = W_dd^2.  All tables are device arrays.  Needs nE * 116 bytes of
+ * shared memory per block (nE up to ~1950 on GB300); more returns DC_ERR_ARG. */
+int dc_jtj_diag(dc_handle *h, const double *phi, int nE, int nD, const int *sa, const int *sb, const double *ia,
+                const double *ib, const int *rm, const int *rn, const double *wm, const double *wn, const double *w2,
+                const double *dsig, double *diag, void *stream);
+
+/* ---- Generic SPD sparse solver (the simpeg Solver plug-in, simpeg_gb300.solver.GPUSolver) ----
+ * Replaces `solver(A)` / `Ainv * RHS` / `Ainv.clean()` of the pymatsolver
+ * plug-in slot (base/pde_simulation.py:493-511, resistivity/simulation.py:105-111)
+ * for any symmetric positive-definite CSR matrix simpeg assembles.
+ * dc_csr_create: host CSR (int64 indptr[n+1], int32 indices, fp64 data) is
+ * validated and uploaded.  dc_csr_solve: x = A^-1 b for k column-major device
+ * RHS by Jacobi-preconditioned fp64 CG to |b - A x| <= rtol |b| per column. */
+typedef struct dc_csr dc_csr;
+int dc_csr_create(int n, long long nnz, const long long *indptr, const int *indices, const double *data,
+                  dc_csr **out);
+int dc_csr_solve(dc_csr *h, const double *b_dev, double *x_dev, int k, double rtol, int maxit, dc_stats *stats,
+                 void *stream);
+void dc_csr_destroy(dc_csr *h);
+
 /* Allocation-free variant of dc_dadm_adj.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory when they need the
  * adjoint model derivative -- a host framework that has reserved the GPU's
@@ -138,8 +165,9 @@ long long dc_kernel_launches(void);
 /* Event timing of the fine-level fp32 Chebyshev/stencil launches of h.
  * enable = 1: start recording (up to 4096 launches); enable = 0: stop and
  * return the summed device time, the number of timed launches and their
- * algorithmic bytes (N*(20*K + 20): read z, r, d, write d, z in fp32 plus
- * 16-byte coefficients and the 4-byte inverse diagonal per node).
+ * algorithmic bytes (per node: 16*K for a step with the momentum term --
+ * read x_k, r, x_{k-1}, write x_{k+1} in fp32 -- or 12*K without it, plus
+ * 16-byte coefficients and the 4-byte inverse diagonal).
  * Instrumentation; no reference counterpart. */
 int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *launches, double *alg_bytes);
 

@@ -65,6 +65,12 @@ _SIG = {
     "dc_fill_sparse": (C.c_int, [C.c_longlong, _DP, _DP, _DP, _VP]),
     "dc_dadm_adj_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _DP, _DP, _DP, _DP, C.c_int, _DP, C.c_double,
                                       _DP, _VP]),
+    "dc_csr_create": (C.c_int, [C.c_int, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
+                                C.POINTER(C.c_double), C.POINTER(_VP)]),
+    "dc_csr_solve": (C.c_int, [_VP, _DP, _DP, C.c_int, C.c_double, C.c_int, C.POINTER(dc_stats), _VP]),
+    "dc_csr_destroy": (None, [_VP]),
+    "dc_jtj_diag": (C.c_int, [_VP, _DP, C.c_int, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP,
+                              _VP]),
     "dc_kernel_launches": (C.c_longlong, []),
     "dc_stencil_timing": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double)]),

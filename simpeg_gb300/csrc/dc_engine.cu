@@ -137,6 +137,7 @@ void set_dims(Level &L) {
   L.dims.N = (long long)L.dims.Nx * L.dims.Ny * L.dims.Nz;
   L.dims.mx = div_magic((unsigned)L.dims.Nx);
   L.dims.mxy = div_magic((unsigned)(L.dims.Nx * L.dims.Ny));
+  L.dims.mn = div_magic((unsigned)L.dims.N);
 }
 
 struct Cheb {
@@ -297,9 +298,11 @@ struct Carve {
 };
 
 int pick_kb(int k) {
-  // largest KB in {32,16,8,4,2,1} whose padding wastes at most 1/8 of the lanes
+  // largest KB in {32,16,8,4,2,1} whose padding wastes at most 1/8 of the lanes,
+  // among those that keep the RHS blocks within kMaxRhsBlocks
   for (int kb = 32; kb >= 1; kb >>= 1) {
     const int nb = (k + kb - 1) / kb;
+    if (nb > kMaxRhsBlocks) return kb * 2 > 32 ? 32 : kb * 2;
     if ((long long)(nb * kb - k) * 8 <= (long long)nb * kb) return kb;
   }
   return 1;
@@ -307,7 +310,7 @@ int pick_kb(int k) {
 
 template <typename T>
 struct MGWork {
-  std::vector<T *> r, z, z2, d, res;
+  std::vector<T *> r, z, z2, res;
 };
 
 struct Scal {
@@ -322,7 +325,6 @@ void carve_mg(Carve &c, const dc_handle *h, int Kp, MGWork<T> &w) {
   w.r.assign(L, nullptr);
   w.z.assign(L, nullptr);
   w.z2.assign(L, nullptr);
-  w.d.assign(L, nullptr);
   w.res.assign(L, nullptr);
   for (int l = 0; l < L; ++l) {
     const size_t n = (size_t)h->lv[l].dims.N * Kp;
@@ -332,7 +334,6 @@ void carve_mg(Carve &c, const dc_handle *h, int Kp, MGWork<T> &w) {
     }
     if (l + 1 < L || L == 1) {
       w.z2[l] = c.take<T>(n);
-      w.d[l] = c.take<T>(n);
       w.res[l] = c.take<T>(n);
     }
   }
@@ -370,12 +371,23 @@ struct SolveWS {
   size_t bytes;
 };
 
+int red_per_sm(int KB) {
+  switch (KB) {
+    case 32: return std::min(Ops<float, 32>::red_blocks_per_sm(), Ops<double, 32>::red_blocks_per_sm());
+    case 16: return std::min(Ops<float, 16>::red_blocks_per_sm(), Ops<double, 16>::red_blocks_per_sm());
+    case 8: return std::min(Ops<float, 8>::red_blocks_per_sm(), Ops<double, 8>::red_blocks_per_sm());
+    case 4: return std::min(Ops<float, 4>::red_blocks_per_sm(), Ops<double, 4>::red_blocks_per_sm());
+    case 2: return std::min(Ops<float, 2>::red_blocks_per_sm(), Ops<double, 2>::red_blocks_per_sm());
+    default: return std::min(Ops<float, 1>::red_blocks_per_sm(), Ops<double, 1>::red_blocks_per_sm());
+  }
+}
+
 void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
   w.KB = pick_kb(k);
   w.nb = (k + w.KB - 1) / w.KB;
   w.Kp = w.nb * w.KB;
   const long long N = h->lv[0].dims.N;
-  w.gx = node_grid(N, w.KB, w.nb);
+  w.gx = node_grid(N, w.KB, w.nb, red_per_sm(w.KB));
   Carve c{base};
   const size_t n = (size_t)N * w.Kp;
   w.B64 = c.take<double>(n);
@@ -409,51 +421,56 @@ const double *ainv<double>(const dc_handle *h) { return h->d_Ainv64; }
 // Chebyshev step; the fine-level fp32 launches are bracketed by events when
 // stencil timing is on (dc_stencil_timing).
 template <typename T, int KB>
-void timed_cheb(const dc_handle *hc, int l, const Level &F, const T *r, const T *zin, T *zout, T *d, int nb,
+void timed_cheb(const dc_handle *hc, int l, const Level &F, const T *r, const T *zin, T *zout, int prev, int nb,
                 double c1, double c2, double *partial, int gx, cudaStream_t s) {
   dc_handle *h = const_cast<dc_handle *>(hc);
   const bool rec = h->prof && l == 0 && sizeof(T) == 4 && h->prof_used + 2 <= (int)h->prof_ev.size();
   if (rec) cudaEventRecord(h->prof_ev[h->prof_used], s);
-  Ops<T, KB>::cheb_step(F, r, zin, zout, d, nb, c1, c2, partial, gx, s);
+  Ops<T, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s);
   if (rec) {
     cudaEventRecord(h->prof_ev[h->prof_used + 1], s);
     h->prof_used += 2;
-    h->prof_bytes += (double)F.dims.N * (20.0 * KB * nb + 20.0);
+    // algorithmic bytes: x_k, r (+ x_{k-1}) read, x_{k+1} written, fp32; coefficients and 1/diag per node
+    h->prof_bytes += (double)F.dims.N * ((prev == 1 ? 16.0 : 12.0) * KB * nb + 20.0);
   }
 }
 
 // Buffer that receives the first pre-smoothing step of level l, chosen so that
-// after (nu_pre - 1) + nu_post ping-pong swaps the result lands in z.
+// after (nu_pre - 1) + nu_post ping-pong steps the result lands in z.
 template <typename T>
 T *first_buffer(const dc_handle *h, int l, T *z, const MGWork<T> &w) {
-  const int swaps = (h->nu_pre - 1) + h->nu_post;
-  return (swaps % 2) ? w.z2[l] : z;
+  const int steps = (h->nu_pre - 1) + h->nu_post;
+  return (steps % 2) ? w.z2[l] : z;
 }
 
 // One V-cycle z = M r from level l.  If `pre_done`, the first Chebyshev step
-// (z1 = d = D^-1 r / theta into first_buffer) was already applied by the caller.
+// (z1 = D^-1 r / theta into first_buffer) was already applied by the caller.
 // If `dot_partial`, the last smoothing step also emits per-block partials of r.z.
+// Two buffers per level (z and z2) alternate: every step writes the one that
+// does not hold the current iterate, which also holds the previous iterate
+// the three-term recurrence needs.
 template <typename T, int KB>
 void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int nb, cudaStream_t s,
             bool pre_done = false, double *dot_partial = nullptr, int gx = 0) {
   using O = Ops<T, KB>;
   const int L = (int)h->lv.size();
   if (l == L - 1) {
-    O::coarse_solve(ainv<T>(h), h->nc, r, z, nb, s);
+    O::coarse_solve(ainv<T>(h), h->lv.back(), r, z, nb, s);
     return;
   }
   const Level &F = h->lv[l];
   const Level &C = h->lv[l + 1];
   const Cheb cp = cheb_params(F.lmax, h->cheb_ratio);
   T *cur = first_buffer(h, l, z, w);
-  T *oth = (cur == z) ? w.z2[l] : z;
+  auto other = [&](T *c) { return c == z ? w.z2[l] : z; };
   // pre-smoothing from zero
-  if (!pre_done) O::cheb_first(F, r, cur, w.d[l], nb, 1.0 / cp.theta, s);
+  if (!pre_done) O::cheb_first(F, r, cur, nb, 1.0 / cp.theta, s);
   double rho_old = 1.0 / cp.sigma1;
   for (int it = 1; it < h->nu_pre; ++it) {
     const double rho = 1.0 / (2.0 * cp.sigma1 - rho_old);
-    timed_cheb<T, KB>(h, l, F, r, cur, oth, w.d[l], nb, rho * rho_old, 2.0 * rho / cp.delta, nullptr, 0, s);
-    std::swap(cur, oth);
+    T *out = other(cur);
+    timed_cheb<T, KB>(h, l, F, r, cur, out, it == 1 ? 2 : 1, nb, rho * rho_old, 2.0 * rho / cp.delta, nullptr, 0, s);
+    cur = out;
     rho_old = rho;
   }
   // coarse-grid correction
@@ -475,8 +492,9 @@ void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int
       rho_old = rho;
     }
     const bool last = it + 1 == h->nu_post;
-    timed_cheb<T, KB>(h, l, F, r, cur, oth, w.d[l], nb, c1, c2, last ? dot_partial : nullptr, gx, s);
-    std::swap(cur, oth);
+    T *out = other(cur);
+    timed_cheb<T, KB>(h, l, F, r, cur, out, it == 0 ? 0 : 1, nb, c1, c2, last ? dot_partial : nullptr, gx, s);
+    cur = out;
   }
   if (cur != z) cudaMemcpyAsync(z, cur, sizeof(T) * F.dims.N * KB * nb, cudaMemcpyDeviceToDevice, s);
 }
@@ -501,6 +519,7 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
   sum_partials(Kp, KB, gx, sc.part_b, sc.bb, s);
   vcycle<T, KB>(h, 0, r, z, w, nb, s, false, sc.part_c, gx);
   if (!fused) O::dot(N, nb, r, z, sc.part_c, gx, s);
+  CK(cudaMemsetAsync(sc.n_active, 0, sizeof(int), s));
   pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 1, s);
   O::copy(N, nb, p, z, s);
   const Cheb cp0 = cheb_params(F.lmax, h->cheb_ratio);
@@ -509,12 +528,12 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
   int since = 0;
   for (it = 0; it < maxit; ++it) {
     O::apply(F, p, q, nb, sc.part_a, gx, s);
-    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, s);
+    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, sc.n_active, s);
     if (fused) {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, 1.0 / cp0.theta, z1, w.d[0], s);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, 1.0 / cp0.theta, z1, s);
       vcycle<T, KB>(h, 0, r, z, w, nb, s, true, sc.part_c, gx);
     } else {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, s);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, s);
       vcycle<T, KB>(h, 0, r, z, w, nb, s);
       O::dot(N, nb, r, z, sc.part_c, gx, s);
     }
@@ -553,6 +572,13 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
   const long long N = F.dims.N;
   const int nb = w.nb, Kp = w.Kp, gx = w.gx;
   pack_colmajor<double>(b, N, k, KB, nb, w.B64, s);
+  if (!h->robin) {
+    // Neumann: the reference pins row 0 of A to the identity
+    // (resistivity/simulation.py:535-540).  Its solution solves the symmetric
+    // singular system with row 0 of the RHS replaced by -(sum of the other
+    // rows) (the compatible RHS), shifted so that u_0 = b_0.
+    neumann_rhs(b, N, k, KB, w.B64, w.sc.rr64, s);
+  }
   CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));
   int total_it = 0, outer = 0, status = 0;
   if (mode == DC_MODE_FP64) {
@@ -578,7 +604,7 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
                 inner_rtol * inner_rtol, kSafety2, s);
-    pack_colmajor<float>(b, N, k, KB, nb, w.r32, s);
+    convert_d2f(w.B64, (long long)N * Kp, w.r32, s);
     const int max_outer = 30;
     for (outer = 0; outer < max_outer;) {
       CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -605,6 +631,7 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     if (outer >= max_outer) status = DC_ERR_NOT_CONVERGED;
   }
   unpack_colmajor<double>(w.X64, N, k, KB, x, s);
+  if (!h->robin) neumann_shift(b, N, k, x, s);
   CK(cudaMemcpyAsync(h->h_maild, w.sc.maxrel, sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));
@@ -747,12 +774,15 @@ int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
   }
   CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), s));
   dense_assemble(h->lv.back(), h->d_dense, s);
+  // The Neumann operator is singular (constants); its coarsest matrix is
+  // pinned at node 0 so that the V-cycle stays an SPD preconditioner.
+  if (!h->robin) dense_pin0(h->d_dense, h->nc, s);
   dense_cholesky_inverse(h->d_dense, h->d_work, h->nc, h->d_Ainv64, h->d_Ainv32, h->d_flag, s);
   int flag = 0;
   CK(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
-  if (flag) return fail(DC_ERR_ARG, "coarsest operator is not positive definite (Neumann operator or bad sigma)");
+  if (flag) return fail(DC_ERR_ARG, "coarsest operator is not positive definite (bad sigma)");
   h->model_set = true;
   return 0;
 }
@@ -767,8 +797,12 @@ int dc_apply(dc_handle *h, const double *x, double *y, int k, void *stream) {
 
 int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes) {
   if (!h || !bytes || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (k > 32 * kMaxRhsBlocks) k = 32 * kMaxRhsBlocks;
   if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
-  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model first");
+  if (!h->built) {
+    int rc = build_hierarchy(h);
+    if (rc) return rc;
+  }
   SolveWS w;
   layout_ws(h, mode, k, nullptr, w);
   *bytes = w.bytes;
@@ -778,6 +812,28 @@ int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes) {
 int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
              int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream) {
   if (!h || !b || !x || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  const int kmax = 32 * kMaxRhsBlocks;
+  if (k > kmax) {
+    // solve in chunks of kmax right-hand sides (one RHS-block sweep each)
+    if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+    const long long N = h->lv[0].dims.N;
+    dc_stats agg{0, 0, 0, (int)h->lv.size(), 0.0};
+    int rc_all = 0;
+    for (int c0 = 0; c0 < k; c0 += kmax) {
+      const int kc = std::min(kmax, k - c0);
+      dc_stats st{};
+      int rc = dc_solve(h, mode, b + (size_t)c0 * N, x + (size_t)c0 * N, kc, rtol, maxit, inner_rtol, inner_maxit,
+                        ws, ws_bytes, &st, stream);
+      agg.iterations = std::max(agg.iterations, st.iterations);
+      agg.outer = std::max(agg.outer, st.outer);
+      agg.max_rel_res = std::max(agg.max_rel_res, st.max_rel_res);
+      if (rc && rc != DC_ERR_NOT_CONVERGED) return rc;
+      if (rc) rc_all = rc;
+    }
+    agg.status = rc_all;
+    if (stats) *stats = agg;
+    return rc_all ? fail(rc_all, "solver did not reach the requested tolerance") : 0;
+  }
   if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
   if (!(rtol > 0.0) || maxit < 1) return fail(DC_ERR_ARG, "rtol must be > 0 and maxit >= 1");
   if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
@@ -862,7 +918,21 @@ int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const d
   return 0;
 }
 
-long long dc_kernel_launches(void) { return dc::launch_counter(); }
+long long dc_kernel_launches(void) { return dc::launch_counter().load(); }
+
+int dc_jtj_diag(dc_handle *h, const double *phi, int nE, int nD, const int *sa, const int *sb, const double *ia,
+                const double *ib, const int *rm, const int *rn, const double *wm, const double *wn, const double *w2,
+                const double *dsig, double *diag, void *stream) {
+  if (!h || !phi || nE < 1 || nD < 0 || !diag) return fail(DC_ERR_ARG, "bad argument");
+  if (nD > 0 && (!sa || !sb || !ia || !ib || !rm || !rn || !wm || !wn || !w2))
+    return fail(DC_ERR_ARG, "NULL datum table");
+  if (!h->built) {
+    int rc = build_hierarchy(h);
+    if (rc) return rc;
+  }
+  return jtj_diag_launch(h->lv[0], h->robin, phi, nE, nD, sa, sb, ia, ib, rm, rn, wm, wn, w2, dsig, diag,
+                         (cudaStream_t)stream);
+}
 
 int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *launches, double *alg_bytes) {
   if (!h) return fail(DC_ERR_ARG, "handle is NULL");

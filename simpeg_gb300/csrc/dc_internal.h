@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -29,10 +30,14 @@ struct Dims {
   int Nx, Ny, Nz;    // nodes per axis
   long long N;       // nodes
   unsigned mx, mxy;  // division magic for Nx and Nx*Ny (see fast_div in dc_stencil.cu)
+  unsigned mn;       // division magic for N
 };
 
 // floor(2^32 / d) + 1: with q = umulhi(n, m), floor(n / d) is q or q - 1 for 0 <= n < 2^31, d >= 2.
-inline unsigned div_magic(unsigned d) { return (unsigned)(0x100000000ull / d + 1ull); }
+inline unsigned div_magic(unsigned d) { return d > 1 ? (unsigned)(0x100000000ull / d + 1ull) : 0u; }
+
+// Largest number of RHS blocks one solve kernel handles (k <= 32 * KB).
+constexpr int kMaxRhsBlocks = 32;
 
 // 1D transfer tables between a fine axis (nf nodes) and its coarse axis (nc nodes).
 struct Axis1D {
@@ -71,30 +76,38 @@ struct Level {
 
 // Every kernel launch of the engine passes its grid through count_launch(),
 // which counts launches for dc_kernel_launches().
-long long &launch_counter();
+std::atomic<long long> &launch_counter();
 inline dim3 count_launch(dim3 g) {
-  ++launch_counter();
+  launch_counter().fetch_add(1, std::memory_order_relaxed);
   return g;
 }
 
 // ---- dc_stencil.cu -----------------------------------------------------------
 void set_sm_count(int n);
-int node_grid(long long nodes, int KB, int nb);
+// grid of the reduction kernels: one block per (node group) up to per_sm resident blocks per SM
+int node_grid(long long nodes, int KB, int nb, int per_sm);
 
 template <typename T, int KB> struct Ops {
+  // resident blocks per SM of the slowest-occupancy reduction kernel
+  static int red_blocks_per_sm();
   // y = A x ; if partial: per-block partial sums of x.y
   static void apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
   static void residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s);
-  static void cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s);
-  // with partial: also per-block partials of r . zout
-  static void cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
+  // z = c0 D^-1 r (first Chebyshev step from zero)
+  static void cheb_first(const Level &L, const T *r, T *z, int nb, double c0, cudaStream_t s);
+  // zout = zin + c1 (zin - prev) + c2 D^-1 (r - A zin); prev: 0 none, 1 = zout's old content, 2 = zero.
+  // With partial: also per-block partials of r . zout.
+  static void cheb_step(const Level &L, const T *r, const T *zin, T *zout, int prev, int nb, double c1, double c2,
                         double *partial, int gx, cudaStream_t s);
+  template <bool DOT, int PREV>
+  static void cheb_launch(const Level &L, const T *r, const T *zin, T *zout, int nb, double c1, double c2,
+                          double *partial, int gx, cudaStream_t s);
   static void restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s);
   static void prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s);
-  static void coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s);
-  // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = d = c0 D^-1 r on that level.
+  static void coarse_solve(const T *Ainv, const Level &c, const T *rc, T *zc, int nb, cudaStream_t s);
+  // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = c0 D^-1 r on that level.
   static void update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                        double *partial, int gx, const Level *smooth, double c0, T *z, T *d, cudaStream_t s);
+                        double *partial, int gx, const Level *smooth, double c0, T *z, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
   static void p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s);
   static void copy(long long N, int nb, T *dst, const T *src, cudaStream_t s);
@@ -107,8 +120,9 @@ template <int KB>
 void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s);
 
 void fill_int(int *a, int n, int v, cudaStream_t s);
+// alpha = rz / (p.q) per active RHS; also zeroes *n_active for the pcg_beta of the same iteration
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
-               int *status, cudaStream_t s);
+               int *status, int *n_active, cudaStream_t s);
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
               const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
               cudaStream_t s);
@@ -123,6 +137,12 @@ void dense_assemble(const Level &L, double *dense, cudaStream_t s);
 void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, float *Ainv32, int *flag,
                             cudaStream_t s);
 
+// Neumann (row-0 pinned) solves, see dc_solve
+void dense_pin0(double *A, int n, cudaStream_t s);
+void neumann_rhs(const double *b, long long N, int K, int KB, double *B, double *sums, cudaStream_t s);
+void neumann_shift(const double *b, long long N, int K, double *x, cudaStream_t s);
+void convert_d2f(const double *a, long long n, float *o, cudaStream_t s);
+
 template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s);
 template <typename T>
@@ -136,6 +156,11 @@ void scale_vec(long long n, double *y, double a, cudaStream_t s);
 void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s);
 void cell_gradient(const Level &L, int robin, const double *P, const double *Q, const double *dsig, double scale,
                    double *g, cudaStream_t s);
+
+// ---- dc_jtj.cu -------------------------------------------------------------
+int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD, const int *sa, const int *sb,
+                    const double *ia, const double *ib, const int *rm, const int *rn, const double *wm,
+                    const double *wn, const double *w2, const double *dsig, double *diag, cudaStream_t stream);
 
 std::string &last_error();
 

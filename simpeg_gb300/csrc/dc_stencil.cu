@@ -2,14 +2,18 @@
 // DC engine.  Every kernel here is bandwidth-bound except the fp64 stencil,
 // which on this part is bounded by fp64 issue rate (see the design notes).
 //
-// Thread mapping of every "node" kernel: blockDim = 256 = NPB nodes x KB lanes
-// (NPB = 256 / KB); blockIdx.y = RHS block; blockIdx.x strides over node
-// groups.  Lane l of node n in RHS block b touches element (b*N + n)*KB + l,
-// so a warp's loads are contiguous.
+// Thread mapping of every "node" kernel: a thread owns W consecutive RHS lanes
+// (16 bytes) of one node, KB/W threads share a node, and a 1D grid sweeps the
+// flat (RHS block, node) index with the RHS block slowest.  Lane l of node n
+// in RHS block b is element (b*N + n)*KB + l, so a warp's loads are contiguous.
 #include "dc_internal.h"
 
 #include <cstdio>
+#include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 
 namespace dc {
 
@@ -19,6 +23,7 @@ constexpr int TPB = 256;
 
 // floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
 __device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
+  if (d == 1) return n;
   unsigned q = __umulhi((unsigned)n, m);
   q -= (q * (unsigned)d > (unsigned)n) ? 1u : 0u;
   return (int)q;
@@ -55,11 +60,17 @@ __device__ __forceinline__ void stv(T *p, const Vec<T, W> &v) {
 }
 
 // Per-thread geometry of the "node x lane-group" mapping.  LPN threads share
-// one node (each owning W consecutive RHS lanes); blockIdx.y is the RHS block.
+// one node (each owning W consecutive RHS lanes of one RHS block).  Kernels
+// sweep the RHS blocks one after the other (RHS block = slowest index of the
+// flat work index), so the L2 working set of the stencil's z-neighbour planes
+// is that of one RHS block at a time.
 template <typename T, int KB> struct Map {
   static constexpr int W = VWidth<T, KB>::v;
   static constexpr int LPN = KB / W;  // threads per node
 };
+
+// Largest number of RHS blocks a reduction kernel accepts (K <= 32 * KB).
+constexpr int MAXNB = kMaxRhsBlocks;
 
 template <typename T, int KB>
 __device__ __forceinline__ const typename CoefT<T>::type *coef_of(const void *c) {
@@ -90,68 +101,92 @@ __device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *
   return acc;
 }
 
-// Block reduction of W per-thread sums (lanes q*W .. q*W+W-1 of the RHS block)
-// into partial[(blockIdx.y * gridDim.x + blockIdx.x) * KB + lane].
-template <int KB, int W, int LPN, typename A>
-__device__ __forceinline__ void block_partial(A (&v)[W], double *partial) {
-  __shared__ double red[TPB / 32][32][W];
-#pragma unroll
-  for (int e = 0; e < W; ++e) {
-#pragma unroll
-    for (int off = 16; off >= LPN; off >>= 1) v[e] += __shfl_xor_sync(0xffffffffu, v[e], off);
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane < LPN) {
-#pragma unroll
-    for (int e = 0; e < W; ++e) red[warp][lane][e] = (double)v[e];
-  }
-  __syncthreads();
-  if (threadIdx.x < KB) {
-    const int q = threadIdx.x / W, e = threadIdx.x % W;
-    double s = 0.0;
-#pragma unroll
-    for (int w = 0; w < TPB / 32; ++w) s += red[w][q][e];
-    partial[((long long)blockIdx.y * gridDim.x + blockIdx.x) * KB + threadIdx.x] = s;
-  }
-}
+// Sweep over (RHS block b, node n, lane group q) with b slowest.  Defines W,
+// LPN, q and, per iteration, ng (flat node index over all RHS blocks), b, n and
+// t (offset of the thread's W lanes).
+#define SWEEP(NN, MAGIC, NB)                                                                   \
+  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;                                      \
+  const int q = threadIdx.x % LPN;                                                             \
+  const long long total_ = (long long)(NN) * (NB) * LPN;                                       \
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total_; g += (long long)gridDim.x * TPB)
 
-#define NODE_LOOP(NNODES)                                                                  \
-  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;                                  \
-  const int q = threadIdx.x % LPN;                                                         \
-  const long long stride = (long long)gridDim.x * TPB;                                     \
-  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g / LPN < (NNODES); g += stride)
+#define SWEEP_INDEX(NN, MAGIC)                        \
+  const int ng = (int)(g / LPN);                      \
+  const int b = fast_div(ng, (int)(NN), (MAGIC));     \
+  const int n = ng - b * (int)(NN);                   \
+  const long long t = (long long)ng * KB + q * W;     \
+  (void)b;                                            \
+  (void)n;
+
+// Per-(RHS block, lane) partial sums: threads add their running sums into
+// shared memory when they move to the next RHS block, then the block writes
+// partial[(b * gridDim.x + blockIdx.x) * KB + lane].
+template <typename T, int KB>
+struct BlockRed {
+  static constexpr int W = Map<T, KB>::W;
+  T acc[W];
+  int cur;
+  __device__ __forceinline__ void init(T *red, int nb) {
+    for (int i = threadIdx.x; i < nb * KB; i += TPB) red[i] = (T)0;
+    cur = -1;
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] = (T)0;
+    __syncthreads();
+  }
+  __device__ __forceinline__ void flush(T *red, int q) {
+    if (cur >= 0) {
+#pragma unroll
+      for (int e = 0; e < W; ++e) atomicAdd(&red[cur * KB + q * W + e], acc[e]);
+    }
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] = (T)0;
+  }
+  __device__ __forceinline__ void at(T *red, int b, int q) {
+    if (b != cur) {
+      flush(red, q);
+      cur = b;
+    }
+  }
+  __device__ __forceinline__ void finish(T *red, int q, int nb, double *partial) {
+    flush(red, q);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb * KB; i += TPB)
+      partial[((long long)(i / KB) * gridDim.x + blockIdx.x) * KB + (i % KB)] = (double)red[i];
+  }
+};
 
 // ---------------------------------------------------------------- stencil ops
 template <typename T, int KB, bool DOT>
 __global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
-                                               T *__restrict__ y, Dims d, double *__restrict__ partial) {
+                                               T *__restrict__ y, Dims d, int nb, double *__restrict__ partial) {
   const auto *coef = coef_of<T, KB>(cf);
-  T acc[Map<T, KB>::W] = {};
-  NODE_LOOP(d.N) {
-    const int n = (int)(g / LPN);
+  __shared__ T red[DOT ? MAXNB * KB : 1];
+  BlockRed<T, KB> R;
+  if (DOT) R.init(red, nb);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
     const Vec<T, W> v = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
     stv<T, W>(y + t, v);
     if (DOT) {
+      R.at(red, b, q);
       const Vec<T, W> xv = ldv<T, W>(x + t);
 #pragma unroll
-      for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
+      for (int e = 0; e < W; ++e) R.acc[e] += v.a[e] * xv.a[e];
     }
   }
-  if (DOT) block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
+  if (DOT) R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
 }
 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, const T *__restrict__ r,
-                                                  const T *__restrict__ z, T *__restrict__ res, Dims d) {
+                                                  const T *__restrict__ z, T *__restrict__ res, Dims d, int nb) {
   const auto *coef = coef_of<T, KB>(cf);
-  NODE_LOOP(d.N) {
-    const int n = (int)(g / LPN);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
     const Vec<T, W> az = stencil_vec<T, KB, W>(coef, z, t, n, i, j, k, d);
     Vec<T, W> rv = ldv<T, W>(r + t);
 #pragma unroll
@@ -160,51 +195,57 @@ __global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, c
   }
 }
 
-// First Chebyshev step from z = 0: d = c0 * D^-1 r ; z = d.
+// First Chebyshev step from z = 0: z = c0 * D^-1 r.
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, const T *__restrict__ r,
-                                                    T *__restrict__ z, T *__restrict__ dv, Dims d, T c0) {
-  NODE_LOOP(d.N) {
-    const int n = (int)(g / LPN);
-    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
+                                                    T *__restrict__ z, Dims d, int nb, T c0) {
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     const T s = c0 * invd[n];
     Vec<T, W> v = ldv<T, W>(r + t);
 #pragma unroll
     for (int e = 0; e < W; ++e) v.a[e] *= s;
     stv<T, W>(z + t, v);
-    stv<T, W>(dv + t, v);
   }
 }
 
-// Chebyshev step: d = c1 d + c2 D^-1 (r - A zin) ; zout = zin + d.  With DOT,
-// also per-block partials of r . zout (the PCG's r.z after the V-cycle).
-template <typename T, int KB, bool DOT>
+// Chebyshev step in three-term form (x_{k+1} = x_k + c1 (x_k - x_{k-1}) + c2 D^-1 (r - A x_k)):
+//   PREV = 0: no momentum term (first step from a nonzero start, c1 = 0)
+//   PREV = 1: x_{k-1} read from zout (overwritten in place with x_{k+1})
+//   PREV = 2: x_{k-1} = 0 (second step of a zero-start sequence)
+// Four streams per RHS lane (x_k, r, x_{k-1} read; x_{k+1} write) instead of the
+// five of the d-vector form.  With DOT, also per-block partials of r . x_{k+1}.
+template <typename T, int KB, bool DOT, int PREV>
 __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
                                                    const T *__restrict__ r, const T *__restrict__ zin,
-                                                   T *__restrict__ zout, T *__restrict__ dv, Dims d, T c1, T c2,
+                                                   T *zout, Dims d, int nb, T c1, T c2,
                                                    double *__restrict__ partial) {
   const auto *coef = coef_of<T, KB>(cf);
-  T acc[Map<T, KB>::W] = {};
-  NODE_LOOP(d.N) {
-    const int n = (int)(g / LPN);
+  __shared__ T red[DOT ? MAXNB * KB : 1];
+  BlockRed<T, KB> R;
+  if (DOT) R.init(red, nb);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
     const Vec<T, W> az = stencil_vec<T, KB, W>(coef, zin, t, n, i, j, k, d);
     const Vec<T, W> rv = ldv<T, W>(r + t);
-    Vec<T, W> dd = ldv<T, W>(dv + t);
-    Vec<T, W> zo = ldv<T, W>(zin + t);
+    const Vec<T, W> zc = ldv<T, W>(zin + t);
+    Vec<T, W> zo;
+    if (PREV == 1) zo = ldv<T, W>(zout + t);
     const T s = c2 * invd[n];
+    if (DOT) R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      dd.a[e] = c1 * dd.a[e] + s * (rv.a[e] - az.a[e]);
-      zo.a[e] += dd.a[e];
-      if (DOT) acc[e] += rv.a[e] * zo.a[e];
+      T mom = (T)0;
+      if (PREV == 1) mom = c1 * (zc.a[e] - zo.a[e]);
+      if (PREV == 2) mom = c1 * zc.a[e];
+      zo.a[e] = zc.a[e] + mom + s * (rv.a[e] - az.a[e]);
+      if (DOT) R.acc[e] += rv.a[e] * zo.a[e];
     }
-    stv<T, W>(dv + t, dd);
     stv<T, W>(zout + t, zo);
   }
-  if (DOT) block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
+  if (DOT) R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
 }
 
 // ---------------------------------------------------------------- transfers
@@ -218,17 +259,17 @@ struct XferTab {
 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *__restrict__ rc, Dims f, Dims c,
-                                                  XferTab tb) {
+                                                  int nb, XferTab tb) {
   const T *wl = (const T *)tb.wl, *wr = (const T *)tb.wr;
-  NODE_LOOP(c.N) {
-    const int n = (int)(g / LPN);
+  SWEEP(c.N, c.mn, nb) {
+    SWEEP_INDEX(c.N, c.mn)
     int I, J, K;
     node_ijk(n, c, I, J, K);
     const int fx = tb.fi[tb.roff[0] + I], fy = tb.fi[tb.roff[1] + J], fz = tb.fi[tb.roff[2] + K];
     const T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
     const T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
     const T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
-    const long long fb = (long long)blockIdx.y * f.N * KB + q * W;
+    const long long fb = (long long)b * f.N * KB + q * W;
     Vec<T, W> acc;
 #pragma unroll
     for (int e = 0; e < W; ++e) acc.a[e] = 0;
@@ -250,32 +291,31 @@ __global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *
         }
       }
     }
-    stv<T, W>(rc + ((long long)blockIdx.y * c.N + n) * KB + q * W, acc);
+    stv<T, W>(rc + t, acc);
   }
 }
 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T *__restrict__ z, Dims f, Dims c,
-                                                     XferTab tb) {
+                                                     int nb, XferTab tb) {
   const T *pw = (const T *)tb.pw;
-  NODE_LOOP(f.N) {
-    const int n = (int)(g / LPN);
+  SWEEP(f.N, f.mn, nb) {
+    SWEEP_INDEX(f.N, f.mn)
     int i, j, k;
     node_ijk(n, f, i, j, k);
     const int I = tb.pl[tb.poff[0] + i], J = tb.pl[tb.poff[1] + j], K = tb.pl[tb.poff[2] + k];
     const T ax = pw[tb.poff[0] + i], ay = pw[tb.poff[1] + j], az = pw[tb.poff[2] + k];
     const T wx[2] = {ax, (T)1 - ax}, wy[2] = {ay, (T)1 - ay}, wz[2] = {az, (T)1 - az};
-    const long long cb = (long long)blockIdx.y * c.N * KB + q * W;
-    const long long t = ((long long)blockIdx.y * f.N + n) * KB + q * W;
+    const long long cb = (long long)b * c.N * KB + q * W;
     Vec<T, W> acc = ldv<T, W>(z + t);
 #pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      if (wz[b] == (T)0) continue;
+    for (int bz = 0; bz < 2; ++bz) {
+      if (wz[bz] == (T)0) continue;
 #pragma unroll
       for (int a = 0; a < 2; ++a) {
         if (wy[a] == (T)0) continue;
-        const T wyz = wy[a] * wz[b];
-        const long long row = ((long long)(K + b) * c.Ny + (J + a)) * c.Nx;
+        const T wyz = wy[a] * wz[bz];
+        const long long row = ((long long)(K + bz) * c.Ny + (J + a)) * c.Nx;
 #pragma unroll
         for (int e2 = 0; e2 < 2; ++e2) {
           if (wx[e2] == (T)0) continue;
@@ -292,22 +332,23 @@ __global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T
 
 // z_c = Ainv r_c on the coarsest level (dense, row-major Ainv[nc][nc]).
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, int nc, const T *__restrict__ rc,
-                                                      T *__restrict__ zc) {
-  NODE_LOOP(nc) {
-    const int n = (int)(g / LPN);
+__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, Dims c, int nb,
+                                                      const T *__restrict__ rc, T *__restrict__ zc) {
+  const int nc = (int)c.N;
+  SWEEP(c.N, c.mn, nb) {
+    SWEEP_INDEX(c.N, c.mn)
     const T *row = Ainv + (long long)n * nc;
-    const long long b = (long long)blockIdx.y * nc * KB + q * W;
+    const long long base = (long long)b * nc * KB + q * W;
     Vec<T, W> acc;
 #pragma unroll
     for (int e = 0; e < W; ++e) acc.a[e] = 0;
     for (int m = 0; m < nc; ++m) {
       const T w = row[m];
-      const Vec<T, W> v = ldv<T, W>(rc + b + (long long)m * KB);
+      const Vec<T, W> v = ldv<T, W>(rc + base + (long long)m * KB);
 #pragma unroll
       for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
     }
-    stv<T, W>(zc + b + (long long)n * KB, acc);
+    stv<T, W>(zc + t, acc);
   }
 }
 
@@ -315,29 +356,24 @@ __global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv
 // x += a p ; r -= a q ; partial |r|^2 (a per RHS).  With SMOOTH, also the first
 // Chebyshev step of the fine level on the new residual: z = d = c0 D^-1 r.
 template <typename T, int KB, bool SMOOTH>
-__global__ void __launch_bounds__(TPB) k_update_xr(long long N, T *__restrict__ x, T *__restrict__ r,
+__global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict__ x, T *__restrict__ r,
                                                    const T *__restrict__ p, const T *__restrict__ qv,
                                                    const double *__restrict__ alpha, double *__restrict__ partial,
-                                                   const T *__restrict__ invd, T *__restrict__ z, T *__restrict__ dv,
-                                                   T c0) {
-  constexpr int Wc = Map<T, KB>::W;
-  T acc[Wc] = {};
-  T a[Wc];
-  {
-    const int qq = threadIdx.x % Map<T, KB>::LPN;
-#pragma unroll
-    for (int e = 0; e < Wc; ++e) a[e] = (T)alpha[blockIdx.y * KB + qq * Wc + e];
-  }
-  NODE_LOOP(N) {
-    const long long n = g / LPN;
-    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
+                                                   const T *__restrict__ invd, T *__restrict__ z, T c0) {
+  __shared__ T red[MAXNB * KB];
+  BlockRed<T, KB> R;
+  R.init(red, nb);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     Vec<T, W> xv = ldv<T, W>(x + t), rv = ldv<T, W>(r + t);
     const Vec<T, W> pv = ldv<T, W>(p + t), qq = ldv<T, W>(qv + t);
+    R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      xv.a[e] += a[e] * pv.a[e];
-      rv.a[e] -= a[e] * qq.a[e];
-      acc[e] += rv.a[e] * rv.a[e];
+      const T a = (T)alpha[b * KB + q * W + e];
+      xv.a[e] += a * pv.a[e];
+      rv.a[e] -= a * qq.a[e];
+      R.acc[e] += rv.a[e] * rv.a[e];
     }
     stv<T, W>(x + t, xv);
     stv<T, W>(r + t, rv);
@@ -346,79 +382,67 @@ __global__ void __launch_bounds__(TPB) k_update_xr(long long N, T *__restrict__ 
 #pragma unroll
       for (int e = 0; e < W; ++e) rv.a[e] *= s;
       stv<T, W>(z + t, rv);
-      stv<T, W>(dv + t, rv);
     }
   }
-  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
+  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
 }
 
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_dot(long long N, const T *__restrict__ a, const T *__restrict__ b,
+__global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict__ a, const T *__restrict__ bb,
                                              double *__restrict__ partial) {
-  T acc[Map<T, KB>::W] = {};
-  NODE_LOOP(N) {
-    const long long n = g / LPN;
-    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
-    const Vec<T, W> av = ldv<T, W>(a + t), bv = ldv<T, W>(b + t);
+  __shared__ T red[MAXNB * KB];
+  BlockRed<T, KB> R;
+  R.init(red, nb);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
+    const Vec<T, W> av = ldv<T, W>(a + t), bv = ldv<T, W>(bb + t);
+    R.at(red, b, q);
 #pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] += av.a[e] * bv.a[e];
+    for (int e = 0; e < W; ++e) R.acc[e] += av.a[e] * bv.a[e];
   }
-  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
+  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
 }
 
 // p = z + beta p
 template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_p_update(long long N, T *__restrict__ p, const T *__restrict__ z,
+__global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, T *__restrict__ p, const T *__restrict__ z,
                                                   const double *__restrict__ beta) {
-  constexpr int Wc = Map<T, KB>::W;
-  T bt[Wc];
-  {
-    const int qq = threadIdx.x % Map<T, KB>::LPN;
-#pragma unroll
-    for (int e = 0; e < Wc; ++e) bt[e] = (T)beta[blockIdx.y * KB + qq * Wc + e];
-  }
-  NODE_LOOP(N) {
-    const long long n = g / LPN;
-    const long long t = ((long long)blockIdx.y * N + n) * KB + q * W;
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     Vec<T, W> pv = ldv<T, W>(p + t);
     const Vec<T, W> zv = ldv<T, W>(z + t);
 #pragma unroll
-    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + bt[e] * pv.a[e];
+    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + (T)beta[b * KB + q * W + e] * pv.a[e];
     stv<T, W>(p + t, pv);
   }
 }
 
 // ---------------------------------------------------------------- refinement
 template <int KB>
-__global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ coef, const double *__restrict__ b,
+__global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ coef, const double *__restrict__ bvec,
                                                      const double *__restrict__ x, double *__restrict__ r64,
-                                                     float *__restrict__ r32, Dims d, const int *__restrict__ active,
-                                                     double *__restrict__ partial) {
+                                                     float *__restrict__ r32, Dims d, int nb,
+                                                     const int *__restrict__ active, double *__restrict__ partial) {
   using T = double;
-  constexpr int Wc = Map<T, KB>::W;
-  double acc[Wc] = {};
-  bool act[Wc];
-  {
-    const int qq = threadIdx.x % Map<T, KB>::LPN;
-#pragma unroll
-    for (int e = 0; e < Wc; ++e) act[e] = active[blockIdx.y * KB + qq * Wc + e] != 0;
-  }
-  NODE_LOOP(d.N) {
-    const int n = (int)(g / LPN);
+  __shared__ T red[MAXNB * KB];
+  BlockRed<T, KB> R;
+  R.init(red, nb);
+  SWEEP(d.N, d.mn, nb) {
+    SWEEP_INDEX(d.N, d.mn)
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const long long t = ((long long)blockIdx.y * d.N + n) * KB + q * W;
     const Vec<T, W> ax = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
-    Vec<T, W> rv = ldv<T, W>(b + t);
+    Vec<T, W> rv = ldv<T, W>(bvec + t);
+    R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       rv.a[e] -= ax.a[e];
-      acc[e] += rv.a[e] * rv.a[e];
-      r32[t + e] = act[e] ? (float)rv.a[e] : 0.0f;
+      R.acc[e] += rv.a[e] * rv.a[e];
+      r32[t + e] = active[b * KB + q * W + e] ? (float)rv.a[e] : 0.0f;
     }
     stv<T, W>(r64 + t, rv);
   }
-  block_partial<KB, Map<T, KB>::W, Map<T, KB>::LPN>(acc, partial);
+  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
 }
 
 __global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total4, double *__restrict__ x64,
@@ -447,74 +471,78 @@ __global__ void k_ir_accumulate_tail(long long start, long long total, double *_
 }
 
 // ---------------------------------------------------------------- PCG scalars
-// Partials layout: [nb][gx][KB]; RHS r = b*KB + l.  One warp reduces one RHS
-// (lanes stride over the gx block partials), so the scalar kernels cost a few
-// microseconds regardless of K.  Fixed lane order keeps the sums deterministic.
-__device__ __forceinline__ double warp_sum_partial(const double *p, int gx, int KB, int r) {
+// Partials layout: [nb][gx][KB]; RHS r = b*KB + l.  One block of SCAL_T
+// threads reduces one RHS (threads stride over the gx block partials, fixed
+// order, so the sums are deterministic); thread 0 then applies the CG scalar
+// logic.  Cost: a few microseconds regardless of K and gx.
+constexpr int SCAL_T = 128;
+
+__device__ __forceinline__ double block_sum_partial(const double *p, int gx, int KB, int r) {
+  __shared__ double red[SCAL_T / 32];
   const int b = r / KB, l = r % KB;
   const double *q = p + (long long)b * gx * KB + l;
-  const int lane = threadIdx.x & 31;
   double s = 0.0;
-  for (int i = lane; i < gx; i += 32) s += q[(long long)i * KB];
+  for (int i = threadIdx.x; i < gx; i += SCAL_T) s += q[(long long)i * KB];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < SCAL_T / 32; ++w) t += red[w];
+  __syncthreads();
+  return t;  // valid in thread 0
 }
 
-#define WARP_RHS_LOOP(K) for (int r = threadIdx.x >> 5; r < (K); r += (blockDim.x >> 5))
-
-__global__ void k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
-                            const double *__restrict__ rz, const int *__restrict__ active,
-                            double *__restrict__ alpha, int *__restrict__ status) {
-  WARP_RHS_LOOP(K) {
-    const double pq = warp_sum_partial(part_pq, gx, KB, r);
-    if ((threadIdx.x & 31) == 0) {
-      double a = 0.0;
-      if (active[r]) {
-        if (!(pq > 0.0) || !isfinite(pq))
-          atomicOr(status, 4);  // breakdown / non-finite
-        else
-          a = rz[r] / pq;
-      }
-      alpha[r] = a;
+__global__ void __launch_bounds__(SCAL_T) k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
+                                                      const double *__restrict__ rz, const int *__restrict__ active,
+                                                      double *__restrict__ alpha, int *__restrict__ status,
+                                                      int *__restrict__ n_active) {
+  const int r = blockIdx.x;
+  const double pq = block_sum_partial(part_pq, gx, KB, r);
+  if (threadIdx.x == 0) {
+    if (r == 0) *n_active = 0;  // recounted by k_pcg_beta later in the iteration
+    double a = 0.0;
+    if (active[r]) {
+      if (!(pq > 0.0) || !isfinite(pq))
+        atomicOr(status, 4);  // breakdown / non-finite
+      else
+        a = rz[r] / pq;
     }
+    alpha[r] = a;
   }
 }
 
 // rz_new = r.z ; rr = |r|^2 ; active &= rr > tol2[r]*bb ; beta = rz_new/rz_old ; counts active
-__global__ void k_pcg_beta(int K, int KB, int gx, const double *__restrict__ part_rz,
-                           const double *__restrict__ part_rr, double *__restrict__ rz,
-                           double *__restrict__ rr_out, const double *__restrict__ bb, const double *__restrict__ tol2,
-                           int *__restrict__ active, double *__restrict__ beta, int *__restrict__ n_active, int first) {
-  __shared__ int cnt;
-  if (threadIdx.x == 0) cnt = 0;
-  __syncthreads();
-  WARP_RHS_LOOP(K) {
-    const double rzn = warp_sum_partial(part_rz, gx, KB, r);
-    const double rr = warp_sum_partial(part_rr, gx, KB, r);
-    if ((threadIdx.x & 31) == 0) {
-      rr_out[r] = rr;
-      int act = active[r];
-      if (act && !(rr > tol2[r] * bb[r])) act = 0;
-      if (act && !isfinite(rr)) act = 0;
-      double bt = 0.0;
-      if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
-      if (act) rz[r] = rzn;
-      beta[r] = first ? 0.0 : bt;
-      active[r] = act;
-      if (act) atomicAdd(&cnt, 1);
-    }
+// (n_active must be zero on entry).
+__global__ void __launch_bounds__(SCAL_T) k_pcg_beta(int K, int KB, int gx, const double *__restrict__ part_rz,
+                                                     const double *__restrict__ part_rr, double *__restrict__ rz,
+                                                     double *__restrict__ rr_out, const double *__restrict__ bb,
+                                                     const double *__restrict__ tol2, int *__restrict__ active,
+                                                     double *__restrict__ beta, int *__restrict__ n_active,
+                                                     int first) {
+  const int r = blockIdx.x;
+  const double rzn = block_sum_partial(part_rz, gx, KB, r);
+  const double rr = block_sum_partial(part_rr, gx, KB, r);
+  if (threadIdx.x == 0) {
+    rr_out[r] = rr;
+    int act = active[r];
+    if (act && !(rr > tol2[r] * bb[r])) act = 0;
+    if (act && !isfinite(rr)) act = 0;
+    double bt = 0.0;
+    if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
+    if (act) rz[r] = rzn;
+    beta[r] = first ? 0.0 : bt;
+    active[r] = act;
+    if (act) atomicAdd(n_active, 1);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) *n_active = cnt;
 }
 
 // per-RHS sums of partials into out (used for |b|^2 and the outer residual norms)
-__global__ void k_sum_partials(int K, int KB, int gx, const double *__restrict__ part, double *__restrict__ out) {
-  WARP_RHS_LOOP(K) {
-    const double v = warp_sum_partial(part, gx, KB, r);
-    if ((threadIdx.x & 31) == 0) out[r] = v;
-  }
+__global__ void __launch_bounds__(SCAL_T) k_sum_partials(int K, int KB, int gx, const double *__restrict__ part,
+                                                         double *__restrict__ out) {
+  const double v = block_sum_partial(part, gx, KB, blockIdx.x);
+  if (threadIdx.x == 0) out[blockIdx.x] = v;
 }
 
 // Outer (refinement) convergence: active = rr > rtol2*bb ; counts ; max relative residual.
@@ -781,6 +809,51 @@ __global__ void k_chol_inverse(const double *__restrict__ L, int n, double *__re
   }
 }
 
+// ---------------------------------------------------------------- Neumann pinning
+__global__ void k_dense_pin0(double *__restrict__ A, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    A[i] = (i == 0) ? 1.0 : 0.0;             // row 0
+    if (i) A[(long long)i * n] = 0.0;        // column 0
+  }
+}
+
+// sums[r] = sum_n b[r*N + n] (column-major input), one block per column, fixed order.
+__global__ void k_colsum(const double *__restrict__ b, long long N, double *__restrict__ sums) {
+  __shared__ double red[TPB / 32];
+  const double *c = b + (long long)blockIdx.x * N;
+  double acc = 0.0;
+  for (long long n = threadIdx.x; n < N; n += TPB) acc += c[n];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int w = 0; w < TPB / 32; ++w) sacc += red[w];
+    sums[blockIdx.x] = sacc;
+  }
+}
+
+// Row 0 of every packed RHS r: b_0 - sum(b) (= -sum of the other rows).
+__global__ void k_neumann_row0(const double *__restrict__ b, long long N, int K, int KB, double *__restrict__ B,
+                               const double *__restrict__ sums) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < K; r += gridDim.x * blockDim.x)
+    B[(long long)(r / KB) * N * KB + (r % KB)] = b[(long long)r * N] - sums[r];
+}
+
+// x[:, r] += b[0, r] - x[0, r]  (column-major), one block per column.
+__global__ void k_neumann_shift(const double *__restrict__ b, long long N, double *__restrict__ x) {
+  __shared__ double delta;
+  double *c = x + (long long)blockIdx.x * N;
+  if (threadIdx.x == 0) delta = b[(long long)blockIdx.x * N] - c[0];
+  __syncthreads();
+  for (long long n = threadIdx.x; n < N; n += TPB) c[n] += delta;
+}
+
+__global__ void k_convert_d2f(const double *__restrict__ a, long long n, float *__restrict__ o) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    o[i] = (float)a[i];
+}
+
 // ---------------------------------------------------------------- layout conversion
 template <typename T>
 __global__ void k_pack(const double *__restrict__ src, long long N, int K, int KB, T *__restrict__ dst,
@@ -805,11 +878,9 @@ __global__ void k_unpack(const T *__restrict__ src, long long N, int K, int KB, 
   }
 }
 
-inline int grid_nodes(long long nodes, int LPN, int nb, int n_sm) {
-  const long long npb = TPB / LPN;
-  long long g = (nodes + npb - 1) / npb;
-  long long cap = (long long)n_sm * 8 / (nb > 0 ? nb : 1);
-  if (cap < 1) cap = 1;
+inline int grid_nodes(long long nodes, int LPN, int nb, int n_sm, int per_sm = 8) {
+  long long g = (nodes * (nb > 0 ? nb : 1) * LPN + TPB - 1) / TPB;
+  const long long cap = (long long)n_sm * per_sm;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;
@@ -823,18 +894,44 @@ inline int grid_flat(long long total, int n_sm) {
   return (int)g;
 }
 
+inline Dims flat_dims(long long N) {
+  Dims d{};
+  d.Nx = 1;
+  d.Ny = 1;
+  d.Nz = (int)N;
+  d.N = N;
+  d.mn = div_magic((unsigned)N);
+  return d;
+}
+
+// Resident blocks per SM of a kernel (cached).  Grids are capped at what the
+// GPU holds at once: a grid-stride sweep whose blocks do not all fit would be
+// run as two sweeps, and the second re-reads from DRAM what the first one had
+// in L2 (the stencil's neighbour planes).
+int resident_blocks(const void *func) {
+  static std::mutex mu;
+  static std::unordered_map<const void *, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(func);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, func, TPB, 0) != cudaSuccess || n < 1) n = 1;
+  cache[func] = n;
+  return n;
+}
+
 }  // namespace
 
 int g_n_sm = 152;
-long long &launch_counter() {
-  static long long c = 0;
+std::atomic<long long> &launch_counter() {
+  static std::atomic<long long> c{0};
   return c;
 }
 void set_sm_count(int n) { g_n_sm = n > 0 ? n : 152; }
 
-int node_grid(long long nodes, int KB, int nb) {
+int node_grid(long long nodes, int KB, int nb, int per_sm) {
   const int W = KB >= 4 ? 4 : KB;
-  return grid_nodes(nodes, KB / W, nb, g_n_sm);
+  return grid_nodes(nodes, KB / W, nb, g_n_sm, per_sm);
 }
 
 // ------------------------------------------------------------------ launchers
@@ -848,35 +945,61 @@ static const T *invd_ptr(const Level &L) {
                                                                     : (const void *)L.d_invd32);
 }
 
-#define GRID(NODES) dim3(grid_nodes((NODES), Map<T, KB>::LPN, nb, g_n_sm), nb)
+#define GRID_K(NODES, KERNEL) \
+  count_launch(dim3(grid_nodes((NODES), Map<T, KB>::LPN, nb, g_n_sm, resident_blocks((const void *)(KERNEL)))))
 
 template <typename T, int KB>
 void Ops<T, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
   if (partial)
-    k_apply<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, partial);
+    k_apply<T, KB, true><<<count_launch(dim3(gx)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nb, partial);
   else
-    k_apply<T, KB, false><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nullptr);
+    k_apply<T, KB, false><<<GRID_K(L.dims.N, (k_apply<T, KB, false>)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nb, nullptr);
+}
+
+template <typename T, int KB>
+int Ops<T, KB>::red_blocks_per_sm() {
+  int m = resident_blocks((const void *)k_apply<T, KB, true>);
+  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 0>));
+  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 1>));
+  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 2>));
+  m = std::min(m, resident_blocks((const void *)k_update_xr<T, KB, true>));
+  m = std::min(m, resident_blocks((const void *)k_update_xr<T, KB, false>));
+  m = std::min(m, resident_blocks((const void *)k_dot<T, KB>));
+  if (std::is_same<T, double>::value) m = std::min(m, resident_blocks((const void *)k_ir_residual<KB>));
+  return m;
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s) {
-  k_residual<T, KB><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), r, z, res, L.dims);
+  k_residual<T, KB><<<GRID_K(L.dims.N, (k_residual<T, KB>)), TPB, 0, s>>>(coef_ptr<T>(L), r, z, res, L.dims, nb);
 }
 
 template <typename T, int KB>
-void Ops<T, KB>::cheb_first(const Level &L, const T *r, T *z, T *d, int nb, double c0, cudaStream_t s) {
-  k_cheb_first<T, KB><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(invd_ptr<T>(L), r, z, d, L.dims, (T)c0);
+void Ops<T, KB>::cheb_first(const Level &L, const T *r, T *z, int nb, double c0, cudaStream_t s) {
+  k_cheb_first<T, KB><<<GRID_K(L.dims.N, (k_cheb_first<T, KB>)), TPB, 0, s>>>(invd_ptr<T>(L), r, z, L.dims, nb, (T)c0);
 }
 
 template <typename T, int KB>
-void Ops<T, KB>::cheb_step(const Level &L, const T *r, const T *zin, T *zout, T *d, int nb, double c1, double c2,
+template <bool DOT, int PREV>
+void Ops<T, KB>::cheb_launch(const Level &L, const T *r, const T *zin, T *zout, int nb, double c1, double c2,
+                             double *partial, int gx, cudaStream_t s) {
+  const dim3 g = DOT ? count_launch(dim3(gx)) : GRID_K(L.dims.N, (k_cheb_step<T, KB, DOT, PREV>));
+  k_cheb_step<T, KB, DOT, PREV><<<g, TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, L.dims, nb, (T)c1,
+                                                  (T)c2, partial);
+}
+
+template <typename T, int KB>
+void Ops<T, KB>::cheb_step(const Level &L, const T *r, const T *zin, T *zout, int prev, int nb, double c1, double c2,
                            double *partial, int gx, cudaStream_t s) {
-  if (partial)
-    k_cheb_step<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, d, L.dims,
-                                                          (T)c1, (T)c2, partial);
-  else
-    k_cheb_step<T, KB, false><<<count_launch(GRID(L.dims.N)), TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, d,
-                                                             L.dims, (T)c1, (T)c2, nullptr);
+  if (partial) {
+    if (prev == 1) cheb_launch<true, 1>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
+    else if (prev == 2) cheb_launch<true, 2>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
+    else cheb_launch<true, 0>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
+  } else {
+    if (prev == 1) cheb_launch<false, 1>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
+    else if (prev == 2) cheb_launch<false, 2>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
+    else cheb_launch<false, 0>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
+  }
 }
 
 template <typename T>
@@ -897,38 +1020,39 @@ static XferTab make_tab(const Level &f) {
 
 template <typename T, int KB>
 void Ops<T, KB>::restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s) {
-  k_restrict<T, KB><<<count_launch(GRID(c.dims.N)), TPB, 0, s>>>(res, rc, f.dims, c.dims, make_tab<T>(f));
+  k_restrict<T, KB><<<GRID_K(c.dims.N, (k_restrict<T, KB>)), TPB, 0, s>>>(res, rc, f.dims, c.dims, nb, make_tab<T>(f));
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s) {
-  k_prolong_add<T, KB><<<count_launch(GRID(f.dims.N)), TPB, 0, s>>>(zc, z, f.dims, c.dims, make_tab<T>(f));
+  k_prolong_add<T, KB><<<GRID_K(f.dims.N, (k_prolong_add<T, KB>)), TPB, 0, s>>>(zc, z, f.dims, c.dims, nb, make_tab<T>(f));
 }
 
 template <typename T, int KB>
-void Ops<T, KB>::coarse_solve(const T *Ainv, int nc, const T *rc, T *zc, int nb, cudaStream_t s) {
-  k_coarse_solve<T, KB><<<count_launch(GRID(nc)), TPB, 0, s>>>(Ainv, nc, rc, zc);
+void Ops<T, KB>::coarse_solve(const T *Ainv, const Level &c, const T *rc, T *zc, int nb, cudaStream_t s) {
+  k_coarse_solve<T, KB><<<GRID_K(c.dims.N, (k_coarse_solve<T, KB>)), TPB, 0, s>>>(Ainv, c.dims, nb, rc, zc);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                           double *partial, int gx, const Level *smooth, double c0, T *z, T *d, cudaStream_t s) {
+                           double *partial, int gx, const Level *smooth, double c0, T *z, cudaStream_t s) {
+  const Dims dd = flat_dims(N);
   if (smooth)
-    k_update_xr<T, KB, true><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, x, r, p, q, alpha, partial, invd_ptr<T>(*smooth), z, d,
-                                                         (T)c0);
+    k_update_xr<T, KB, true><<<count_launch(dim3(gx)), TPB, 0, s>>>(dd, nb, x, r, p, q, alpha, partial,
+                                                                     invd_ptr<T>(*smooth), z, (T)c0);
   else
-    k_update_xr<T, KB, false><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, x, r, p, q, alpha, partial, nullptr, nullptr, nullptr,
-                                                          (T)0);
+    k_update_xr<T, KB, false><<<count_launch(dim3(gx)), TPB, 0, s>>>(dd, nb, x, r, p, q, alpha, partial, nullptr,
+                                                                      nullptr, (T)0);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s) {
-  k_dot<T, KB><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(N, a, b, partial);
+  k_dot<T, KB><<<count_launch(dim3(gx)), TPB, 0, s>>>(flat_dims(N), nb, a, b, partial);
 }
 
 template <typename T, int KB>
 void Ops<T, KB>::p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s) {
-  k_p_update<T, KB><<<count_launch(GRID(N)), TPB, 0, s>>>(N, p, z, beta);
+  k_p_update<T, KB><<<GRID_K(N, (k_p_update<T, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z, beta);
 }
 
 template <typename T, int KB>
@@ -939,7 +1063,7 @@ void Ops<T, KB>::copy(long long N, int nb, T *dst, const T *src, cudaStream_t s)
 template <int KB>
 void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
                  const int *active, double *partial, int gx, cudaStream_t s) {
-  k_ir_residual<KB><<<count_launch(dim3(gx, nb)), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, active, partial);
+  k_ir_residual<KB><<<count_launch(dim3(gx)), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, nb, active, partial);
 }
 
 template <int KB>
@@ -955,18 +1079,19 @@ void fill_int(int *a, int n, int v, cudaStream_t s) {
 }
 
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
-               int *status, cudaStream_t s) {
-  k_pcg_alpha<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status);
+               int *status, int *n_active, cudaStream_t s) {
+  k_pcg_alpha<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status, n_active);
 }
 
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
               const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
               cudaStream_t s) {
-  k_pcg_beta<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta, n_active, first);
+  k_pcg_beta<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta,
+                                                      n_active, first);
 }
 
 void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s) {
-  k_sum_partials<<<count_launch(1), 1024, 0, s>>>(K, KB, gx, part, out);
+  k_sum_partials<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part, out);
 }
 
 void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
@@ -1002,6 +1127,23 @@ void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, 
                             cudaStream_t s) {
   k_cholesky<<<count_launch(1), 1024, 0, s>>>(dense, n, flag);
   k_chol_inverse<<<count_launch((n * 32 + 255) / 256), 256, 0, s>>>(dense, n, work, Ainv64, Ainv32);
+}
+
+void dense_pin0(double *A, int n, cudaStream_t s) {
+  k_dense_pin0<<<count_launch(dim3((n + TPB - 1) / TPB)), TPB, 0, s>>>(A, n);
+}
+
+void neumann_rhs(const double *b, long long N, int K, int KB, double *B, double *sums, cudaStream_t s) {
+  k_colsum<<<count_launch(dim3(K)), TPB, 0, s>>>(b, N, sums);
+  k_neumann_row0<<<count_launch(dim3((K + TPB - 1) / TPB)), TPB, 0, s>>>(b, N, K, KB, B, sums);
+}
+
+void neumann_shift(const double *b, long long N, int K, double *x, cudaStream_t s) {
+  k_neumann_shift<<<count_launch(dim3(K)), TPB, 0, s>>>(b, N, x);
+}
+
+void convert_d2f(const double *a, long long n, float *o, cudaStream_t s) {
+  k_convert_d2f<<<count_launch(dim3(grid_flat(n, g_n_sm))), TPB, 0, s>>>(a, n, o);
 }
 
 template <typename T>

@@ -158,6 +158,18 @@ class DCEngine:
         check(lib().dc_stencil_timing(self._h, 1 if enable else 0, C.byref(ms), C.byref(n), C.byref(b)))
         return (ms.value, n.value, b.value) if not enable else None
 
+    def reserve(self, k, mode="mixed"):
+        """Allocate the solve workspace for k right-hand sides now (bounded, reused by later solves)."""
+        need = self.workspace_bytes(k, mode)
+        cur = self._ws.get((mode,))
+        if cur is None or cur.numel() < need:
+            self._ws[(mode,)] = torch.empty(need, dtype=torch.uint8, device="cuda")
+        return need
+
+    @staticmethod
+    def make_stream():
+        return torch.cuda.Stream()
+
     def release_workspace(self):
         self._ws.clear()
 

@@ -66,9 +66,6 @@ class Simulation3DNodal:
             raise ValueError("Dirichlet conditions are not supported in the Nodal formulation")
         if bc_type not in ("Robin", "Neumann"):
             raise ValueError(f"bc_type must be Neumann, Robin or Mixed, not {bc_type!r}")
-        if bc_type == "Neumann":
-            raise NotImplementedError(
-                "Neumann (row-0 pinned, non-symmetric) A is not supported by the GPU PCG path; use Robin")
         self.bc_type = bc_type
         self.surface_faces = surface_faces
         if precision not in ("mixed", "fp64"):
@@ -88,7 +85,9 @@ class Simulation3DNodal:
         if self._miniaturize:
             self._dipoles, self._invs, self._mini_survey = mini_pole_pole(self.survey)
         eo = dict(engine_opts or {})
-        bface = robin_face_weights(mesh, surface_faces)
+        # Neumann: no Robin term; the engine reproduces the reference's row-0
+        # pinned solve (simulation.py:535-540) on the symmetric operator.
+        bface = robin_face_weights(mesh, surface_faces) if bc_type == "Robin" else None
         self.engine = DCEngine(mesh.h, bface, **eo)
         self.nN = self.engine.nN
         self.nC = self.engine.nC
@@ -357,11 +356,119 @@ class Simulation3DNodal:
         return J
 
     def getJtJdiag(self, m, W=None, f=None):
+        """diag(J^T W^T W J) (``simulation.py:137-154``), exact and without forming J.
+
+        Uses electrode reciprocity: one pole solve per unique electrode of the
+        survey, then the ``dc_jtj_diag`` kernel evaluates every datum's cell
+        sensitivities from the pole solutions of its (up to) four electrodes and
+        accumulates ``W_d^2 J_dc^2``.  Falls back to the batched full-J path for
+        multipole sources, non-diagonal model maps or more unique electrodes
+        than the kernel's shared-memory tile holds.
+        """
         if self._gtgdiag is None:
-            J = self.getJ(m, f=f)
-            w = np.ones(J.shape[0]) if W is None else np.asarray(W.diagonal()) ** 2
-            self._gtgdiag = (w[:, None] * J * J).sum(axis=0)
+            self.model = m
+            w = None if W is None else np.asarray(W.diagonal(), dtype=np.float64)
+            out = self._jtj_diag_reciprocity(w)
+            if out is None:
+                J = self.getJ(m, f=f)
+                w2 = np.ones(J.shape[0]) if w is None else w ** 2
+                out = (w2[:, None] * J * J).sum(axis=0)
+            self._gtgdiag = out
         return self._gtgdiag
+
+    def _electrode_tables(self):
+        """Unique electrodes and, per datum, its source/receiver electrodes and weights."""
+        locs, rows = [], []
+        for src in self.survey.source_list:
+            L = np.atleast_2d(src.location)
+            if L.shape[0] > 2:
+                return None
+            cur = np.asarray(src.electrode_currents() if hasattr(src, "electrode_currents") else src.current,
+                             dtype=np.float64)
+            if cur.size == 1 and L.shape[0] > 1:
+                cur = np.full(L.shape[0], cur[0])
+            for rx in src.receiver_list:
+                fac = np.ones(rx.nD)
+                if rx.data_type == "apparent_resistivity":
+                    fac = 1.0 / np.asarray(rx.geometric_factor[src], dtype=np.float64)
+                if isinstance(rx.locations, (list, tuple)):
+                    Ms, Ns = np.atleast_2d(rx.locations[0]), np.atleast_2d(rx.locations[1])
+                else:
+                    Ms, Ns = np.atleast_2d(rx.locations), None
+                for d in range(rx.nD):
+                    rows.append((L, cur, Ms[d], None if Ns is None else Ns[d], fac[d]))
+        if not rows:
+            return None
+        for L, cur, M, N, _ in rows:
+            locs.extend(list(L))
+            locs.append(M)
+            if N is not None:
+                locs.append(N)
+        allp = np.asarray(locs, dtype=np.float64)
+        uniq, inv = np.unique(allp, axis=0, return_inverse=True)
+        inv = np.asarray(inv).ravel()
+        nD = len(rows)
+        sa = np.full(nD, -1, np.int32)
+        sb = np.full(nD, -1, np.int32)
+        rm = np.full(nD, -1, np.int32)
+        rn = np.full(nD, -1, np.int32)
+        ia = np.zeros(nD)
+        ib = np.zeros(nD)
+        wm = np.zeros(nD)
+        wn = np.zeros(nD)
+        pos = 0
+        for d, (L, cur, M, N, fac) in enumerate(rows):
+            sa[d] = inv[pos]
+            ia[d] = cur[0]
+            pos += 1
+            if L.shape[0] == 2:
+                sb[d] = inv[pos]
+                ib[d] = cur[1]
+                pos += 1
+            rm[d] = inv[pos]
+            wm[d] = fac
+            pos += 1
+            if N is not None:
+                rn[d] = inv[pos]
+                wn[d] = -fac
+                pos += 1
+        return uniq, dict(sa=sa, sb=sb, rm=rm, rn=rn, ia=ia, ib=ib, wm=wm, wn=wn)
+
+    def _jtj_diag_reciprocity(self, w):
+        import ctypes as C
+
+        from .._lib import check, lib
+        from .electrodes import interpolation_matrix
+
+        dsig_np = self._sigma_deriv()
+        if not isinstance(dsig_np, np.ndarray):
+            return None
+        tab = self._electrode_tables()
+        if tab is None:
+            return None
+        uniq, t = tab
+        nE = uniq.shape[0]
+        if nE * 116 > 220 * 1024:
+            return None
+        self._ensure_model()
+        dev = self.device
+        P = interpolation_matrix(self.mesh, uniq).tocoo()
+        P.sum_duplicates()
+        Q = torch.zeros(nE, self.nN, dtype=torch.float64, device=dev)
+        flat = torch.from_numpy((P.row.astype(np.int64) * self.nN + P.col).astype(np.int64)).to(dev)
+        fill_sparse(flat, torch.from_numpy(P.data.astype(np.float64)).to(dev), Q.view(-1))
+        Phi = self._solve(Q)
+        nD = t["sa"].size
+        w2 = np.ones(nD) if w is None else w ** 2
+        dv = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in t.items()}
+        w2d = torch.from_numpy(np.ascontiguousarray(w2, dtype=np.float64)).to(dev)
+        dsig = torch.from_numpy(np.ascontiguousarray(dsig_np)).to(dev)
+        diag = torch.empty(self.nC, dtype=torch.float64, device=dev)
+        p = lambda x: C.c_void_p(x.data_ptr())
+        check(lib().dc_jtj_diag(self.engine._h, p(Phi), nE, nD, p(dv["sa"]), p(dv["sb"]), p(dv["ia"]), p(dv["ib"]),
+                                p(dv["rm"]), p(dv["rn"]), p(dv["wm"]), p(dv["wn"]), p(w2d), p(dsig), p(diag),
+                                C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return diag.cpu().numpy()
 
     # ------------------------------------------------------------ miniaturize
     def _mini_survey_data(self, d_mini):
