@@ -48,7 +48,7 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
     ap.add_argument("--sources", type=int, default=0, help="use only the first N sources (profiling runs)")
-    ap.add_argument("--workload", default="forward", choices=["forward", "differentiation"],
+    ap.add_argument("--workload", default="forward", choices=["forward", "differentiation", "gauss_newton"],
                     help="forward: the headline 1M-cell line; differentiation: the 96x96x48 gradient checks")
     ap.add_argument("--fd-directions", type=int, default=32)
     return ap.parse_args()
@@ -434,8 +434,63 @@ def run_differentiation(args):
     print(json.dumps(out), flush=True)
 
 
+def run_gauss_newton(args):
+    """160x160x80 cells (~2.05 M), 512 dipole sources x 48 receivers, m = ln sigma.
+
+    One inexact Gauss-Newton step at the starting model: fields, data misfit
+    gradient plus smallness + smoothness regularisation, exact getJtJdiag
+    (electrode reciprocity) for the Jacobi preconditioner, and 10 CG iterations
+    on 2 J^T W^2 J + 2 beta R, each one batched Jvec and one batched Jtvec.
+    Run in mixed precision and in plain fp64 on the same GPU; prints times and
+    the relative differences of g, diag(J^T J) and the search direction.
+    """
+    import numpy as np
+    import torch
+
+    from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.inversion import L2DataMisfit, WeightedLeastSquares, inexact_gauss_newton_direction
+    from simpeg_gb300.resistivity import Simulation3DNodal
+
+    torch.cuda.set_device(0)
+    mesh, m_true, m0, survey = workloads.gauss_newton(seed=4)
+    truth = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=1e-10)
+    rng = np.random.default_rng(9)
+    d = truth.dpred(m_true)
+    dobs = d * (1 + 0.02 * rng.standard_normal(d.size))
+    W = 1.0 / (0.02 * np.abs(dobs) + 1e-5 * np.abs(dobs).max())
+    del truth
+    torch.cuda.empty_cache()
+    beta = 10.0
+    out = {"metric": "Gauss-Newton step (getJtJdiag + gradient + 10 CG iterations): mixed vs fp64",
+           "workload": "dc3d_gauss_newton",
+           "config": {"mesh_cells": list(mesh.shape_cells), "nodes": int(mesh.n_nodes), "sources": survey.nSrc,
+                      "data": survey.nD, "beta": beta, "cg_iterations": 10, "rtol": RTOL}}
+    res = {}
+    for precision in ("mixed", "fp64"):
+        sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=precision, rtol=RTOL)
+        dmis = L2DataMisfit(sim, dobs, W=W)
+        reg = WeightedLeastSquares(mesh, sim)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p, info = inexact_gauss_newton_direction(dmis, reg, beta, m0, cg_maxiter=10)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        res[precision] = (p.cpu().numpy(), info["g"].cpu().numpy(), info["jtj_diag"].cpu().numpy())
+        out[precision] = {"seconds": dt, "cg_rel_res": info["cg_rel_res"][-1]}
+        del sim, dmis, reg, p, info
+        torch.cuda.empty_cache()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out["speedup_vs_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    out["rel_err_mixed_vs_fp64"] = {"direction": rel(res["mixed"][0], res["fp64"][0]),
+                                    "gradient": rel(res["mixed"][1], res["fp64"][1]),
+                                    "jtj_diag": rel(res["mixed"][2], res["fp64"][2])}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = _args()
+    if args.workload == "gauss_newton" and args.impl != "reference":
+        return run_gauss_newton(args)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "differentiation":

@@ -65,6 +65,11 @@ const char *dc_last_error(void);
 /* Smoother / hierarchy parameters (before dc_set_model).  Non-positive values keep defaults. */
 int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int coarse_max, int check_every);
 
+/* RHS-block width of the solver's interleaved layout: 1, 2, 4, 8, 16 or 32
+ * lanes per node (0 = automatic: the widest that pads at most 1/8 of the
+ * lanes).  Set by the autotuner. */
+int dc_set_rhs_block(dc_handle *h, int kb);
+
 /* Number of multigrid levels and nodes of level `lvl`. */
 int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3);
 
@@ -85,6 +90,31 @@ int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes);
  * ws may be NULL (the handle then allocates and caches its own). */
 int dc_solve(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, double rtol, int maxit,
              double inner_rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream);
+
+/* Fixed-iteration solve that never synchronises with the host, so that it can
+ * be recorded into a CUDA graph: exactly n_outer refinement sweeps of n_inner
+ * fp32 PCG iterations (DC_MODE_MIXED) or n_inner fp64 PCG iterations
+ * (DC_MODE_FP64).  Right-hand sides that reach rtol are frozen on the device,
+ * so extra iterations do not change them.  ws must be caller-provided (sized by
+ * dc_solve_workspace_bytes); the convergence state stays in it and
+ * dc_solve_check reads it afterwards.  Same arithmetic as dc_solve. */
+int dc_solve_fixed(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, double rtol, int n_inner,
+                   int n_outer, void *ws, size_t ws_bytes, void *stream);
+int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged);
+
+/* Independent problems (each its own handle: mesh, model, sources) solved by
+ * ONE CUDA-graph launch: every problem's fixed-iteration solve is captured on
+ * its own stream into a child graph, and the children are independent nodes
+ * of one parent graph, so their kernels run concurrently.  This is the batched
+ * form of running the reference's per-simulation `fields` over many
+ * simulations (simpeg/meta/simulation.py:194-330).  Arrays are per problem
+ * (b[i], x[i] column-major N_i x k[i]; ws[i] as for dc_solve_fixed). */
+typedef struct dc_graph dc_graph;
+int dc_batch_graph_create(int n, dc_handle *const *hs, int mode, const double *const *b, double *const *x,
+                          const int *k, double rtol, const int *n_inner, const int *n_outer, void *const *ws,
+                          const size_t *ws_bytes, dc_graph **out);
+int dc_graph_launch(dc_graph *g, void *stream);
+void dc_graph_destroy(dc_graph *g);
 
 /* out = scale * (dA/dsigma . dsig) u  for k column-major u.  Equals
  * scale * getADeriv(u, v) with dsig = sigmaDeriv @ v (simulation.py:557-571,
@@ -123,6 +153,14 @@ int dc_fill_sparse(long long nnz, const long long *idx_dev, const double *val_de
 int dc_jtj_diag(dc_handle *h, const double *phi, int nE, int nD, const int *sa, const int *sb, const double *ia,
                 const double *ib, const int *rm, const int *rn, const double *wm, const double *wn, const double *w2,
                 const double *dsig, double *diag, void *stream);
+
+/* Regulariser of the inversion step: out = scale * R v and/or diag = scale * diag(R), with
+ *   (R v)_c = alpha_s V_c v_c + sum_dir alpha_dir sum_{interior faces f} w_f (v_c - v_nbr) / dx_f^2,
+ *   w_f = (V_c + V_nbr)/2, dx_f = cell-centre distance: half the second derivative of
+ * WeightedLeastSquares' Smallness + SmoothnessFirstOrder on an all-active tensor mesh
+ * (regularization/base.py:13-466, :758-1207).  v, out, diag: device (nC). */
+int dc_reg_apply(dc_handle *h, double alpha_s, double alpha_x, double alpha_y, double alpha_z, const double *v,
+                 double *out, double *diag, double scale, void *stream);
 
 /* ---- Generic SPD sparse solver (the simpeg Solver plug-in, simpeg_gb300.solver.GPUSolver) ----
  * Replaces `solver(A)` / `Ainv * RHS` / `Ainv.clean()` of the pymatsolver

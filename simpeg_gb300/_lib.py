@@ -53,6 +53,7 @@ _SIG = {
     "dc_destroy": (None, [_VP]),
     "dc_last_error": (C.c_char_p, []),
     "dc_set_params": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
+    "dc_set_rhs_block": (C.c_int, [_VP, C.c_int]),
     "dc_level_info": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
     "dc_set_model": (C.c_int, [_VP, _DP, _VP]),
     "dc_apply": (C.c_int, [_VP, _DP, _DP, C.c_int, _VP]),
@@ -71,6 +72,15 @@ _SIG = {
     "dc_csr_destroy": (None, [_VP]),
     "dc_jtj_diag": (C.c_int, [_VP, _DP, C.c_int, C.c_int, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP,
                               _VP]),
+    "dc_reg_apply": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, _DP, _DP, _DP, C.c_double, _VP]),
+    "dc_solve_fixed": (C.c_int, [_VP, C.c_int, _DP, _DP, C.c_int, C.c_double, C.c_int, C.c_int, _DP, C.c_size_t,
+                                 _VP]),
+    "dc_solve_check": (C.c_int, [_VP, C.c_int, C.c_int, _DP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "dc_batch_graph_create": (C.c_int, [C.c_int, C.POINTER(_VP), C.c_int, C.POINTER(_VP), C.POINTER(_VP),
+                                        C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(_VP), C.POINTER(C.c_size_t), C.POINTER(_VP)]),
+    "dc_graph_launch": (C.c_int, [_VP, _VP]),
+    "dc_graph_destroy": (None, [_VP]),
     "dc_kernel_launches": (C.c_longlong, []),
     "dc_stencil_timing": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double)]),

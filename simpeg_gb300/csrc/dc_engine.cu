@@ -170,6 +170,7 @@ struct dc_handle {
   double cheb_ratio = 30.0;
   int coarse_max = 200;
   int check_every = 1;
+  int kb_force = 0;  // RHS-block width override (0: pick_kb)
   bool built = false;
   // cached internal workspace
   void *ws = nullptr;
@@ -384,6 +385,11 @@ int red_per_sm(int KB) {
 
 void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
   w.KB = pick_kb(k);
+  if (h->kb_force > 0) {
+    int kb = h->kb_force;
+    while ((k + kb - 1) / kb > kMaxRhsBlocks && kb < 32) kb *= 2;
+    w.KB = kb;
+  }
   w.nb = (k + w.KB - 1) / w.KB;
   w.Kp = w.nb * w.KB;
   const long long N = h->lv[0].dims.N;
@@ -504,7 +510,7 @@ void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int
 // init_active (nullable): RHS with init_active[r] == 0 are left untouched.
 template <typename T, int KB>
 int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Scal &sc, int nb, int gx,
-        const int *init_active, const double *tol2, int maxit, int *iters, cudaStream_t s) {
+        const int *init_active, const double *tol2, int maxit, int *iters, cudaStream_t s, bool fixed = false) {
   using O = Ops<T, KB>;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
@@ -539,6 +545,7 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
     }
     pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 0, s);
     O::p_update(N, nb, p, z, sc.beta, s);
+    if (fixed) continue;  // fixed iteration count: no host synchronisation (stream capture)
     if (++since >= h->check_every || it + 1 == maxit) {
       since = 0;
       CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -556,6 +563,7 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
     }
   }
   *iters = it;
+  if (fixed) return 0;
   CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));
   CK(cudaEventSynchronize(h->ev));
@@ -567,7 +575,8 @@ constexpr double kSafety2 = 0.09;
 
 template <int KB>
 int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
-             int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s) {
+             int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s, int fixed_outer = 0) {
+  const bool fixed = fixed_outer > 0;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
   const int nb = w.nb, Kp = w.Kp, gx = w.gx;
@@ -586,7 +595,7 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     int it = 0;
     fill_double(w.sc.tol2, Kp, rtol * rtol, s);
     status = pcg<double, KB>(h, w.X64, w.R64, w.p64, w.q64, w.z64, w.mg64, w.sc, nb, gx, nullptr, w.sc.tol2, maxit,
-                             &it, s);
+                             &it, s, fixed);
     if (status == DC_ERR_BREAKDOWN) return status;
     total_it = it;
     outer = 1;
@@ -605,20 +614,23 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
                 inner_rtol * inner_rtol, kSafety2, s);
     convert_d2f(w.B64, (long long)N * Kp, w.r32, s);
-    const int max_outer = 30;
+    const int max_outer = fixed ? fixed_outer : 30;
     for (outer = 0; outer < max_outer;) {
-      CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CK(cudaEventRecord(h->ev, s));
-      CK(cudaEventSynchronize(h->ev));
-      if (h->h_mail[0] == 0) break;
-      if (total_it >= maxit) {
-        status = DC_ERR_NOT_CONVERGED;
-        break;
+      if (!fixed) {
+        CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(h->ev, s));
+        CK(cudaEventSynchronize(h->ev));
+        if (h->h_mail[0] == 0) break;
+        if (total_it >= maxit) {
+          status = DC_ERR_NOT_CONVERGED;
+          break;
+        }
       }
       CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
       int it = 0;
       int rc = pcg<float, KB>(h, w.d32, w.r32, w.p32, w.q32, w.z32, w.mg32, w.sc, nb, gx, w.sc.active_out,
-                              w.sc.tol2, std::min(inner_maxit, maxit - total_it), &it, s);
+                              w.sc.tol2, fixed ? inner_maxit : std::min(inner_maxit, maxit - total_it), &it, s,
+                              fixed);
       total_it += it;
       if (rc == DC_ERR_BREAKDOWN) return rc;
       ir_accumulate<KB>(N, nb, w.X64, w.d32, s);
@@ -628,10 +640,20 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel,
                   w.sc.tol2, inner_rtol * inner_rtol, kSafety2, s);
     }
-    if (outer >= max_outer) status = DC_ERR_NOT_CONVERGED;
+    if (outer >= max_outer && !fixed) status = DC_ERR_NOT_CONVERGED;
   }
   unpack_colmajor<double>(w.X64, N, k, KB, x, s);
   if (!h->robin) neumann_shift(b, N, k, x, s);
+  if (fixed) {  // the convergence state stays on the device (dc_solve_check)
+    if (st) {
+      st->iterations = total_it;
+      st->outer = outer;
+      st->status = 0;
+      st->n_levels = (int)h->lv.size();
+      st->max_rel_res = -1.0;
+    }
+    return 0;
+  }
   CK(cudaMemcpyAsync(h->h_maild, w.sc.maxrel, sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));
@@ -733,6 +755,14 @@ int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int 
     h->coarse_max = coarse_max;
   }
   if (check_every > 0) h->check_every = check_every;
+  return 0;
+}
+
+int dc_set_rhs_block(dc_handle *h, int kb) {
+  if (!h) return fail(DC_ERR_ARG, "handle is NULL");
+  if (kb != 0 && kb != 1 && kb != 2 && kb != 4 && kb != 8 && kb != 16 && kb != 32)
+    return fail(DC_ERR_ARG, "RHS block width must be 0 (automatic) or a power of two <= 32");
+  h->kb_force = kb;
   return 0;
 }
 
@@ -872,6 +902,98 @@ int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double r
   return rc;
 }
 
+int dc_solve_fixed(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int n_inner, int n_outer,
+                   void *ws, size_t ws_bytes, void *stream) {
+  if (!h || !b || !x || k < 1 || !ws) return fail(DC_ERR_ARG, "bad argument (the workspace must be caller-provided)");
+  if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
+  if (!(rtol > 0.0) || n_inner < 1 || n_outer < 1) return fail(DC_ERR_ARG, "rtol, n_inner, n_outer must be positive");
+  if (k > 32 * kMaxRhsBlocks) return fail(DC_ERR_ARG, "k too large for one fixed solve");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  SolveWS w;
+  layout_ws(h, mode, k, nullptr, w);
+  if (ws_bytes < w.bytes) return fail(DC_ERR_NOMEM, "workspace too small");
+  char *base = (char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+  layout_ws(h, mode, k, base, w);
+  cudaStream_t s = (cudaStream_t)stream;
+  const double inner_rtol = 1e-4;
+  int rc;
+  switch (w.KB) {
+    case 32: rc = solve_kb<32>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+    case 16: rc = solve_kb<16>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+    case 8: rc = solve_kb<8>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+    case 4: rc = solve_kb<4>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+    case 2: rc = solve_kb<2>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+    default: rc = solve_kb<1>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
+  }
+  return rc;
+}
+
+int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged) {
+  if (!h || !ws || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  SolveWS w;
+  char *base = (char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+  layout_ws(h, mode, k, base, w);
+  double mr = 0.0;
+  int na = 0;
+  CK(cudaMemcpy(&mr, w.sc.maxrel, sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&na, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost));
+  if (max_rel_res) *max_rel_res = mr;
+  if (n_unconverged) *n_unconverged = na;
+  return 0;
+}
+
+struct dc_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaGraph_t> children;
+  std::vector<cudaStream_t> streams;
+};
+
+void dc_graph_destroy(dc_graph *g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  for (auto c : g->children) cudaGraphDestroy(c);
+  for (auto st : g->streams) cudaStreamDestroy(st);
+  delete g;
+}
+
+int dc_batch_graph_create(int n, dc_handle *const *hs, int mode, const double *const *b, double *const *x,
+                          const int *k, double rtol, const int *n_inner, const int *n_outer, void *const *ws,
+                          const size_t *ws_bytes, dc_graph **out) {
+  if (n < 1 || !hs || !b || !x || !k || !n_inner || !n_outer || !ws || !ws_bytes || !out)
+    return fail(DC_ERR_ARG, "bad argument");
+  *out = nullptr;
+  std::unique_ptr<dc_graph, void (*)(dc_graph *)> g(new (std::nothrow) dc_graph(), dc_graph_destroy);
+  if (!g) return fail(DC_ERR_NOMEM, "host allocation failed");
+  for (int i = 0; i < n; ++i) {
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    g->streams.push_back(st);
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = dc_solve_fixed(hs[i], mode, b[i], x[i], k[i], rtol, n_inner[i], n_outer[i], ws[i], ws_bytes[i], st);
+    cudaGraph_t child = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &child);
+    if (child) g->children.push_back(child);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(DC_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+  }
+  CK(cudaGraphCreate(&g->graph, 0));
+  for (auto c : g->children) {
+    cudaGraphNode_t node;
+    CK(cudaGraphAddChildGraphNode(&node, g->graph, nullptr, 0, c));
+  }
+  CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  *out = g.release();
+  return 0;
+}
+
+int dc_graph_launch(dc_graph *g, void *stream) {
+  if (!g || !g->exec) return fail(DC_ERR_ARG, "bad graph");
+  CK(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return 0;
+}
+
 static int ensure_dlev(dc_handle *h) {
   if (h->dlev.d_coef64) return 0;
   const Level &L0 = h->lv[0];
@@ -919,6 +1041,18 @@ int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const d
 }
 
 long long dc_kernel_launches(void) { return dc::launch_counter().load(); }
+
+int dc_reg_apply(dc_handle *h, double alpha_s, double alpha_x, double alpha_y, double alpha_z, const double *v,
+                 double *out, double *diag, double scale, void *stream) {
+  if (!h || (!out && !diag) || (out && !v)) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->built) {
+    int rc = build_hierarchy(h);
+    if (rc) return rc;
+  }
+  reg_apply(h->lv[0], alpha_s, alpha_x, alpha_y, alpha_z, v, out, diag, scale, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
 
 int dc_jtj_diag(dc_handle *h, const double *phi, int nE, int nD, const int *sa, const int *sb, const double *ia,
                 const double *ib, const int *rm, const int *rn, const double *wm, const double *wn, const double *w2,

@@ -162,6 +162,10 @@ int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD
                     const double *ia, const double *ib, const int *rm, const int *rn, const double *wm,
                     const double *wn, const double *w2, const double *dsig, double *diag, cudaStream_t stream);
 
+// regulariser apply (dc_sens.cu): out = scale * R v, dg = scale * diag(R) (either may be null; v null -> only dg)
+void reg_apply(const Level &L, double as, double ax, double ay, double az, const double *v, double *out, double *dg,
+               double scale, cudaStream_t s);
+
 std::string &last_error();
 
 }  // namespace dc

@@ -150,3 +150,49 @@ void cell_gradient(const Level &L, int robin, const double *P, const double *Q, 
 }
 
 }  // namespace dc
+
+// ---------------------------------------------------------------------------
+// Model regularisation of the inversion that consumes this path
+// (regularization/base.py WeightedLeastSquares: Smallness + SmoothnessFirstOrder
+// on a tensor mesh with every cell active):
+//   (R v)_c = a_s V_c v_c + sum_dir a_dir sum_{interior faces f of c} w_f (v_c - v_n) / dx_f^2
+// with w_f = (V_c + V_n) / 2 and dx_f the distance between the two cell centres
+// (zero gradient on boundary faces).  R = deriv2 / 2 of the regulariser.
+namespace dc {
+namespace {
+__global__ void k_reg_apply(const double *__restrict__ h, int nx, int ny, int nz, double as, double ax, double ay,
+                            double az, const double *__restrict__ v, double *__restrict__ out, double *__restrict__ dg,
+                            double scale) {
+  const double *hx = h, *hy = h + nx, *hz = h + nx + ny;
+  const long long nC = (long long)nx * ny * nz;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(c / ((long long)nx * ny));
+    const int r = (int)(c - (long long)k * nx * ny);
+    const int j = r / nx, i = r - j * nx;
+    const double V = hx[i] * hy[j] * hz[k];
+    const double vc = v ? v[c] : 0.0;
+    double acc = as * V * vc, d = as * V;
+    auto face = [&](long long nb, double Vn, double dx, double a) {
+      const double w = a * 0.5 * (V + Vn) / (dx * dx);
+      d += w;
+      if (v) acc += w * (vc - v[nb]);
+    };
+    if (i > 0) face(c - 1, hx[i - 1] * hy[j] * hz[k], 0.5 * (hx[i - 1] + hx[i]), ax);
+    if (i + 1 < nx) face(c + 1, hx[i + 1] * hy[j] * hz[k], 0.5 * (hx[i] + hx[i + 1]), ax);
+    if (j > 0) face(c - nx, hx[i] * hy[j - 1] * hz[k], 0.5 * (hy[j - 1] + hy[j]), ay);
+    if (j + 1 < ny) face(c + nx, hx[i] * hy[j + 1] * hz[k], 0.5 * (hy[j] + hy[j + 1]), ay);
+    if (k > 0) face(c - (long long)nx * ny, hx[i] * hy[j] * hz[k - 1], 0.5 * (hz[k - 1] + hz[k]), az);
+    if (k + 1 < nz) face(c + (long long)nx * ny, hx[i] * hy[j] * hz[k + 1], 0.5 * (hz[k] + hz[k + 1]), az);
+    if (out) out[c] = scale * acc;
+    if (dg) dg[c] = scale * d;
+  }
+}
+}  // namespace
+
+void reg_apply(const Level &L, double as, double ax, double ay, double az, const double *v, double *out, double *dg,
+               double scale, cudaStream_t s) {
+  const long long nC = (long long)L.nx * L.ny * L.nz;
+  k_reg_apply<<<count_launch(dim3(grid_flat(nC, g_n_sm))), TPB, 0, s>>>(L.d_h, L.nx, L.ny, L.nz, as, ax, ay, az, v,
+                                                                        out, dg, scale);
+}
+}  // namespace dc

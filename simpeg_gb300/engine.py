@@ -100,6 +100,11 @@ class DCEngine:
     def set_params(self, nu_pre=0, nu_post=0, cheb_ratio=0.0, coarse_max=0, check_every=0):
         check(lib().dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
 
+    def set_rhs_block(self, kb):
+        """Force the RHS-block width (1..32 lanes per node; 0 = automatic)."""
+        check(lib().dc_set_rhs_block(self._h, int(kb)))
+        self._ws.clear()
+
     def set_model(self, sigma):
         sigma = _dev64(sigma, (self.nC,), "sigma")
         check(lib().dc_set_model(self._h, _ptr(sigma), _stream()))

@@ -1,0 +1,187 @@
+"""The inversion step that consumes the DC path, on the device.
+
+Mirrors the callers of ``dpred / Jvec / Jtvec / getJtJdiag`` in simpeg's
+inversion stack:
+
+* :class:`L2DataMisfit` -- ``phi_d = ||W (d(m) - d_obs)||^2``, ``deriv = 2 J^T W^T W r``,
+  ``deriv2 v = 2 J^T W W J v`` (``simpeg/data_misfit.py:238-343``);
+* :class:`WeightedLeastSquares` -- Smallness + first-order Smoothness on an
+  all-active tensor mesh (``simpeg/regularization/base.py:13-466,758-1207,1540-``):
+  ``phi_m = alpha_s ||V^1/2 (m - m_ref)||^2 + sum_j alpha_j ||W_j G_j m||^2`` with
+  ``W_j^2`` the average volume on the interior faces, ``alpha_j = (length_scale_j *
+  base_length)^2`` (base_length: smallest cell width); applied by ``dc_reg_apply``;
+* :func:`inexact_gauss_newton_direction` -- ``p = CG(H, -g, M)`` with ``maxiter``
+  iterations (``simpeg/optimization.py:1345-1415``) and the Jacobi
+  preconditioner of the ``UpdatePreconditioner`` directive
+  ``M = diag(1 / (getJtJdiag(m, W) + beta * diag(reg.deriv2)))``
+  (``simpeg/directives/_directives.py:2180-2260``).
+
+All model-sized vectors stay on the device; every ``H v`` is one batched Jvec
+and one batched Jtvec (two multi-RHS solves over all sources).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._lib import check, lib
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+class L2DataMisfit:
+    def __init__(self, simulation, dobs, W=None):
+        self.simulation = simulation
+        dev = simulation.device
+        self.dobs = torch.as_tensor(np.asarray(dobs, dtype=np.float64), device=dev)
+        if W is None:
+            w = np.ones(self.dobs.numel())
+        elif np.ndim(W) == 1:
+            w = np.asarray(W, dtype=np.float64)
+        else:  # a (sparse) diagonal weighting matrix, as simpeg's misfit holds it
+            w = np.asarray(W.diagonal(), dtype=np.float64)
+        self.w = torch.as_tensor(w, device=dev)
+        self.W = w
+
+    def residual_dev(self, m):
+        sim = self.simulation
+        f = sim._fields_for(m, None)
+        return sim._gather(f.phi_dev) - self.dobs
+
+    def __call__(self, m):
+        r = self.w * self.residual_dev(m)
+        return float((r * r).sum().item())
+
+    def deriv_dev(self, m):
+        r = self.residual_dev(m)
+        return 2.0 * self.simulation.jtvec_dev(self.w * self.w * r)
+
+    def deriv2_dev(self, m, v_dev):
+        sim = self.simulation
+        return 2.0 * sim.jtvec_dev(self.w * self.w * sim.jvec_dev(v_dev))
+
+
+class WeightedLeastSquares:
+    def __init__(self, mesh, simulation, alpha_s=1.0, alpha_x=None, alpha_y=None, alpha_z=None,
+                 length_scale_x=None, length_scale_y=None, length_scale_z=None, reference_model=None,
+                 reference_model_in_smooth=False):
+        self.mesh = mesh
+        self.simulation = simulation
+        base = min(float(np.min(h)) for h in mesh.h)
+        self.base_length = base
+
+        def alpha(a, ls):
+            if a is not None:
+                if ls is not None:
+                    raise ValueError("Attempted to set both alpha and length_scale at the same time")
+                return float(a)
+            return float((1.0 if ls is None else ls) * base) ** 2
+
+        self.alpha_s = float(alpha_s)
+        self.alpha_x = alpha(alpha_x, length_scale_x)
+        self.alpha_y = alpha(alpha_y, length_scale_y)
+        self.alpha_z = alpha(alpha_z, length_scale_z)
+        dev = simulation.device
+        nC = simulation.nC
+        mref = np.zeros(nC) if reference_model is None else np.asarray(reference_model, dtype=np.float64)
+        self.mref = torch.as_tensor(mref, device=dev)
+        self.reference_model_in_smooth = bool(reference_model_in_smooth)
+
+    def _apply(self, v, a_s, smooth=True, scale=1.0):
+        h = self.simulation.engine._h
+        out = torch.empty_like(v)
+        ax, ay, az = (self.alpha_x, self.alpha_y, self.alpha_z) if smooth else (0.0, 0.0, 0.0)
+        check(lib().dc_reg_apply(h, a_s, ax, ay, az, _p(v.contiguous()), _p(out), C.c_void_p(0), scale, _stream()))
+        return out
+
+    def R(self, v):
+        """(deriv2 / 2) v."""
+        return self._apply(v, self.alpha_s)
+
+    def diag_deriv2(self):
+        h = self.simulation.engine._h
+        d = torch.empty(self.simulation.nC, dtype=torch.float64, device=self.mref.device)
+        check(lib().dc_reg_apply(h, self.alpha_s, self.alpha_x, self.alpha_y, self.alpha_z, C.c_void_p(0),
+                                 C.c_void_p(0), _p(d), 2.0, _stream()))
+        return d
+
+    def __call__(self, m_dev):
+        dm = m_dev - self.mref
+        ms = dm if self.reference_model_in_smooth else m_dev
+        small = self._apply(dm, self.alpha_s, smooth=False)
+        smooth = self._apply(ms, 0.0)
+        return float((dm * small).sum().item() + (ms * smooth).sum().item())
+
+    def deriv_dev(self, m_dev):
+        dm = m_dev - self.mref
+        ms = dm if self.reference_model_in_smooth else m_dev
+        return 2.0 * (self._apply(dm, self.alpha_s, smooth=False) + self._apply(ms, 0.0))
+
+    def deriv2_dev(self, v_dev):
+        return 2.0 * self.R(v_dev)
+
+
+def inexact_gauss_newton_direction(dmis, reg, beta, m, cg_maxiter=10, cg_rtol=0.0, precondition=True):
+    """One Gauss-Newton search direction at model m (host array).
+
+    Returns (p, info) with p a device tensor and info a dict of the pieces
+    (gradient, JtJ diagonal, CG residual history)."""
+    sim = dmis.simulation
+    sim.model = m
+    sim._ensure_model()
+    dev = sim.device
+    mt = torch.as_tensor(np.asarray(m, dtype=np.float64), device=dev)
+    sim.fields(m)
+    g = dmis.deriv_dev(m) + beta * reg.deriv_dev(mt)
+    info = {"g": g}
+    if precondition:
+        jtj = torch.as_tensor(sim.getJtJdiag(m, W=_Diag(dmis.W)), device=dev)
+        dA = jtj + beta * reg.diag_deriv2()
+        Minv = torch.where(dA != 0, 1.0 / dA, torch.zeros_like(dA))
+        info["jtj_diag"] = jtj
+    else:
+        Minv = torch.ones_like(g)
+
+    def H(v):
+        return dmis.deriv2_dev(m, v) + beta * reg.deriv2_dev(v)
+
+    # preconditioned CG on H p = -g from p = 0 (scipy.sparse.linalg.cg semantics)
+    b = -g
+    x = torch.zeros_like(b)
+    r = b.clone()
+    z = Minv * r
+    pvec = z.clone()
+    rz = float((r * z).sum())
+    bnorm = float(torch.linalg.vector_norm(b))
+    hist = [float(torch.linalg.vector_norm(r)) / bnorm]
+    for _ in range(cg_maxiter):
+        q = H(pvec)
+        alpha = rz / float((pvec * q).sum())
+        x = x + alpha * pvec
+        r = r - alpha * q
+        hist.append(float(torch.linalg.vector_norm(r)) / bnorm)
+        if hist[-1] <= cg_rtol:
+            break
+        z = Minv * r
+        rz_new = float((r * z).sum())
+        pvec = z + (rz_new / rz) * pvec
+        rz = rz_new
+    info["cg_rel_res"] = hist
+    return x, info
+
+
+class _Diag:
+    def __init__(self, w):
+        self._w = np.asarray(w, dtype=np.float64)
+
+    def diagonal(self):
+        return self._w

@@ -146,6 +146,7 @@ class Simulation3DNodal:
         self._clear()
 
     def _clear(self):
+        self._dsig_cache = None
         self._sigma_dev = None
         self._f_cache = None
         self._Jmatrix = None
@@ -218,8 +219,22 @@ class Simulation3DNodal:
             self.engine.set_model(self._sigma_dev)
         return self._sigma_dev
 
+    # device bytes the solver workspace may take per call; larger RHS sets are solved in chunks
+    workspace_budget = 48 << 30
+
     def _solve(self, B):
-        X, info = self.engine.solve(B, mode=self.precision, rtol=self.rtol, maxit=self.maxit)
+        k = B.shape[0]
+        per = max(1, self.engine.workspace_bytes(min(k, 1024), self.precision) // min(k, 1024))
+        chunk = int(max(32, min(k, self.workspace_budget // per)))
+        if chunk >= k:
+            X, info = self.engine.solve(B, mode=self.precision, rtol=self.rtol, maxit=self.maxit)
+            self.last_solve_info = info
+            return X
+        X = torch.empty_like(B)
+        for c0 in range(0, k, chunk):
+            c1 = min(k, c0 + chunk)
+            X[c0:c1], info = self.engine.solve(B[c0:c1].contiguous(), mode=self.precision, rtol=self.rtol,
+                                               maxit=self.maxit)
         self.last_solve_info = info
         return X
 
@@ -326,6 +341,35 @@ class Simulation3DNodal:
         Lam = self._solve(PTv)
         g = self.engine.dadm_adj(f.phi_dev, Lam, None, scale=-1.0).cpu().numpy()
         return self._map_adjoint(g)
+
+    # ------------------------------------------------------------ device-resident products
+    def jvec_dev(self, v_dev, f=None):
+        """J v with v a device tensor (nP,) at the current model; returns a device tensor (nD,).
+
+        Same operations as :meth:`Jvec` (``simulation.py:156-187``) without host round trips:
+        ``-dA/dm v`` by the stencil kernel, one multi-RHS solve, receiver gather."""
+        f = f if f is not None else self._fields_for(self._model, None)
+        d = self._sigma_deriv()
+        if not isinstance(d, np.ndarray):
+            raise NotImplementedError("device products need a map with a diagonal derivative")
+        dsig = self._dsig_diag_dev() * v_dev
+        R = self.engine.dadm_fwd(f.phi_dev, dsig.contiguous(), scale=-1.0)
+        return self._gather(self._solve(R))
+
+    def jtvec_dev(self, w_dev, f=None):
+        """J^T w with w a device tensor (nD,) at the current model; returns a device tensor (nP,)."""
+        f = f if f is not None else self._fields_for(self._model, None)
+        t, tq = self._get_tables()
+        PTv = torch.zeros(t.nSrc, self.nN, dtype=torch.float64, device=self.device)
+        csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], w_dev.contiguous(), PTv.view(-1), out_idx=tq["PT_out"])
+        Lam = self._solve(PTv)
+        return self.engine.dadm_adj(f.phi_dev, Lam, self._dsig_diag_dev(), scale=-1.0)
+
+    def _dsig_diag_dev(self):
+        if getattr(self, "_dsig_cache", None) is None or self._dsig_cache[0] is not self._model:
+            d = self._sigma_deriv()
+            self._dsig_cache = (self._model, torch.from_numpy(np.ascontiguousarray(d)).to(self.device))
+        return self._dsig_cache[1]
 
     def getJ(self, m, f=None):
         """Full sensitivity (nD, nP): one adjoint solve per datum, batched."""

@@ -125,3 +125,61 @@ def differentiation(seed=2, n_src=128, n_rx=30, ncore_xy=80, ncore_z=40, core_h=
             N = np.c_[xs[js + 1], np.full(n_rx, yv), np.zeros(n_rx)]
             src_list.append(sources.Dipole([receivers.Dipole(M, N)], np.r_[a, yv, 0.0], np.r_[b, yv, 0.0]))
     return mesh, m, Survey(src_list)
+
+
+# ---------------------------------------------------------------- Gauss-Newton step
+def gauss_newton(seed=4, n_lines=16, src_per_line=32, n_rx=48, ncore_xy=144, ncore_z=72, core_h=5.0):
+    """160x160x80 cells (~2.05 M), m = ln sigma, 512 dipole sources x 48 dipole receivers.
+
+    16 survey lines along x, stations every 5 m; source i of a line is the dipole
+    (station i, i+1) and its receivers are the dipoles (i+1+n, i+2+n), n = 1..48.
+    Returns mesh, true model, starting model (the true field's mean) and survey.
+    """
+    rng = np.random.default_rng(seed)
+    mesh = padded_mesh(ncore_xy, ncore_z, core_h)
+    m_true = np.log(10.0) * log10_sigma_field(mesh, rng)
+    m0 = np.full(mesh.n_cells, m_true.mean())
+    half = core_h * ncore_xy / 2.0
+    ys = np.round(np.linspace(-0.75 * half, 0.75 * half, n_lines) / core_h) * core_h
+    nst = src_per_line + n_rx + 2
+    x0 = -np.round((nst * core_h) / 2.0 / core_h) * core_h
+    xs = x0 + core_h * np.arange(nst)
+    src_list = []
+    for yv in ys:
+        for i in range(src_per_line):
+            js = i + 1 + np.arange(1, n_rx + 1)
+            M = np.c_[xs[js], np.full(n_rx, yv), np.zeros(n_rx)]
+            N = np.c_[xs[js + 1], np.full(n_rx, yv), np.zeros(n_rx)]
+            src_list.append(sources.Dipole([receivers.Dipole(M, N)], np.r_[xs[i], yv, 0.0],
+                                           np.r_[xs[i + 1], yv, 0.0]))
+    return mesh, m_true, m0, Survey(src_list)
+
+
+# ---------------------------------------------------------------- batched uneven problems
+def batched_problems(seed=5, n=64, lo=(32, 32, 16), hi=(96, 96, 64), h=10.0, src_range=(16, 128), n_rx=20):
+    """n independent problems: cell counts log-uniform per axis between lo and hi (even),
+    sources uniform in src_range (pole sources on a surface line), n_rx dipoles each,
+    conductivity = random field (log10 mean -2, std 0.5, correlation 6 cells) + one 0.1 S/m block."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        dims = [int(2 * round(np.exp(rng.uniform(np.log(a), np.log(b))) / 2)) for a, b in zip(lo, hi)]
+        mesh = TensorMesh([[(h, d)] for d in dims], origin="CCN")
+        log10s = log10_sigma_field(mesh, rng, corr_cells=6.0).reshape(dims, order="F")
+        bx, by, bz = [max(2, d // 5) for d in dims]
+        i0, j0, k0 = [int(rng.integers(1, d - b - 1)) for d, b in zip(dims, (bx, by, bz))]
+        log10s[i0:i0 + bx, j0:j0 + by, k0:k0 + bz] = -1.0
+        sigma = 10.0 ** log10s.ravel(order="F")
+        ns = int(rng.integers(src_range[0], src_range[1] + 1))
+        half_x = h * dims[0] / 2.0
+        half_y = h * dims[1] / 2.0
+        xs = np.round(np.linspace(-0.8 * half_x, 0.8 * half_x, n_rx + 1) / h) * h
+        src_list = []
+        for s in range(ns):
+            yv = np.round(rng.uniform(-0.7 * half_y, 0.7 * half_y) / h) * h
+            xv = np.round(rng.uniform(-0.8 * half_x, 0.8 * half_x) / h) * h
+            M = np.c_[xs[:-1], np.full(n_rx, yv), np.zeros(n_rx)]
+            N = np.c_[xs[1:], np.full(n_rx, yv), np.zeros(n_rx)]
+            src_list.append(sources.Pole([receivers.Dipole(M, N)], np.r_[xv, yv, 0.0]))
+        out.append((mesh, sigma, Survey(src_list)))
+    return out
