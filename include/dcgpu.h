@@ -100,19 +100,31 @@ int dc_solve(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, 
  * dc_solve_check reads it afterwards.  Same arithmetic as dc_solve. */
 int dc_solve_fixed(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, double rtol, int n_inner,
                    int n_outer, void *ws, size_t ws_bytes, void *stream);
-int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged);
+/* Convergence state left in ws by the last dc_solve_fixed or graph-recorded
+ * solve on it: max relative residual, RHS still above rtol, inner iterations
+ * summed over sweeps and refinement sweeps (the last two are counted by the
+ * graph-recorded solves only; 0 after dc_solve_fixed).  Outputs may be NULL. */
+int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged,
+                   int *iterations, int *sweeps);
 
 /* Independent problems (each its own handle: mesh, model, sources) solved by
- * ONE CUDA-graph launch: every problem's fixed-iteration solve is captured on
- * its own stream into a child graph, and the children are independent nodes
- * of one parent graph, so their kernels run concurrently.  This is the batched
- * form of running the reference's per-simulation `fields` over many
- * simulations (simpeg/meta/simulation.py:194-330).  Arrays are per problem
- * (b[i], x[i] column-major N_i x k[i]; ws[i] as for dc_solve_fixed). */
+ * ONE CUDA-graph launch.  Every problem's adaptive solve is recorded on its own
+ * stream (forked from and joined to one capture), and its iteration loops
+ * become conditional WHILE nodes whose conditions are set on the device from
+ * the per-RHS convergence counters: a launch runs each problem exactly as far
+ * as dc_solve would with its default inner settings (same arithmetic, same
+ * stopping rule; at most maxit inner iterations in total, 200 per sweep, and
+ * 30 refinement sweeps), the problems' kernels run
+ * concurrently, and the host is not involved until the launch ends.  This is
+ * the batched form of running the reference's per-simulation `fields` over
+ * many simulations (simpeg/meta/simulation.py:194-330).  Arrays are per
+ * problem (b[i], x[i] column-major N_i x k[i], k[i] <= 1024; ws[i] sized by
+ * dc_solve_workspace_bytes); a handle may appear once per batch; read the
+ * result's convergence with dc_solve_check. */
 typedef struct dc_graph dc_graph;
 int dc_batch_graph_create(int n, dc_handle *const *hs, int mode, const double *const *b, double *const *x,
-                          const int *k, double rtol, const int *n_inner, const int *n_outer, void *const *ws,
-                          const size_t *ws_bytes, dc_graph **out);
+                          const int *k, double rtol, int maxit, void *const *ws, const size_t *ws_bytes,
+                          dc_graph **out);
 int dc_graph_launch(dc_graph *g, void *stream);
 void dc_graph_destroy(dc_graph *g);
 

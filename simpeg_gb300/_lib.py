@@ -75,9 +75,10 @@ _SIG = {
     "dc_reg_apply": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, _DP, _DP, _DP, C.c_double, _VP]),
     "dc_solve_fixed": (C.c_int, [_VP, C.c_int, _DP, _DP, C.c_int, C.c_double, C.c_int, C.c_int, _DP, C.c_size_t,
                                  _VP]),
-    "dc_solve_check": (C.c_int, [_VP, C.c_int, C.c_int, _DP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "dc_solve_check": (C.c_int, [_VP, C.c_int, C.c_int, _DP, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "dc_batch_graph_create": (C.c_int, [C.c_int, C.POINTER(_VP), C.c_int, C.POINTER(_VP), C.POINTER(_VP),
-                                        C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.c_double, C.c_int,
                                         C.POINTER(_VP), C.POINTER(C.c_size_t), C.POINTER(_VP)]),
     "dc_graph_launch": (C.c_int, [_VP, _VP]),
     "dc_graph_destroy": (None, [_VP]),

@@ -4,29 +4,25 @@ Each problem is ``(mesh, sigma, survey)`` -- its own mesh size, conductivity
 and sources, as the simulations of simpeg's meta-simulation fan-out
 (``simpeg/meta/simulation.py:194-330``) or of an inversion over many sites.
 :class:`BatchedForward` gives every problem its own engine handle (hierarchy,
-coefficients, workspace), calibrates each solve once with the adaptive solver
-to learn its refinement sweeps and inner iterations, and then records every
-problem's *fixed-iteration* solve on its own stream into one CUDA graph whose
-child graphs are independent: a single ``cudaGraphLaunch`` runs all problems,
-their kernels overlapping on the GPU.  Right-hand sides that converge early
-are frozen on the device, so the safety margin on the iteration counts costs
-time but never changes results; after each launch the device-side
-convergence state is checked and any problem that missed the tolerance is
-re-solved with the adaptive solver (and reported).
+coefficients, workspace) and records every problem's adaptive solve on its own
+stream into ONE CUDA graph.  The solver's loops (PCG iterations, refinement
+sweeps) are conditional WHILE nodes whose conditions are set on the device
+from the per-RHS convergence counters, so a single ``cudaGraphLaunch`` runs
+every problem exactly as far as the stand-alone solver would, their kernels
+overlapping on the GPU, with no host round trip until the launch ends.  After
+a launch the device-side convergence state is read back; a problem that hit
+the iteration cap is re-solved with the host-driven solver (and reported).
 
-Smoother degree and Chebyshev interval per problem come from
+RHS-block width, smoother degree and Chebyshev interval per problem come from
 :mod:`simpeg_gb300.autotune` when ``tune=True``.
 """
 
 from __future__ import annotations
 
 import ctypes as C
-import math
-
 import numpy as np
 import torch
 
-from . import _lib
 from ._lib import check, lib
 from .engine import DCEngine, MODES, csr_spmv, fill_sparse
 from .resistivity.boundary import robin_face_weights
@@ -40,10 +36,10 @@ class _Problem:
 
 
 class BatchedForward:
-    def __init__(self, problems, precision="mixed", rtol=1e-9, margin=1.3, tune=False, device=None):
+    def __init__(self, problems, precision="mixed", rtol=1e-9, maxit=2000, tune=False, device=None):
         self.precision = precision
         self.rtol = float(rtol)
-        self.margin = float(margin)
+        self.maxit = int(maxit)
         self.device = torch.device(device if device is not None else "cuda")
         self.problems = []
         for mesh, sigma, survey in problems:
@@ -73,22 +69,16 @@ class BatchedForward:
             p.X = torch.empty_like(p.Q)
             p.ws = torch.empty(p.engine.workspace_bytes(p.k, self.precision), dtype=torch.uint8, device=dev)
             p.P = [torch.from_numpy(a).to(dev) for a in (t.P_ptr, t.P_idx, t.P_w)]
-            # calibration: the adaptive solver tells how many sweeps / iterations this problem needs
-            _, info = p.engine.solve(p.Q, mode=self.precision, rtol=self.rtol, ws=p.ws)
-            p.n_outer = max(1, info.outer)
-            p.n_inner = max(2, int(math.ceil(info.iterations / p.n_outer * self.margin)) + 1)
         torch.cuda.synchronize()
         n = len(self.problems)
         hs = (C.c_void_p * n)(*[p.engine._h for p in self.problems])
         bs = (C.c_void_p * n)(*[p.Q.data_ptr() for p in self.problems])
         xs = (C.c_void_p * n)(*[p.X.data_ptr() for p in self.problems])
         ks = (C.c_int * n)(*[p.k for p in self.problems])
-        ni = (C.c_int * n)(*[p.n_inner for p in self.problems])
-        no = (C.c_int * n)(*[p.n_outer for p in self.problems])
         ws = (C.c_void_p * n)(*[p.ws.data_ptr() for p in self.problems])
         wb = (C.c_size_t * n)(*[p.ws.numel() for p in self.problems])
         g = C.c_void_p()
-        check(lib().dc_batch_graph_create(n, hs, MODES[self.precision], bs, xs, ks, self.rtol, ni, no, ws, wb,
+        check(lib().dc_batch_graph_create(n, hs, MODES[self.precision], bs, xs, ks, self.rtol, self.maxit, ws, wb,
                                           C.byref(g)))
         self._graph = g
 
@@ -97,13 +87,13 @@ class BatchedForward:
         check(lib().dc_graph_launch(self._graph, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
 
     def convergence(self):
-        """Per problem: (max relative residual, number of RHS above rtol) read from the device."""
+        """Per problem: (max relative residual, RHS above rtol, inner iterations, sweeps) read from the device."""
         out = []
         for p in self.problems:
-            mr, na = C.c_double(), C.c_int()
+            mr, na, it, sw = C.c_double(), C.c_int(), C.c_int(), C.c_int()
             check(lib().dc_solve_check(p.engine._h, MODES[self.precision], p.k, C.c_void_p(p.ws.data_ptr()),
-                                       C.byref(mr), C.byref(na)))
-            out.append((mr.value, na.value))
+                                       C.byref(mr), C.byref(na), C.byref(it), C.byref(sw)))
+            out.append((mr.value, na.value, it.value, sw.value))
         return out
 
     def run(self):
@@ -111,7 +101,7 @@ class BatchedForward:
         self.launch()
         torch.cuda.synchronize()
         self.resolved = []
-        for i, (p, (mr, na)) in enumerate(zip(self.problems, self.convergence())):
+        for i, (p, (mr, na, _, _)) in enumerate(zip(self.problems, self.convergence())):
             if na != 0:
                 X, _ = p.engine.solve(p.Q, mode=self.precision, rtol=self.rtol, ws=p.ws)
                 p.X.copy_(X)  # the graph keeps writing into p.X: refresh it in place

@@ -182,6 +182,8 @@ struct dc_handle {
   int *h_mail = nullptr;
   double *h_maild = nullptr;
   cudaEvent_t ev = nullptr;
+  // streams that record the bodies of device-side solve loops (graph capture)
+  cudaStream_t body_s[2] = {nullptr, nullptr};
   // optional timing of the fine-level fp32 Chebyshev stencil launches
   bool prof = false;
   std::vector<cudaEvent_t> prof_ev;  // start/stop pairs
@@ -318,6 +320,7 @@ struct Scal {
   double *part_a, *part_b, *part_c;  // partials (gx * Kp each)
   double *rz, *rr, *bb, *alpha, *beta, *rr64, *bb64, *maxrel, *tol2;
   int *active, *active_out, *n_active, *n_active_out, *status;
+  int *loop;  // device-loop counters: {iterations this sweep, iterations in total, sweeps, unused}
 };
 
 template <typename T>
@@ -358,6 +361,7 @@ void carve_scal(Carve &c, int Kp, int gx, Scal &s) {
   s.n_active = c.take<int>(1);
   s.n_active_out = c.take<int>(1);
   s.status = c.take<int>(1);
+  s.loop = c.take<int>(4);
 }
 
 // Lays out (or, with base == nullptr, sizes) the whole solve workspace.
@@ -505,12 +509,70 @@ void vcycle(const dc_handle *h, int l, const T *r, T *z, const MGWork<T> &w, int
   if (cur != z) cudaMemcpyAsync(z, cur, sizeof(T) * F.dims.N * KB * nb, cudaMemcpyDeviceToDevice, s);
 }
 
+// ------------------------------------------------------------------ loops
+// How the iteration loops of a solve are driven:
+//  LOOP_HOST   -- the host polls the device's convergence counter (one pinned
+//                 read per check_every iterations) and stops issuing work;
+//  LOOP_FIXED  -- a fixed iteration count, no host synchronisation;
+//  LOOP_DEVICE -- the stream is being captured into a CUDA graph and every
+//                 loop becomes a conditional WHILE node whose condition a
+//                 one-thread kernel sets from the device-side counters, so a
+//                 graph launch runs the adaptive solve with no host involvement.
+enum { LOOP_HOST = 0, LOOP_FIXED = 1, LOOP_DEVICE = 2 };
+
+// Creates the condition handle of a WHILE node in the graph being captured on s.
+int while_handle(cudaStream_t s, cudaGraphConditionalHandle *hc) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive || !g) return fail(DC_ERR_STATE, "device-side loop outside stream capture");
+  CK(cudaGraphConditionalHandleCreate(hc, g, 0, 0));
+  return 0;
+}
+
+// Appends the WHILE node after the work captured so far on s and starts
+// recording its body on `body`.
+int open_while(cudaStream_t s, cudaGraphConditionalHandle hc, cudaStream_t body) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, &edges, &nd));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = hc;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
+  CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CK(cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  return 0;
+}
+
+int close_while(cudaStream_t body) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamEndCapture(body, &g));
+  return 0;
+}
+
+int body_stream(dc_handle *h, int depth, cudaStream_t *out) {
+  if (!h->body_s[depth]) CK(cudaStreamCreateWithFlags(&h->body_s[depth], cudaStreamNonBlocking));
+  *out = h->body_s[depth];
+  return 0;
+}
+
 // ------------------------------------------------------------------ PCG
 // Solves A x = r0 (x = 0 on entry, r holds r0 and is overwritten by the residual).
 // init_active (nullable): RHS with init_active[r] == 0 are left untouched.
+// `depth` selects the body stream of a LOOP_DEVICE loop (0 unless nested in a
+// refinement loop); total_max caps the iterations summed over sweeps.
 template <typename T, int KB>
 int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Scal &sc, int nb, int gx,
-        const int *init_active, const double *tol2, int maxit, int *iters, cudaStream_t s, bool fixed = false) {
+        const int *init_active, const double *tol2, int maxit, int total_max, int *iters, cudaStream_t s,
+        int loop = LOOP_HOST, int depth = 0) {
   using O = Ops<T, KB>;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
@@ -530,22 +592,39 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
   O::copy(N, nb, p, z, s);
   const Cheb cp0 = cheb_params(F.lmax, h->cheb_ratio);
   T *z1 = fused ? first_buffer(h, 0, z, w) : nullptr;
+  // one PCG iteration on stream st
+  auto iteration = [&](cudaStream_t st) {
+    O::apply(F, p, q, nb, sc.part_a, gx, st);
+    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, sc.n_active, st);
+    if (fused) {
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, 1.0 / cp0.theta, z1, st);
+      vcycle<T, KB>(h, 0, r, z, w, nb, st, true, sc.part_c, gx);
+    } else {
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, st);
+      vcycle<T, KB>(h, 0, r, z, w, nb, st);
+      O::dot(N, nb, r, z, sc.part_c, gx, st);
+    }
+    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 0, st);
+    O::p_update(N, nb, p, z, sc.beta, st);
+  };
+  if (loop == LOOP_DEVICE) {
+    int rc;
+    cudaGraphConditionalHandle hc;
+    cudaStream_t sb;
+    if ((rc = body_stream(h, depth, &sb))) return rc;
+    if ((rc = while_handle(s, &hc))) return rc;
+    inner_loop_cond(hc, 1, sc.n_active, sc.status, sc.loop, maxit, total_max, s);
+    if ((rc = open_while(s, hc, sb))) return rc;
+    iteration(sb);
+    inner_loop_cond(hc, 0, sc.n_active, sc.status, sc.loop, maxit, total_max, sb);
+    *iters = 0;
+    return close_while(sb);
+  }
   int it = 0;
   int since = 0;
   for (it = 0; it < maxit; ++it) {
-    O::apply(F, p, q, nb, sc.part_a, gx, s);
-    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, sc.n_active, s);
-    if (fused) {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, 1.0 / cp0.theta, z1, s);
-      vcycle<T, KB>(h, 0, r, z, w, nb, s, true, sc.part_c, gx);
-    } else {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, s);
-      vcycle<T, KB>(h, 0, r, z, w, nb, s);
-      O::dot(N, nb, r, z, sc.part_c, gx, s);
-    }
-    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 0, s);
-    O::p_update(N, nb, p, z, sc.beta, s);
-    if (fixed) continue;  // fixed iteration count: no host synchronisation (stream capture)
+    iteration(s);
+    if (loop == LOOP_FIXED) continue;  // fixed iteration count: no host synchronisation
     if (++since >= h->check_every || it + 1 == maxit) {
       since = 0;
       CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -563,7 +642,7 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, T *z, const MGWork<T> &w, const Sc
     }
   }
   *iters = it;
-  if (fixed) return 0;
+  if (loop == LOOP_FIXED) return 0;
   CK(cudaMemcpyAsync(h->h_mail, sc.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));
   CK(cudaEventSynchronize(h->ev));
@@ -575,8 +654,9 @@ constexpr double kSafety2 = 0.09;
 
 template <int KB>
 int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
-             int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s, int fixed_outer = 0) {
-  const bool fixed = fixed_outer > 0;
+             int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s, int loop = LOOP_HOST, int max_outer = 30) {
+  const bool fixed = loop == LOOP_FIXED;
+  const bool device = loop == LOOP_DEVICE;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
   const int nb = w.nb, Kp = w.Kp, gx = w.gx;
@@ -589,14 +669,16 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     neumann_rhs(b, N, k, KB, w.B64, w.sc.rr64, s);
   }
   CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));
+  CK(cudaMemsetAsync(w.sc.loop, 0, 4 * sizeof(int), s));
+  CK(cudaMemsetAsync(w.sc.status, 0, sizeof(int), s));  // read by the device-loop conditions before the first PCG
   int total_it = 0, outer = 0, status = 0;
   if (mode == DC_MODE_FP64) {
     CK(cudaMemcpyAsync(w.R64, w.B64, sizeof(double) * N * Kp, cudaMemcpyDeviceToDevice, s));
     int it = 0;
     fill_double(w.sc.tol2, Kp, rtol * rtol, s);
     status = pcg<double, KB>(h, w.X64, w.R64, w.p64, w.q64, w.z64, w.mg64, w.sc, nb, gx, nullptr, w.sc.tol2, maxit,
-                             &it, s, fixed);
-    if (status == DC_ERR_BREAKDOWN) return status;
+                             maxit, &it, s, loop, 0);
+    if (status == DC_ERR_BREAKDOWN || (device && status)) return status;
     total_it = it;
     outer = 1;
     // true residual
@@ -614,37 +696,54 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
                 inner_rtol * inner_rtol, kSafety2, s);
     convert_d2f(w.B64, (long long)N * Kp, w.r32, s);
-    const int max_outer = fixed ? fixed_outer : 30;
-    for (outer = 0; outer < max_outer;) {
-      if (!fixed) {
-        CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
-        CK(cudaEventRecord(h->ev, s));
-        CK(cudaEventSynchronize(h->ev));
-        if (h->h_mail[0] == 0) break;
-        if (total_it >= maxit) {
-          status = DC_ERR_NOT_CONVERGED;
-          break;
-        }
-      }
-      CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
-      int it = 0;
+    // one refinement sweep on stream so: inner fp32 PCG, accumulate, fp64 residual, new flags
+    auto sweep = [&](cudaStream_t so, int inner_cap, int *it) -> int {
+      CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
       int rc = pcg<float, KB>(h, w.d32, w.r32, w.p32, w.q32, w.z32, w.mg32, w.sc, nb, gx, w.sc.active_out,
-                              w.sc.tol2, fixed ? inner_maxit : std::min(inner_maxit, maxit - total_it), &it, s,
-                              fixed);
-      total_it += it;
-      if (rc == DC_ERR_BREAKDOWN) return rc;
-      ir_accumulate<KB>(N, nb, w.X64, w.d32, s);
-      ++outer;
-      ir_residual<KB>(F, w.B64, w.X64, w.R64, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, s);
-      sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
+                              w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
+      if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
+      ir_accumulate<KB>(N, nb, w.X64, w.d32, so);
+      ir_residual<KB>(F, w.B64, w.X64, w.R64, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, so);
+      sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, so);
       outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel,
-                  w.sc.tol2, inner_rtol * inner_rtol, kSafety2, s);
+                  w.sc.tol2, inner_rtol * inner_rtol, kSafety2, so);
+      return 0;
+    };
+    if (device) {
+      int rc, it = 0;
+      cudaGraphConditionalHandle ho;
+      cudaStream_t so;
+      if ((rc = body_stream(h, 0, &so))) return rc;
+      if ((rc = while_handle(s, &ho))) return rc;
+      outer_loop_cond(ho, 1, w.sc.n_active_out, w.sc.status, w.sc.loop, max_outer, maxit, s);
+      if ((rc = open_while(s, ho, so))) return rc;
+      if ((rc = sweep(so, inner_maxit, &it))) return rc;
+      outer_loop_cond(ho, 0, w.sc.n_active_out, w.sc.status, w.sc.loop, max_outer, maxit, so);
+      if ((rc = close_while(so))) return rc;
+    } else {
+      for (outer = 0; outer < max_outer;) {
+        if (!fixed) {
+          CK(cudaMemcpyAsync(h->h_mail, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+          CK(cudaEventRecord(h->ev, s));
+          CK(cudaEventSynchronize(h->ev));
+          if (h->h_mail[0] == 0) break;
+          if (total_it >= maxit) {
+            status = DC_ERR_NOT_CONVERGED;
+            break;
+          }
+        }
+        int it = 0;
+        int rc = sweep(s, fixed ? inner_maxit : std::min(inner_maxit, maxit - total_it), &it);
+        total_it += it;
+        if (rc == DC_ERR_BREAKDOWN) return rc;
+        ++outer;
+      }
+      if (outer >= max_outer && !fixed) status = DC_ERR_NOT_CONVERGED;
     }
-    if (outer >= max_outer && !fixed) status = DC_ERR_NOT_CONVERGED;
   }
   unpack_colmajor<double>(w.X64, N, k, KB, x, s);
   if (!h->robin) neumann_shift(b, N, k, x, s);
-  if (fixed) {  // the convergence state stays on the device (dc_solve_check)
+  if (fixed || device) {  // the convergence state stays on the device (dc_solve_check)
     if (st) {
       st->iterations = total_it;
       st->outer = outer;
@@ -668,6 +767,19 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
   }
   if (status) return fail(status, "solver did not reach the requested tolerance");
   return 0;
+}
+
+int solve_dispatch(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit,
+                   double inner_rtol, int inner_maxit, SolveWS &w, dc_stats *st, cudaStream_t s, int loop,
+                   int max_outer) {
+  switch (w.KB) {
+    case 32: return solve_kb<32>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+    case 16: return solve_kb<16>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+    case 8: return solve_kb<8>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+    case 4: return solve_kb<4>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+    case 2: return solve_kb<2>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+    default: return solve_kb<1>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, st, s, loop, max_outer);
+  }
 }
 
 }  // namespace
@@ -739,6 +851,8 @@ void dc_destroy(dc_handle *h) {
   if (h->h_mail) cudaFreeHost(h->h_mail);
   if (h->h_maild) cudaFreeHost(h->h_maild);
   if (h->ev) cudaEventDestroy(h->ev);
+  for (auto st : h->body_s)
+    if (st) cudaStreamDestroy(st);
   for (auto &e : h->prof_ev) cudaEventDestroy(e);
   delete h;
 }
@@ -888,15 +1002,7 @@ int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double r
   }
   base = (char *)(((uintptr_t)base + 255) & ~(uintptr_t)255);
   layout_ws(h, mode, k, base, w);
-  int rc;
-  switch (w.KB) {
-    case 32: rc = solve_kb<32>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-    case 16: rc = solve_kb<16>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-    case 8: rc = solve_kb<8>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-    case 4: rc = solve_kb<4>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-    case 2: rc = solve_kb<2>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-    default: rc = solve_kb<1>(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s); break;
-  }
+  int rc = solve_dispatch(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, w, stats, s, LOOP_HOST, 30);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(DC_ERR_CUDA, std::string("dc_solve: ") + cudaGetErrorString(e));
   return rc;
@@ -916,72 +1022,120 @@ int dc_solve_fixed(dc_handle *h, int mode, const double *b, double *x, int k, do
   layout_ws(h, mode, k, base, w);
   cudaStream_t s = (cudaStream_t)stream;
   const double inner_rtol = 1e-4;
-  int rc;
-  switch (w.KB) {
-    case 32: rc = solve_kb<32>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-    case 16: rc = solve_kb<16>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-    case 8: rc = solve_kb<8>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-    case 4: rc = solve_kb<4>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-    case 2: rc = solve_kb<2>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-    default: rc = solve_kb<1>(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, n_outer); break;
-  }
-  return rc;
+  return solve_dispatch(h, mode, b, x, k, rtol, n_inner, inner_rtol, n_inner, w, nullptr, s, LOOP_FIXED, n_outer);
 }
 
-int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged) {
+int dc_solve_check(dc_handle *h, int mode, int k, const void *ws, double *max_rel_res, int *n_unconverged,
+                   int *iterations, int *sweeps) {
   if (!h || !ws || k < 1) return fail(DC_ERR_ARG, "bad argument");
   SolveWS w;
   char *base = (char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
   layout_ws(h, mode, k, base, w);
   double mr = 0.0;
-  int na = 0;
+  int na = 0, ctr[4] = {0, 0, 0, 0};
   CK(cudaMemcpy(&mr, w.sc.maxrel, sizeof(double), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(&na, w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ctr, w.sc.loop, sizeof(ctr), cudaMemcpyDeviceToHost));
   if (max_rel_res) *max_rel_res = mr;
   if (n_unconverged) *n_unconverged = na;
+  if (iterations) *iterations = ctr[1];
+  if (sweeps) *sweeps = mode == DC_MODE_FP64 ? 1 : ctr[2];
   return 0;
 }
 
 struct dc_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  std::vector<cudaGraph_t> children;
   std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;
 };
 
 void dc_graph_destroy(dc_graph *g) {
   if (!g) return;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
-  for (auto c : g->children) cudaGraphDestroy(c);
+  for (auto e : g->events) cudaEventDestroy(e);
   for (auto st : g->streams) cudaStreamDestroy(st);
   delete g;
 }
 
+// Ends every capture still open on the given streams (error path).
+static void abort_captures(const std::vector<cudaStream_t> &streams) {
+  for (auto st : streams) {
+    if (!st) continue;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t tmp = nullptr;
+      cudaStreamEndCapture(st, &tmp);
+      if (tmp) cudaGraphDestroy(tmp);
+    }
+  }
+  cudaGetLastError();
+}
+
 int dc_batch_graph_create(int n, dc_handle *const *hs, int mode, const double *const *b, double *const *x,
-                          const int *k, double rtol, const int *n_inner, const int *n_outer, void *const *ws,
-                          const size_t *ws_bytes, dc_graph **out) {
-  if (n < 1 || !hs || !b || !x || !k || !n_inner || !n_outer || !ws || !ws_bytes || !out)
-    return fail(DC_ERR_ARG, "bad argument");
+                          const int *k, double rtol, int maxit, void *const *ws, const size_t *ws_bytes,
+                          dc_graph **out) {
+  if (n < 1 || !hs || !b || !x || !k || !ws || !ws_bytes || !out) return fail(DC_ERR_ARG, "bad argument");
+  if (mode != DC_MODE_FP64 && mode != DC_MODE_MIXED) return fail(DC_ERR_ARG, "bad mode");
+  if (!(rtol > 0.0) || maxit < 1) return fail(DC_ERR_ARG, "rtol and maxit must be positive");
   *out = nullptr;
+  std::vector<SolveWS> wsl(n);
+  for (int i = 0; i < n; ++i) {
+    dc_handle *h = hs[i];
+    if (!h || !b[i] || !x[i] || k[i] < 1 || !ws[i]) return fail(DC_ERR_ARG, "bad problem entry");
+    if (k[i] > 32 * kMaxRhsBlocks) return fail(DC_ERR_ARG, "k too large for one graph-recorded solve");
+    if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+    for (int j = 0; j < i; ++j)
+      if (hs[j] == h) return fail(DC_ERR_ARG, "a handle appears twice in one batch");
+    layout_ws(h, mode, k[i], nullptr, wsl[i]);
+    if (ws_bytes[i] < wsl[i].bytes) return fail(DC_ERR_NOMEM, "workspace too small");
+    layout_ws(h, mode, k[i], (char *)(((uintptr_t)ws[i] + 255) & ~(uintptr_t)255), wsl[i]);
+  }
   std::unique_ptr<dc_graph, void (*)(dc_graph *)> g(new (std::nothrow) dc_graph(), dc_graph_destroy);
   if (!g) return fail(DC_ERR_NOMEM, "host allocation failed");
-  for (int i = 0; i < n; ++i) {
+  for (int i = 0; i <= n; ++i) {
     cudaStream_t st;
+    cudaEvent_t ev;
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     g->streams.push_back(st);
-    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = dc_solve_fixed(hs[i], mode, b[i], x[i], k[i], rtol, n_inner[i], n_outer[i], ws[i], ws_bytes[i], st);
-    cudaGraph_t child = nullptr;
-    cudaError_t e = cudaStreamEndCapture(st, &child);
-    if (child) g->children.push_back(child);
-    if (rc) return rc;
-    if (e != cudaSuccess) return fail(DC_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    g->events.push_back(ev);
   }
-  CK(cudaGraphCreate(&g->graph, 0));
-  for (auto c : g->children) {
-    cudaGraphNode_t node;
-    CK(cudaGraphAddChildGraphNode(&node, g->graph, nullptr, 0, c));
+  // One capture: stream 0 forks every problem onto its own stream and joins them.
+  std::vector<cudaStream_t> all(g->streams);
+  for (int i = 0; i < n; ++i)
+    for (auto bs : hs[i]->body_s) all.push_back(bs);
+  cudaStream_t s0 = g->streams[0];
+  CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  if (cudaEventRecord(g->events[0], s0) != cudaSuccess) rc = fail(DC_ERR_CUDA, "event record in capture");
+  const double inner_rtol = 1e-4;
+  for (int i = 0; i < n && !rc; ++i) {
+    dc_handle *h = hs[i];
+    cudaStream_t st = g->streams[i + 1];
+    if (cudaStreamWaitEvent(st, g->events[0], 0) != cudaSuccess) {
+      rc = fail(DC_ERR_CUDA, "stream wait in capture");
+      break;
+    }
+    const bool prof = h->prof;
+    h->prof = false;  // no event records inside conditional bodies
+    rc = solve_dispatch(h, mode, b[i], x[i], k[i], rtol, maxit, inner_rtol, std::min(maxit, 200), wsl[i], nullptr,
+                        st, LOOP_DEVICE, 30);
+    h->prof = prof;
+    for (auto bs : h->body_s) all.push_back(bs);
+    if (rc) break;
+    if (cudaEventRecord(g->events[i + 1], st) != cudaSuccess || cudaStreamWaitEvent(s0, g->events[i + 1], 0) != cudaSuccess)
+      rc = fail(DC_ERR_CUDA, "join in capture");
+  }
+  if (rc) {
+    abort_captures(all);
+    return rc;
+  }
+  cudaError_t e = cudaStreamEndCapture(s0, &g->graph);
+  if (e != cudaSuccess) {
+    abort_captures(all);
+    return fail(DC_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
   }
   CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
   *out = g.release();

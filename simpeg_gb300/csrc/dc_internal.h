@@ -130,6 +130,13 @@ void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaSt
 void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
                  double *maxrel, double *inner_tol2, double inner_floor2, double safety2, cudaStream_t s);
 void fill_double(double *a, int n, double v, cudaStream_t s);
+// Condition kernels of the device-side (CUDA-graph WHILE node) solve loops;
+// ctr = {inner iterations of this sweep, inner iterations in total, sweeps}.
+void inner_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_active, const int *status, int *ctr,
+                     int maxit, int total_max, cudaStream_t s);
+void outer_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_active_out, const int *status, int *ctr,
+                     int max_outer, int total_max, cudaStream_t s);
+
 
 void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s);
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s);

@@ -69,8 +69,6 @@ template <typename T, int KB> struct Map {
   static constexpr int LPN = KB / W;  // threads per node
 };
 
-// Largest number of RHS blocks a reduction kernel accepts (K <= 32 * KB).
-constexpr int MAXNB = kMaxRhsBlocks;
 
 template <typename T, int KB>
 __device__ __forceinline__ const typename CoefT<T>::type *coef_of(const void *c) {
@@ -118,65 +116,91 @@ __device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *
   (void)b;                                            \
   (void)n;
 
-// Per-(RHS block, lane) partial sums: threads add their running sums into
-// shared memory when they move to the next RHS block, then the block writes
-// partial[(b * gridDim.x + blockIdx.x) * KB + lane].
+// Reductions (per-RHS dot products) are bitwise reproducible: every thread
+// sums its own elements in sweep order, threads of one lane group are
+// combined by warp shuffles, and the warps' sums in warp order -- no
+// floating-point atomics, so a solve repeated on the same data (or recorded in
+// a CUDA graph) takes the same iterations and returns the same bits.
+// Block partials land in partial[(b * gridDim.x + blockIdx.x) * KB + lane].
 template <typename T, int KB>
-struct BlockRed {
-  static constexpr int W = Map<T, KB>::W;
+__device__ __forceinline__ void block_reduce(T (&acc)[Map<T, KB>::W], T *red, int b, double *partial) {
+  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
+#pragma unroll
+  for (int o = 16; o >= LPN; o >>= 1)
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < LPN)
+#pragma unroll
+    for (int e = 0; e < W; ++e) red[warp * KB + lane * W + e] = acc[e];
+  __syncthreads();
+  if (threadIdx.x < KB) {
+    T v = (T)0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; ++w) v += red[w * KB + threadIdx.x];
+    partial[((long long)b * gridDim.x + blockIdx.x) * KB + threadIdx.x] = (double)v;
+  }
+  __syncthreads();
+}
+
+// Sweep of a reducing kernel: the RHS blocks one after the other (the whole
+// grid on one RHS block at a time, as in the flat sweep), each closed by the
+// block reduction of that RHS block's per-thread sums.
+// body(b, n, q, t, acc): RHS block, node, lane group, element offset, sums.
+template <typename T, int KB, typename Body>
+__device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, Body body) {
+  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
+  __shared__ T red[(TPB / 32) * KB];
+  const int q = threadIdx.x % LPN;
+  const long long per = (long long)N * LPN;
+  for (int b = 0; b < nb; ++b) {
+    T acc[W];
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] = (T)0;
+    const long long base = (long long)b * N;
+    for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < per; g += (long long)gridDim.x * TPB) {
+      const int n = (int)(g / LPN);
+      body(b, n, q, (base + n) * KB + q * W, acc);
+    }
+    block_reduce<T, KB>(acc, red, b, partial);
+  }
+}
+
+// The same body over the flat (RHS block, node, lane group) sweep, no reduction.
+template <typename T, int KB, typename Body>
+__device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body) {
+  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
+  const int q = threadIdx.x % LPN;
+  const long long total = (long long)N * nb * LPN;
   T acc[W];
-  int cur;
-  __device__ __forceinline__ void init(T *red, int nb) {
-    for (int i = threadIdx.x; i < nb * KB; i += TPB) red[i] = (T)0;
-    cur = -1;
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] = (T)0;
-    __syncthreads();
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total; g += (long long)gridDim.x * TPB) {
+    const int ng = (int)(g / LPN);
+    const int b = fast_div(ng, N, mn);
+    body(b, ng - b * N, q, (long long)ng * KB + q * W, acc);
   }
-  __device__ __forceinline__ void flush(T *red, int q) {
-    if (cur >= 0) {
-#pragma unroll
-      for (int e = 0; e < W; ++e) atomicAdd(&red[cur * KB + q * W + e], acc[e]);
-    }
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] = (T)0;
-  }
-  __device__ __forceinline__ void at(T *red, int b, int q) {
-    if (b != cur) {
-      flush(red, q);
-      cur = b;
-    }
-  }
-  __device__ __forceinline__ void finish(T *red, int q, int nb, double *partial) {
-    flush(red, q);
-    __syncthreads();
-    for (int i = threadIdx.x; i < nb * KB; i += TPB)
-      partial[((long long)(i / KB) * gridDim.x + blockIdx.x) * KB + (i % KB)] = (double)red[i];
-  }
-};
+}
 
 // ---------------------------------------------------------------- stencil ops
 template <typename T, int KB, bool DOT>
 __global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
                                                T *__restrict__ y, Dims d, int nb, double *__restrict__ partial) {
+  constexpr int W = Map<T, KB>::W;
   const auto *coef = coef_of<T, KB>(cf);
-  __shared__ T red[DOT ? MAXNB * KB : 1];
-  BlockRed<T, KB> R;
-  if (DOT) R.init(red, nb);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
+  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
     const Vec<T, W> v = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
     stv<T, W>(y + t, v);
     if (DOT) {
-      R.at(red, b, q);
       const Vec<T, W> xv = ldv<T, W>(x + t);
 #pragma unroll
-      for (int e = 0; e < W; ++e) R.acc[e] += v.a[e] * xv.a[e];
+      for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
     }
-  }
-  if (DOT) R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
+  };
+  if (DOT)
+    sweep_reduce<T, KB>(d.N, nb, partial, body);
+  else
+    sweep_flat<T, KB>(d.N, d.mn, nb, body);
 }
 
 template <typename T, int KB>
@@ -220,12 +244,9 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
                                                    const T *__restrict__ r, const T *__restrict__ zin,
                                                    T *zout, Dims d, int nb, T c1, T c2,
                                                    double *__restrict__ partial) {
+  constexpr int W = Map<T, KB>::W;
   const auto *coef = coef_of<T, KB>(cf);
-  __shared__ T red[DOT ? MAXNB * KB : 1];
-  BlockRed<T, KB> R;
-  if (DOT) R.init(red, nb);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
+  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
     const Vec<T, W> az = stencil_vec<T, KB, W>(coef, zin, t, n, i, j, k, d);
@@ -234,18 +255,20 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
     Vec<T, W> zo;
     if (PREV == 1) zo = ldv<T, W>(zout + t);
     const T s = c2 * invd[n];
-    if (DOT) R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       T mom = (T)0;
       if (PREV == 1) mom = c1 * (zc.a[e] - zo.a[e]);
       if (PREV == 2) mom = c1 * zc.a[e];
       zo.a[e] = zc.a[e] + mom + s * (rv.a[e] - az.a[e]);
-      if (DOT) R.acc[e] += rv.a[e] * zo.a[e];
+      if (DOT) acc[e] += rv.a[e] * zo.a[e];
     }
     stv<T, W>(zout + t, zo);
-  }
-  if (DOT) R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
+  };
+  if (DOT)
+    sweep_reduce<T, KB>(d.N, nb, partial, body);
+  else
+    sweep_flat<T, KB>(d.N, d.mn, nb, body);
 }
 
 // ---------------------------------------------------------------- transfers
@@ -360,20 +383,16 @@ __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict
                                                    const T *__restrict__ p, const T *__restrict__ qv,
                                                    const double *__restrict__ alpha, double *__restrict__ partial,
                                                    const T *__restrict__ invd, T *__restrict__ z, T c0) {
-  __shared__ T red[MAXNB * KB];
-  BlockRed<T, KB> R;
-  R.init(red, nb);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
+  constexpr int W = Map<T, KB>::W;
+  sweep_reduce<T, KB>(d.N, nb, partial, [&](int b, int n, int q, long long t, T(&acc)[W]) {
     Vec<T, W> xv = ldv<T, W>(x + t), rv = ldv<T, W>(r + t);
     const Vec<T, W> pv = ldv<T, W>(p + t), qq = ldv<T, W>(qv + t);
-    R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       const T a = (T)alpha[b * KB + q * W + e];
       xv.a[e] += a * pv.a[e];
       rv.a[e] -= a * qq.a[e];
-      R.acc[e] += rv.a[e] * rv.a[e];
+      acc[e] += rv.a[e] * rv.a[e];
     }
     stv<T, W>(x + t, xv);
     stv<T, W>(r + t, rv);
@@ -383,24 +402,18 @@ __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict
       for (int e = 0; e < W; ++e) rv.a[e] *= s;
       stv<T, W>(z + t, rv);
     }
-  }
-  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
+  });
 }
 
 template <typename T, int KB>
 __global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict__ a, const T *__restrict__ bb,
                                              double *__restrict__ partial) {
-  __shared__ T red[MAXNB * KB];
-  BlockRed<T, KB> R;
-  R.init(red, nb);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
+  constexpr int W = Map<T, KB>::W;
+  sweep_reduce<T, KB>(d.N, nb, partial, [&](int, int, int, long long t, T(&acc)[W]) {
     const Vec<T, W> av = ldv<T, W>(a + t), bv = ldv<T, W>(bb + t);
-    R.at(red, b, q);
 #pragma unroll
-    for (int e = 0; e < W; ++e) R.acc[e] += av.a[e] * bv.a[e];
-  }
-  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
+    for (int e = 0; e < W; ++e) acc[e] += av.a[e] * bv.a[e];
+  });
 }
 
 // p = z + beta p
@@ -424,25 +437,20 @@ __global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ 
                                                      float *__restrict__ r32, Dims d, int nb,
                                                      const int *__restrict__ active, double *__restrict__ partial) {
   using T = double;
-  __shared__ T red[MAXNB * KB];
-  BlockRed<T, KB> R;
-  R.init(red, nb);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
+  constexpr int W = Map<T, KB>::W;
+  sweep_reduce<T, KB>(d.N, nb, partial, [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
     const Vec<T, W> ax = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
     Vec<T, W> rv = ldv<T, W>(bvec + t);
-    R.at(red, b, q);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       rv.a[e] -= ax.a[e];
-      R.acc[e] += rv.a[e] * rv.a[e];
+      acc[e] += rv.a[e] * rv.a[e];
       r32[t + e] = active[b * KB + q * W + e] ? (float)rv.a[e] : 0.0f;
     }
     stv<T, W>(r64 + t, rv);
-  }
-  R.finish(red, threadIdx.x % Map<T, KB>::LPN, nb, partial);
+  });
 }
 
 __global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total4, double *__restrict__ x64,
@@ -578,6 +586,36 @@ __global__ void k_outer_check(int K, const double *__restrict__ rr, const double
     *n_active = cnt;
     *maxrel = v;
   }
+}
+
+// Device-side loop control for solves recorded into a CUDA graph with
+// conditional WHILE nodes.  ctr[0] = iterations of the current inner loop,
+// ctr[1] = inner iterations summed over sweeps, ctr[2] = refinement sweeps.
+// `init` kernels run before a WHILE node (reset the loop's counter, first
+// test); `step` kernels end its body (count, test again).  Every loop is
+// bounded by its iteration cap.
+__global__ void k_inner_loop(cudaGraphConditionalHandle hc, int init, const int *__restrict__ n_active,
+                             const int *__restrict__ status, int *__restrict__ ctr, int maxit, int total_max) {
+  if (init) {
+    ctr[0] = 0;
+  } else {
+    ctr[0] += 1;
+    ctr[1] += 1;
+  }
+  const unsigned go = (*n_active > 0) && (*status == 0) && (ctr[0] < maxit) && (ctr[1] < total_max);
+  cudaGraphSetConditional(hc, go);
+}
+
+__global__ void k_outer_loop(cudaGraphConditionalHandle hc, int init, const int *__restrict__ n_active_out,
+                             const int *__restrict__ status, int *__restrict__ ctr, int max_outer, int total_max) {
+  if (init) {
+    ctr[1] = 0;
+    ctr[2] = 0;
+  } else {
+    ctr[2] += 1;
+  }
+  const unsigned go = (*n_active_out > 0) && (*status == 0) && (ctr[2] < max_outer) && (ctr[1] < total_max);
+  cudaGraphSetConditional(hc, go);
 }
 
 __global__ void k_fill_double(double *__restrict__ a, int n, double v) {
@@ -1097,6 +1135,16 @@ void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaSt
 void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
                  double *maxrel, double *inner_tol2, double inner_floor2, double safety2, cudaStream_t s) {
   k_outer_check<<<count_launch(1), 1024, 0, s>>>(K, rr, bb, rtol2, active, n_active, maxrel, inner_tol2, inner_floor2, safety2);
+}
+
+void inner_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_active, const int *status, int *ctr,
+                     int maxit, int total_max, cudaStream_t s) {
+  k_inner_loop<<<count_launch(1), 1, 0, s>>>(hc, init, n_active, status, ctr, maxit, total_max);
+}
+
+void outer_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_active_out, const int *status, int *ctr,
+                     int max_outer, int total_max, cudaStream_t s) {
+  k_outer_loop<<<count_launch(1), 1, 0, s>>>(hc, init, n_active_out, status, ctr, max_outer, total_max);
 }
 
 void fill_double(double *a, int n, double v, cudaStream_t s) {

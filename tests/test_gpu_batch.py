@@ -1,6 +1,8 @@
-"""Independent problems of uneven size in one CUDA-graph launch: every
-problem's data equals its own adaptive solve (rtol 1e-10 -> 1e-8 relative),
-a second launch reproduces the first, and the autotuner's choice solves."""
+"""Independent problems of uneven size in one CUDA-graph launch whose solver
+loops run on the device: every problem's solution is bit-identical to its own
+host-driven adaptive solve (same arithmetic, same stopping rule), its data
+matches the simulation's dpred, a second launch reproduces the first, and the
+autotuner's choice solves."""
 
 import numpy as np
 import pytest
@@ -12,16 +14,27 @@ from simpeg_gb300.workloads import batched_problems
 pytestmark = pytest.mark.gpu
 
 
-def test_graph_batch_matches_individual_solves(cuda):
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_batch_matches_individual_solves(cuda, precision):
+    import torch
+
     from simpeg_gb300.batch import BatchedForward
 
     probs = batched_problems(seed=7, n=6, lo=(12, 12, 8), hi=(28, 24, 16), src_range=(3, 40), n_rx=5)
-    bf = BatchedForward(probs, precision="mixed", rtol=1e-10)
+    bf = BatchedForward(probs, precision=precision, rtol=1e-10)
     d1 = bf.run()
+    assert bf.resolved == []
     conv = bf.convergence()
-    assert all(na == 0 and mr <= 1e-10 for mr, na in conv), conv
+    assert all(na == 0 and mr <= 1e-10 and it > 0 for mr, na, it, _ in conv), conv
+    X1 = [p.X.clone() for p in bf.problems]
+    for p in bf.problems:  # stale workspace contents (all-ones bytes: NaN doubles) must not matter
+        p.ws.fill_(255)
     bf.launch()
     d2 = bf.data()
+    for p, x1, (mr, na, it, sw) in zip(bf.problems, X1, conv):
+        xs, info = p.engine.solve(p.Q, mode=precision, rtol=1e-10)
+        torch.testing.assert_close(x1, xs, rtol=0, atol=0)
+        assert info.iterations == it and info.outer == sw
     for (mesh, sigma, survey), a, b in zip(probs, d1, d2):
         sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.IdentityMap(mesh), rtol=1e-10)
         ref = sim.dpred(sigma)
