@@ -70,6 +70,19 @@ int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int 
  * lanes).  Set by the autotuner. */
 int dc_set_rhs_block(dc_handle *h, int kb);
 
+/* Storage of the multigrid vectors inside the mixed-precision solve: 16
+ * (fp16, default; the V-cycle input is scaled to unit norm per RHS and every
+ * operation is done in fp32) or 32 bits.  The preconditioner only steers the
+ * fp32 PCG, which the fp64 refinement corrects, so this changes iteration
+ * counts, not the accuracy the solve reaches.  The fp64 solve keeps fp64. */
+int dc_set_mg_storage(dc_handle *h, int bits);
+
+/* Multigrid smoother: Chebyshev polynomial of D^-1 A of the first kind on
+ * [lmax/cheb_ratio, lmax] (kind 1, default) or of the fourth kind on
+ * [0, lmax] (kind 4, which needs no lower bound), lmax the Gershgorin bound of
+ * D^-1 A; degrees nu_pre / nu_post (dc_set_params). */
+int dc_set_smoother(dc_handle *h, int kind);
+
 /* Number of multigrid levels and nodes of level `lvl`. */
 int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3);
 
@@ -86,7 +99,9 @@ int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes);
 
 /* x = A^-1 b for k column-major RHS.  Replaces `Ainv * RHS`
  * (simulation.py:111, :181, :245).  Converged when |b - A x| <= rtol |b| per RHS.
- * inner_rtol / inner_maxit apply to the fp32 inner solves of DC_MODE_MIXED.
+ * inner_rtol / inner_maxit apply to the fp32 inner solves of DC_MODE_MIXED:
+ * an inner solve stops at the tolerance that closes the remaining outer gap
+ * (x0.3) but never asks for less than inner_rtol (<= 0 selects 3e-5).
  * ws may be NULL (the handle then allocates and caches its own). */
 int dc_solve(dc_handle *h, int mode, const double *b_dev, double *x_dev, int k, double rtol, int maxit,
              double inner_rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream);

@@ -54,6 +54,8 @@ _SIG = {
     "dc_last_error": (C.c_char_p, []),
     "dc_set_params": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
     "dc_set_rhs_block": (C.c_int, [_VP, C.c_int]),
+    "dc_set_mg_storage": (C.c_int, [_VP, C.c_int]),
+    "dc_set_smoother": (C.c_int, [_VP, C.c_int]),
     "dc_level_info": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
     "dc_set_model": (C.c_int, [_VP, _DP, _VP]),
     "dc_apply": (C.c_int, [_VP, _DP, _DP, C.c_int, _VP]),

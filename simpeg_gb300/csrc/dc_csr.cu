@@ -191,7 +191,7 @@ int dc_csr_solve(dc_csr *h, const double *b, double *x, int k, double rtol, int 
   double *pa = z + nk, *pb = pa + (size_t)gx * k, *pc = pb + (size_t)gx * k;
   double *rz = pc + (size_t)gx * k, *rr = rz + k, *bb = rr + k, *al = bb + k, *be = al + k, *tol2 = be + k;
   int *active = (int *)(tol2 + k), *n_active = active + k, *status = n_active + 1;
-  using O = Ops<double, 1>;
+  using O = Ops<double, double, 1>;
   CK(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
   CK(cudaMemcpyAsync(r, b, sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
   fill_int(active, k, 1, s);
@@ -203,12 +203,12 @@ int dc_csr_solve(dc_csr *h, const double *b, double *x, int k, double rtol, int 
   k_jacobi_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->dinv, r, z, pc);
   CK(cudaMemsetAsync(n_active, 0, sizeof(int), s));
   pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, n_active, 1, s);
-  O::copy(n, k, p, z, s);
+  O::copy_z(n, k, p, z, s);
   int it = 0;
   for (; it < maxit; ++it) {
     k_csr_apply_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->ptr, h->idx, h->val, p, q, pa);
     pcg_alpha(k, 1, gx, pa, rz, active, al, status, n_active, s);
-    O::update_xr(n, k, x, r, p, q, al, pb, gx, nullptr, 0.0, nullptr, s);
+    O::update_xr(n, k, x, r, p, q, al, pb, gx, nullptr, 0.0, nullptr, nullptr, nullptr, s);
     k_jacobi_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->dinv, r, z, pc);
     pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, n_active, 0, s);
     O::p_update(n, k, p, z, be, s);

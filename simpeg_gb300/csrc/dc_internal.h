@@ -87,30 +87,46 @@ void set_sm_count(int n);
 // grid of the reduction kernels: one block per (node group) up to per_sm resident blocks per SM
 int node_grid(long long nodes, int KB, int nb, int per_sm);
 
-template <typename T, int KB> struct Ops {
-  // resident blocks per SM of the slowest-occupancy reduction kernel
+// Right-hand side of a smoothing kernel: on the finest level the PCG residual
+// (type T; multiplied per RHS lane by `scale` when that is set), on coarser
+// levels the restricted residual (the multigrid storage type V).
+template <typename T, typename V> struct Rhs {
+  const T *full = nullptr;
+  const V *part = nullptr;
+  const float *scale = nullptr;
+};
+
+// Launchers of the node kernels (dc_kernels.cuh).  T: arithmetic and PCG
+// vector type; V: storage type of the multigrid vectors (T, or __half inside
+// the mixed-precision solve); KB: RHS lanes per block.
+template <typename T, typename V, int KB> struct Ops {
+  // resident blocks per SM of the highest-occupancy reduction kernel (sizes the partial arrays)
   static int red_blocks_per_sm();
   // y = A x ; if partial: per-block partial sums of x.y
   static void apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
-  static void residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s);
+  // res = r - A z
+  static void residual(const Level &L, Rhs<T, V> r, const V *z, V *res, int nb, cudaStream_t s);
   // z = c0 D^-1 r (first Chebyshev step from zero)
-  static void cheb_first(const Level &L, const T *r, T *z, int nb, double c0, cudaStream_t s);
+  static void cheb_first(const Level &L, Rhs<T, V> r, V *z, int nb, double c0, cudaStream_t s);
   // zout = zin + c1 (zin - prev) + c2 D^-1 (r - A zin); prev: 0 none, 1 = zout's old content, 2 = zero.
-  // With partial: also per-block partials of r . zout.
-  static void cheb_step(const Level &L, const T *r, const T *zin, T *zout, int prev, int nb, double c1, double c2,
-                        double *partial, int gx, cudaStream_t s);
-  template <bool DOT, int PREV>
-  static void cheb_launch(const Level &L, const T *r, const T *zin, T *zout, int nb, double c1, double c2,
-                          double *partial, int gx, cudaStream_t s);
-  static void restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s);
-  static void prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s);
-  static void coarse_solve(const T *Ainv, const Level &c, const T *rc, T *zc, int nb, cudaStream_t s);
-  // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = c0 D^-1 r on that level.
+  // With partial (finest level only): also per-block partials of r . zout.
+  static void cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb, double c1,
+                        double c2, double *partial, int gx, cudaStream_t s);
+  static void restrict_(const Level &f, const Level &c, const V *res, V *rc, int nb, cudaStream_t s);
+  static void prolong_add(const Level &f, const Level &c, const V *zc, V *z, int nb, cudaStream_t s);
+  static void coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V *zc, int nb, cudaStream_t s);
+  // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = c0 D^-1 (scale r) on that level
+  // and, when rv_out is set, rv_out = V(scale r).
   static void update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                        double *partial, int gx, const Level *smooth, double c0, T *z, cudaStream_t s);
+                        double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
+                        V *rv_out, cudaStream_t s);
+  // rv_out = V(scale r)
+  static void scale_to(long long N, int nb, const T *r, const float *scale, V *rv_out, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
-  static void p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s);
-  static void copy(long long N, int nb, T *dst, const T *src, cudaStream_t s);
+  static void dot_z(long long N, int nb, const T *a, const V *b, double *partial, int gx, cudaStream_t s);
+  // p = z + beta p
+  static void p_update(long long N, int nb, T *p, const V *z, const double *beta, cudaStream_t s);
+  static void copy_z(long long N, int nb, T *dst, const V *src, cudaStream_t s);
 };
 
 template <int KB>
@@ -118,15 +134,20 @@ void ir_residual(const Level &L, const double *b, const double *x, double *r64, 
                  const int *active, double *partial, int gx, cudaStream_t s);
 template <int KB>
 void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s);
+template <int KB>
+int ir_blocks_per_sm();
 
 void fill_int(int *a, int n, int v, cudaStream_t s);
 // alpha = rz / (p.q) per active RHS; also zeroes *n_active for the pcg_beta of the same iteration
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
                int *status, int *n_active, cudaStream_t s);
+// rz = r.z (divided per RHS by rz_div when set: z came from the scaled input) ;
+// rr = |r|^2 ; active &= rr > tol2*bb ; beta ; counts active ; scale_out = 1/sqrt(rr) when set
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
               const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
-              cudaStream_t s);
-void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s);
+              cudaStream_t s, const float *rz_div = nullptr, float *scale_out = nullptr);
+// per-RHS sums of block partials; with scale, also scale = 1/sqrt(sum) (the V-cycle input scale)
+void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s, float *scale = nullptr);
 void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
                  double *maxrel, double *inner_tol2, double inner_floor2, double safety2, cudaStream_t s);
 void fill_double(double *a, int n, double v, cudaStream_t s);

@@ -1,0 +1,747 @@
+// Node kernels of the nodal DC engine: stencil, Chebyshev smoothing,
+// multigrid transfers, PCG vector updates and fixed-order reductions, with the
+// host-side launchers of Ops<T, V, KB>.  Included by the translation units
+// that instantiate Ops for one (compute, storage) pair each, so the template
+// instantiations compile in parallel.
+//
+// Thread mapping of every node kernel: a thread owns W consecutive RHS lanes
+// of one node (16 bytes of the compute type T: 4 fp32 / 2 fp64 lanes),
+// KB/W threads share a node, and a 1D grid sweeps the flat (RHS block, node)
+// index with the RHS block slowest.  Lane l of node n in RHS block b is
+// element (b*N + n)*KB + l, so a warp's accesses are contiguous.
+//
+// Types: T is the arithmetic type (float inside the mixed-precision inner
+// solve, double in the fp64 solve).  V is the storage type of the multigrid
+// vectors (smoother iterates, residuals and corrections on every level, and
+// the preconditioned vector z): T itself, or __half for the mixed solve,
+// which halves the bytes the V-cycle moves.  Arithmetic is always in T.
+// R is the type of a smoother's right-hand side: the PCG residual (T) on the
+// finest level, the restricted residual (V) below it.
+#pragma once
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <type_traits>
+
+#include "dc_internal.h"
+
+namespace dc {
+
+extern int g_n_sm;
+int resident_blocks(const void *func);
+
+namespace {
+
+constexpr int TPB = 256;
+
+// floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
+__device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
+  if (d == 1) return n;
+  unsigned q = __umulhi((unsigned)n, m);
+  q -= (q * (unsigned)d > (unsigned)n) ? 1u : 0u;
+  return (int)q;
+}
+
+__device__ __forceinline__ void node_ijk(int n, const Dims &d, int &i, int &j, int &k) {
+  const int nxy = d.Nx * d.Ny;
+  k = fast_div(n, nxy, d.mxy);
+  const int r = n - k * nxy;
+  j = fast_div(r, d.Nx, d.mx);
+  i = r - j * d.Nx;
+}
+
+template <typename C> struct CoefT;
+template <> struct CoefT<double> { using type = Coef64; };
+template <> struct CoefT<float> { using type = Coef32; };
+
+template <typename T, int W> struct alignas(sizeof(T) * W) Vec {
+  T a[W];
+};
+
+// W lanes of storage type S at p, converted to T (and back).  For S == T a
+// plain vector access; for __half an 8-byte (W = 4) access and conversions.
+template <typename T, int W, typename S>
+__device__ __forceinline__ Vec<T, W> ld(const S *p) {
+  if constexpr (std::is_same<S, T>::value) {
+    return *reinterpret_cast<const Vec<T, W> *>(p);
+  } else {
+    const Vec<S, W> raw = *reinterpret_cast<const Vec<S, W> *>(p);
+    Vec<T, W> v;
+#pragma unroll
+    for (int e = 0; e < W; ++e) v.a[e] = (T)(float)raw.a[e];
+    return v;
+  }
+}
+
+template <typename T, int W, typename S>
+__device__ __forceinline__ void st(S *p, const Vec<T, W> &v) {
+  if constexpr (std::is_same<S, T>::value) {
+    *reinterpret_cast<Vec<T, W> *>(p) = v;
+  } else {
+    Vec<S, W> raw;
+#pragma unroll
+    for (int e = 0; e < W; ++e) raw.a[e] = S((float)v.a[e]);
+    *reinterpret_cast<Vec<S, W> *>(p) = raw;
+  }
+}
+
+// Per-thread geometry of the "node x lane-group" mapping: a thread owns W
+// consecutive RHS lanes of one RHS block, 16 bytes of the storage type S the
+// kernel streams (4 fp32, 2 fp64 or 8 fp16 lanes), and LPN threads share one
+// node.  Kernels sweep the RHS blocks one after the other (RHS block =
+// slowest index of the flat work index), so the L2 working set of the
+// stencil's z-neighbour planes is that of one RHS block at a time.
+template <typename S, int KB> struct Lanes {
+  static constexpr int W = (int)(16 / sizeof(S)) < KB ? (int)(16 / sizeof(S)) : KB;
+  static constexpr int LPN = KB / W;  // threads per node
+};
+
+template <typename T, int KB>
+__device__ __forceinline__ const typename CoefT<T>::type *coef_of(const void *c) {
+  return reinterpret_cast<const typename CoefT<T>::type *>(c);
+}
+
+// (A x) for the W lanes at element t of node n = (i, j, k); x stored as S.
+// Branch-free: all seven loads are issued unconditionally (off-mesh
+// neighbours are redirected to the node itself and get weight 0; c* is zero
+// on the last node of its axis), so they are all in flight at once.
+template <typename T, int KB, int W, typename S>
+__device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *__restrict__ coef,
+                                                  const S *__restrict__ x, long long t, int n, int i, int j, int k,
+                                                  const Dims &d) {
+  const int sxn = 1, syn = d.Nx, szn = d.Nx * d.Ny;
+  const bool hx = i > 0, hy = j > 0, hz = k > 0;
+  const bool px = i + 1 < d.Nx, py = j + 1 < d.Ny, pz = k + 1 < d.Nz;
+  const auto c = coef[n];
+  const T wxm = coef[hx ? n - sxn : n].cx, wym = coef[hy ? n - syn : n].cy, wzm = coef[hz ? n - szn : n].cz;
+  const Vec<T, W> v0 = ld<T, W>(x + t);
+  const Vec<T, W> vxp = ld<T, W>(x + t + (px ? (long long)sxn * KB : 0));
+  const Vec<T, W> vxm = ld<T, W>(x + t - (hx ? (long long)sxn * KB : 0));
+  const Vec<T, W> vyp = ld<T, W>(x + t + (py ? (long long)syn * KB : 0));
+  const Vec<T, W> vym = ld<T, W>(x + t - (hy ? (long long)syn * KB : 0));
+  const Vec<T, W> vzp = ld<T, W>(x + t + (pz ? (long long)szn * KB : 0));
+  const Vec<T, W> vzm = ld<T, W>(x + t - (hz ? (long long)szn * KB : 0));
+  const T cxp = px ? c.cx : (T)0, cyp = py ? c.cy : (T)0, czp = pz ? c.cz : (T)0;
+  const T cxm = hx ? wxm : (T)0, cym = hy ? wym : (T)0, czm = hz ? wzm : (T)0;
+  Vec<T, W> acc;
+#pragma unroll
+  for (int e = 0; e < W; ++e)
+    acc.a[e] = c.d * v0.a[e] - cxp * vxp.a[e] - cxm * vxm.a[e] - cyp * vyp.a[e] - cym * vym.a[e] - czp * vzp.a[e] -
+               czm * vzm.a[e];
+  return acc;
+}
+
+// Right-hand side r (type R) of a smoothing kernel at element t, times the
+// per-lane scale when given (the finest level's PCG residual, see Rhs).
+template <typename T, int KB, int W, typename R>
+__device__ __forceinline__ Vec<T, W> rhs_at(const R *__restrict__ r, const float *__restrict__ scale, long long t,
+                                             int b, int q) {
+  Vec<T, W> v = ld<T, W>(r + t);
+  if (scale) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) v.a[e] *= (T)scale[b * KB + q * W + e];
+  }
+  return v;
+}
+
+// Sweep over (RHS block b, node n, lane group q) with b slowest, W lanes per
+// thread.  Defines W,
+// LPN, q and, per iteration, ng (flat node index over all RHS blocks), b, n and
+// t (offset of the thread's W lanes).
+#define SWEEP(NN, MAGIC, NB, WIDTH)                                                            \
+  constexpr int W = (WIDTH), LPN = KB / W;                                                     \
+  const int q = threadIdx.x % LPN;                                                             \
+  const long long total_ = (long long)(NN) * (NB) * LPN;                                       \
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total_; g += (long long)gridDim.x * TPB)
+
+#define SWEEP_INDEX(NN, MAGIC)                        \
+  const int ng = (int)(g / LPN);                      \
+  const int b = fast_div(ng, (int)(NN), (MAGIC));     \
+  const int n = ng - b * (int)(NN);                   \
+  const long long t = (long long)ng * KB + q * W;     \
+  (void)b;                                            \
+  (void)n;
+
+// Reductions (per-RHS dot products) are bitwise reproducible: every thread
+// sums its own elements in sweep order, threads of one lane group are
+// combined by warp shuffles, and the warps' sums in warp order -- no
+// floating-point atomics, so a solve repeated on the same data (or recorded in
+// a CUDA graph) takes the same iterations and returns the same bits.
+// Block partials land in partial[(b * gs + blockIdx.x) * KB + lane]; gs >=
+// gridDim.x is the stride the consumer sums over (block 0 zeroes the unused
+// tail), so every reduction kernel can run its own resident-capped grid.
+template <typename T, int KB, int W>
+__device__ __forceinline__ void block_reduce(T (&acc)[W], T *red, int b, double *partial, int gs) {
+  constexpr int LPN = KB / W;
+#pragma unroll
+  for (int o = 16; o >= LPN; o >>= 1)
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < LPN)
+#pragma unroll
+    for (int e = 0; e < W; ++e) red[warp * KB + lane * W + e] = acc[e];
+  __syncthreads();
+  if (threadIdx.x < KB) {
+    T v = (T)0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; ++w) v += red[w * KB + threadIdx.x];
+    partial[((long long)b * gs + blockIdx.x) * KB + threadIdx.x] = (double)v;
+  }
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < (gs - (int)gridDim.x) * KB; i += TPB)
+      partial[((long long)b * gs + gridDim.x) * KB + i] = 0.0;
+  __syncthreads();
+}
+
+// Sweep of a reducing kernel: the RHS blocks one after the other (the whole
+// grid on one RHS block at a time, as in the flat sweep), each closed by the
+// block reduction of that RHS block's per-thread sums.
+// body(b, n, q, t, acc): RHS block, node, lane group, element offset, sums.
+template <typename T, int KB, int W, typename Body>
+__device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int gs, Body body) {
+  constexpr int LPN = KB / W;
+  __shared__ T red[(TPB / 32) * KB];
+  const int q = threadIdx.x % LPN;
+  const long long per = (long long)N * LPN;
+  for (int b = 0; b < nb; ++b) {
+    T acc[W];
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] = (T)0;
+    const long long base = (long long)b * N;
+    for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < per; g += (long long)gridDim.x * TPB) {
+      const int n = (int)(g / LPN);
+      body(b, n, q, (base + n) * KB + q * W, acc);
+    }
+    block_reduce<T, KB, W>(acc, red, b, partial, gs);
+  }
+}
+
+// The same body over the flat (RHS block, node, lane group) sweep, no reduction.
+template <typename T, int KB, int W, typename Body>
+__device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body) {
+  constexpr int LPN = KB / W;
+  const int q = threadIdx.x % LPN;
+  const long long total = (long long)N * nb * LPN;
+  T acc[W];
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total; g += (long long)gridDim.x * TPB) {
+    const int ng = (int)(g / LPN);
+    const int b = fast_div(ng, N, mn);
+    body(b, ng - b * N, q, (long long)ng * KB + q * W, acc);
+  }
+}
+
+// ---------------------------------------------------------------- stencil ops
+// y = A x (PCG vectors, type T); with DOT also per-block partials of x.y.
+template <typename T, int KB, bool DOT>
+__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
+                                               T *__restrict__ y, Dims d, int nb, double *__restrict__ partial,
+                                               int gs) {
+  constexpr int W = Lanes<T, KB>::W;
+  const auto *coef = coef_of<T, KB>(cf);
+  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const Vec<T, W> v = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
+    st<T, W>(y + t, v);
+    if (DOT) {
+      const Vec<T, W> xv = ld<T, W>(x + t);
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
+    }
+  };
+  if (DOT)
+    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body);
+  else
+    sweep_flat<T, KB, W>(d.N, d.mn, nb, body);
+}
+
+// res = r - A z
+template <typename T, typename V, typename R, int KB>
+__global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, const R *__restrict__ r,
+                                                  const float *__restrict__ scale, const V *__restrict__ z,
+                                                  V *__restrict__ res, Dims d, int nb) {
+  constexpr int W = Lanes<V, KB>::W;
+  const auto *coef = coef_of<T, KB>(cf);
+  sweep_flat<T, KB, W>(d.N, d.mn, nb, [&](int b, int n, int q, long long t, T(&)[W]) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, z, t, n, i, j, k, d);
+    Vec<T, W> rv = rhs_at<T, KB, W>(r, scale, t, b, q);
+#pragma unroll
+    for (int e = 0; e < W; ++e) rv.a[e] -= az.a[e];
+    st<T, W>(res + t, rv);
+  });
+}
+
+// First Chebyshev step from z = 0: z = c0 * D^-1 r.
+template <typename T, typename V, typename R, int KB>
+__global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, const R *__restrict__ r,
+                                                    const float *__restrict__ scale, V *__restrict__ z, Dims d,
+                                                    int nb, T c0) {
+  constexpr int W = Lanes<V, KB>::W;
+  sweep_flat<T, KB, W>(d.N, d.mn, nb, [&](int b, int n, int q, long long t, T(&)[W]) {
+    const T s = c0 * invd[n];
+    Vec<T, W> v = rhs_at<T, KB, W>(r, scale, t, b, q);
+#pragma unroll
+    for (int e = 0; e < W; ++e) v.a[e] *= s;
+    st<T, W>(z + t, v);
+  });
+}
+
+// Chebyshev step in three-term form (x_{k+1} = x_k + c1 (x_k - x_{k-1}) + c2 D^-1 (r - A x_k)):
+//   PREV = 0: no momentum term (first step from a nonzero start, c1 = 0)
+//   PREV = 1: x_{k-1} read from zout (overwritten in place with x_{k+1})
+//   PREV = 2: x_{k-1} = 0 (second step of a zero-start sequence)
+// Four streams per RHS lane (x_k, r, x_{k-1} read; x_{k+1} write) instead of the
+// five of the d-vector form.  With DOT (finest level), also per-block partials
+// of r . x_{k+1} with the unscaled PCG residual r.
+template <typename T, typename V, typename R, int KB, bool DOT, int PREV>
+__global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
+                                                   const R *__restrict__ r, const float *__restrict__ scale,
+                                                   const V *__restrict__ zin, V *zout, Dims d, int nb, T c1, T c2,
+                                                   double *__restrict__ partial, int gs) {
+  constexpr int W = Lanes<V, KB>::W;
+  const auto *coef = coef_of<T, KB>(cf);
+  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, zin, t, n, i, j, k, d);
+    const Vec<T, W> rv = ld<T, W>(r + t);
+    const Vec<T, W> zc = ld<T, W>(zin + t);
+    Vec<T, W> zo;
+    if (PREV == 1) zo = ld<T, W>(zout + t);
+    const T s = c2 * invd[n];
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      T mom = (T)0;
+      if (PREV == 1) mom = c1 * (zc.a[e] - zo.a[e]);
+      if (PREV == 2) mom = c1 * zc.a[e];
+      const T re = scale ? rv.a[e] * (T)scale[b * KB + q * W + e] : rv.a[e];
+      zo.a[e] = zc.a[e] + mom + s * (re - az.a[e]);
+    }
+    st<T, W>(zout + t, zo);
+    if (DOT) {
+      // r . z with z as stored (rounded to V): the preconditioned vector PCG uses
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        if constexpr (std::is_same<V, T>::value)
+          acc[e] += rv.a[e] * zo.a[e];
+        else
+          acc[e] += rv.a[e] * (T)(float)V((float)zo.a[e]);
+      }
+    }
+  };
+  if (DOT)
+    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body);
+  else
+    sweep_flat<T, KB, W>(d.N, d.mn, nb, body);
+}
+
+// ---------------------------------------------------------------- transfers
+struct XferTab {
+  const int *fi;        // coarse node -> fine node, per axis at roff[a]
+  const void *wl, *wr;  // T weights of fine fi-1 / fi+1
+  const int *pl;        // fine node -> left coarse node, per axis at poff[a]
+  const void *pw;       // T weight on pl
+  long long roff[3], poff[3];
+};
+
+template <typename T, typename V, int KB>
+__global__ void __launch_bounds__(TPB) k_restrict(const V *__restrict__ res, V *__restrict__ rc, Dims f, Dims c,
+                                                  int nb, XferTab tb) {
+  const T *wl = (const T *)tb.wl, *wr = (const T *)tb.wr;
+  SWEEP(c.N, c.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(c.N, c.mn)
+    int I, J, K;
+    node_ijk(n, c, I, J, K);
+    const int fx = tb.fi[tb.roff[0] + I], fy = tb.fi[tb.roff[1] + J], fz = tb.fi[tb.roff[2] + K];
+    const T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
+    const T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
+    const T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
+    const long long fb = (long long)b * f.N * KB + q * W;
+    Vec<T, W> acc;
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc.a[e] = 0;
+#pragma unroll
+    for (int cz = 0; cz < 3; ++cz) {
+      if (wz[cz] == (T)0) continue;
+#pragma unroll
+      for (int cy = 0; cy < 3; ++cy) {
+        if (wy[cy] == (T)0) continue;
+        const T wyz = wy[cy] * wz[cz];
+        const long long row = ((long long)(fz + cz - 1) * f.Ny + (fy + cy - 1)) * f.Nx;
+#pragma unroll
+        for (int cx = 0; cx < 3; ++cx) {
+          if (wx[cx] == (T)0) continue;
+          const T w = wx[cx] * wyz;
+          const Vec<T, W> v = ld<T, W>(res + fb + (row + fx + cx - 1) * KB);
+#pragma unroll
+          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
+        }
+      }
+    }
+    st<T, W>(rc + t, acc);
+  }
+}
+
+template <typename T, typename V, int KB>
+__global__ void __launch_bounds__(TPB) k_prolong_add(const V *__restrict__ zc, V *__restrict__ z, Dims f, Dims c,
+                                                     int nb, XferTab tb) {
+  const T *pw = (const T *)tb.pw;
+  SWEEP(f.N, f.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(f.N, f.mn)
+    int i, j, k;
+    node_ijk(n, f, i, j, k);
+    const int I = tb.pl[tb.poff[0] + i], J = tb.pl[tb.poff[1] + j], K = tb.pl[tb.poff[2] + k];
+    const T ax = pw[tb.poff[0] + i], ay = pw[tb.poff[1] + j], az = pw[tb.poff[2] + k];
+    const T wx[2] = {ax, (T)1 - ax}, wy[2] = {ay, (T)1 - ay}, wz[2] = {az, (T)1 - az};
+    const long long cb = (long long)b * c.N * KB + q * W;
+    Vec<T, W> acc = ld<T, W>(z + t);
+#pragma unroll
+    for (int bz = 0; bz < 2; ++bz) {
+      if (wz[bz] == (T)0) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        if (wy[a] == (T)0) continue;
+        const T wyz = wy[a] * wz[bz];
+        const long long row = ((long long)(K + bz) * c.Ny + (J + a)) * c.Nx;
+#pragma unroll
+        for (int e2 = 0; e2 < 2; ++e2) {
+          if (wx[e2] == (T)0) continue;
+          const T w = wx[e2] * wyz;
+          const Vec<T, W> v = ld<T, W>(zc + cb + (row + I + e2) * KB);
+#pragma unroll
+          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
+        }
+      }
+    }
+    st<T, W>(z + t, acc);
+  }
+}
+
+// z_c = Ainv r_c on the coarsest level (dense, row-major Ainv[nc][nc]).
+template <typename T, typename V, typename R, int KB>
+__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, Dims c, int nb,
+                                                      const R *__restrict__ rc, const float *__restrict__ scale,
+                                                      V *__restrict__ zc) {
+  const int nc = (int)c.N;
+  SWEEP(c.N, c.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(c.N, c.mn)
+    const T *row = Ainv + (long long)n * nc;
+    const long long base = (long long)b * nc * KB + q * W;
+    Vec<T, W> acc;
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc.a[e] = 0;
+    for (int m = 0; m < nc; ++m) {
+      const T w = row[m];
+      const Vec<T, W> v = rhs_at<T, KB, W>(rc, scale, base + (long long)m * KB, b, q);
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
+    }
+    st<T, W>(zc + t, acc);
+  }
+}
+
+// ---------------------------------------------------------------- PCG vectors
+// x += a p ; r -= a q ; partial |r|^2 (a per RHS).  With SMOOTH, also the first
+// Chebyshev step of the fine level on the new residual: z = c0 D^-1 (scale r).
+template <typename T, typename V, int KB, bool SMOOTH>
+__global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict__ x, T *__restrict__ r,
+                                                   const T *__restrict__ p, const T *__restrict__ qv,
+                                                   const double *__restrict__ alpha, double *__restrict__ partial,
+                                                   const T *__restrict__ invd, V *__restrict__ z, T c0,
+                                                   const float *__restrict__ scale, V *__restrict__ rv_out, int gs) {
+  constexpr int W = Lanes<T, KB>::W;
+  sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
+    Vec<T, W> xv = ld<T, W>(x + t), rv = ld<T, W>(r + t);
+    const Vec<T, W> pv = ld<T, W>(p + t), qq = ld<T, W>(qv + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const T a = (T)alpha[b * KB + q * W + e];
+      xv.a[e] += a * pv.a[e];
+      rv.a[e] -= a * qq.a[e];
+      acc[e] += rv.a[e] * rv.a[e];
+    }
+    st<T, W>(x + t, xv);
+    st<T, W>(r + t, rv);
+    if (SMOOTH) {
+      if (scale) {
+#pragma unroll
+        for (int e = 0; e < W; ++e) rv.a[e] *= (T)scale[b * KB + q * W + e];
+      }
+      if (rv_out) st<T, W>(rv_out + t, rv);
+      const T s = c0 * invd[n];
+#pragma unroll
+      for (int e = 0; e < W; ++e) rv.a[e] *= s;
+      st<T, W>(z + t, rv);
+    }
+  });
+}
+
+// rv_out = V(scale r): the finest level's V-cycle input in the storage type.
+template <typename T, typename V, int KB>
+__global__ void __launch_bounds__(TPB) k_scale_to(Dims d, int nb, const T *__restrict__ r,
+                                                  const float *__restrict__ scale, V *__restrict__ rv_out) {
+  SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(d.N, d.mn)
+    st<T, W>(rv_out + t, rhs_at<T, KB, W>(r, scale, t, b, q));
+  }
+}
+
+template <typename T, typename S, int KB>
+__global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict__ a, const S *__restrict__ bb,
+                                             double *__restrict__ partial, int gs) {
+  constexpr int W = Lanes<S, KB>::W;
+  sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int, int, int, long long t, T(&acc)[W]) {
+    const Vec<T, W> av = ld<T, W>(a + t), bv = ld<T, W>(bb + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[e] += av.a[e] * bv.a[e];
+  });
+}
+
+// p = z + beta p
+template <typename T, typename V, int KB>
+__global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, T *__restrict__ p, const V *__restrict__ z,
+                                                  const double *__restrict__ beta) {
+  SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(d.N, d.mn)
+    Vec<T, W> pv = ld<T, W>(p + t);
+    const Vec<T, W> zv = ld<T, W>(z + t);
+#pragma unroll
+    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + (T)beta[b * KB + q * W + e] * pv.a[e];
+    st<T, W>(p + t, pv);
+  }
+}
+
+// p = z (type conversion copy)
+template <typename T, typename V, int KB>
+__global__ void __launch_bounds__(TPB) k_copy_z(Dims d, int nb, T *__restrict__ p, const V *__restrict__ z) {
+  SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
+    SWEEP_INDEX(d.N, d.mn)
+    st<T, W>(p + t, ld<T, W>(z + t));
+  }
+}
+
+// ---------------------------------------------------------------- grids
+inline int grid_nodes(long long nodes, int LPN, int nb, int n_sm, int per_sm = 8) {
+  long long g = (nodes * (nb > 0 ? nb : 1) * LPN + TPB - 1) / TPB;
+  const long long cap = (long long)n_sm * per_sm;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+inline int grid_flat(long long total, int n_sm) {
+  long long g = (total + TPB - 1) / TPB;
+  long long cap = (long long)n_sm * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+inline Dims flat_dims(long long N) {
+  Dims d{};
+  d.Nx = 1;
+  d.Ny = 1;
+  d.Nz = (int)N;
+  d.N = N;
+  d.mn = div_magic((unsigned)N);
+  return d;
+}
+
+template <typename T>
+const void *coef_ptr(const Level &L) {
+  return std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32;
+}
+template <typename T>
+const T *invd_ptr(const Level &L) {
+  return reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
+                                                                    : (const void *)L.d_invd32);
+}
+
+template <typename T>
+XferTab make_tab(const Level &f) {
+  XferTab tb;
+  const bool dbl = std::is_same<T, double>::value;
+  tb.fi = f.d_r_fi;
+  tb.wl = dbl ? (const void *)f.d_r_wl : (const void *)f.d_r_wl32;
+  tb.wr = dbl ? (const void *)f.d_r_wr : (const void *)f.d_r_wr32;
+  tb.pl = f.d_pl_idx;
+  tb.pw = dbl ? (const void *)f.d_pl_w : (const void *)f.d_pl_w32;
+  for (int a = 0; a < 3; ++a) {
+    tb.roff[a] = f.r_off[a];
+    tb.poff[a] = f.pl_off[a];
+  }
+  return tb;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+// Grids of the non-reducing sweeps are capped at the blocks the GPU holds at
+// once (resident_blocks), so every sweep is one wave and the stencil's
+// neighbour planes are reused from L2.
+#define GRID_KL(NODES, KERNEL, LPN) \
+  count_launch(dim3(grid_nodes((NODES), (LPN), nb, g_n_sm, resident_blocks((const void *)(KERNEL)))))
+#define GRID_K(NODES, KERNEL) GRID_KL(NODES, KERNEL, (Lanes<V, KB>::LPN))
+
+// Grid of a reducing kernel: its own resident-capped grid, at most gx (the
+// stride of the partial arrays).
+#define RED_GRID(NODES, KERNEL, LPN) \
+  count_launch(dim3(std::min(gx, grid_nodes((NODES), (LPN), nb, g_n_sm, resident_blocks((const void *)(KERNEL))))))
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
+  if (partial)
+    k_apply<T, KB, true><<<RED_GRID(L.dims.N, (k_apply<T, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+        coef_ptr<T>(L), x, y, L.dims, nb, partial, gx);
+  else
+    k_apply<T, KB, false><<<GRID_KL(L.dims.N, (k_apply<T, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+        coef_ptr<T>(L), x, y, L.dims, nb, nullptr, 0);
+}
+
+template <typename T, typename V, int KB>
+int Ops<T, V, KB>::red_blocks_per_sm() {
+  int m = resident_blocks((const void *)k_apply<T, KB, true>);
+  m = std::max(m, resident_blocks((const void *)k_cheb_step<T, V, T, KB, true, 1>));
+  m = std::max(m, resident_blocks((const void *)k_cheb_step<T, V, V, KB, true, 1>));
+  m = std::max(m, resident_blocks((const void *)k_update_xr<T, V, KB, true>));
+  m = std::max(m, resident_blocks((const void *)k_update_xr<T, V, KB, false>));
+  m = std::max(m, resident_blocks((const void *)k_dot<T, T, KB>));
+  m = std::max(m, resident_blocks((const void *)k_dot<T, V, KB>));
+  return m;
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::residual(const Level &L, Rhs<T, V> r, const V *z, V *res, int nb, cudaStream_t s) {
+  if (r.full)
+    k_residual<T, V, T, KB><<<GRID_K(L.dims.N, (k_residual<T, V, T, KB>)), TPB, 0, s>>>(
+        coef_ptr<T>(L), r.full, r.scale, z, res, L.dims, nb);
+  else
+    k_residual<T, V, V, KB><<<GRID_K(L.dims.N, (k_residual<T, V, V, KB>)), TPB, 0, s>>>(
+        coef_ptr<T>(L), r.part, nullptr, z, res, L.dims, nb);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::cheb_first(const Level &L, Rhs<T, V> r, V *z, int nb, double c0, cudaStream_t s) {
+  if (r.full)
+    k_cheb_first<T, V, T, KB><<<GRID_K(L.dims.N, (k_cheb_first<T, V, T, KB>)), TPB, 0, s>>>(
+        invd_ptr<T>(L), r.full, r.scale, z, L.dims, nb, (T)c0);
+  else
+    k_cheb_first<T, V, V, KB><<<GRID_K(L.dims.N, (k_cheb_first<T, V, V, KB>)), TPB, 0, s>>>(
+        invd_ptr<T>(L), r.part, nullptr, z, L.dims, nb, (T)c0);
+}
+
+template <typename T, typename V, int KB, typename R, bool DOT, int PREV>
+static void cheb_launch(const Level &L, const R *r, const float *scale, const V *zin, V *zout, int nb, double c1,
+                        double c2, double *partial, int gx, cudaStream_t s) {
+  const dim3 g = DOT ? RED_GRID(L.dims.N, (k_cheb_step<T, V, R, KB, DOT, PREV>), (Lanes<V, KB>::LPN))
+                     : GRID_K(L.dims.N, (k_cheb_step<T, V, R, KB, DOT, PREV>));
+  k_cheb_step<T, V, R, KB, DOT, PREV><<<g, TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, scale, zin, zout, L.dims,
+                                                        nb, (T)c1, (T)c2, partial, gx);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb, double c1,
+                              double c2, double *partial, int gx, cudaStream_t s) {
+  if (r.full) {
+    const T *rp = r.full;
+    const float *sc = r.scale;
+    if (partial) {
+      if (prev == 1) cheb_launch<T, V, KB, T, true, 1>(L, rp, sc, zin, zout, nb, c1, c2, partial, gx, s);
+      else if (prev == 2) cheb_launch<T, V, KB, T, true, 2>(L, rp, sc, zin, zout, nb, c1, c2, partial, gx, s);
+      else cheb_launch<T, V, KB, T, true, 0>(L, rp, sc, zin, zout, nb, c1, c2, partial, gx, s);
+    } else {
+      if (prev == 1) cheb_launch<T, V, KB, T, false, 1>(L, rp, sc, zin, zout, nb, c1, c2, nullptr, gx, s);
+      else if (prev == 2) cheb_launch<T, V, KB, T, false, 2>(L, rp, sc, zin, zout, nb, c1, c2, nullptr, gx, s);
+      else cheb_launch<T, V, KB, T, false, 0>(L, rp, sc, zin, zout, nb, c1, c2, nullptr, gx, s);
+    }
+  } else {
+    const V *rp = r.part;
+    if (partial) {
+      if (prev == 1) cheb_launch<T, V, KB, V, true, 1>(L, rp, nullptr, zin, zout, nb, c1, c2, partial, gx, s);
+      else if (prev == 2) cheb_launch<T, V, KB, V, true, 2>(L, rp, nullptr, zin, zout, nb, c1, c2, partial, gx, s);
+      else cheb_launch<T, V, KB, V, true, 0>(L, rp, nullptr, zin, zout, nb, c1, c2, partial, gx, s);
+    } else {
+      if (prev == 1) cheb_launch<T, V, KB, V, false, 1>(L, rp, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s);
+      else if (prev == 2) cheb_launch<T, V, KB, V, false, 2>(L, rp, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s);
+      else cheb_launch<T, V, KB, V, false, 0>(L, rp, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s);
+    }
+  }
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::restrict_(const Level &f, const Level &c, const V *res, V *rc, int nb, cudaStream_t s) {
+  k_restrict<T, V, KB><<<GRID_K(c.dims.N, (k_restrict<T, V, KB>)), TPB, 0, s>>>(res, rc, f.dims, c.dims, nb,
+                                                                               make_tab<T>(f));
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::prolong_add(const Level &f, const Level &c, const V *zc, V *z, int nb, cudaStream_t s) {
+  k_prolong_add<T, V, KB><<<GRID_K(f.dims.N, (k_prolong_add<T, V, KB>)), TPB, 0, s>>>(zc, z, f.dims, c.dims, nb,
+                                                                                     make_tab<T>(f));
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V *zc, int nb, cudaStream_t s) {
+  if (rc.full)
+    k_coarse_solve<T, V, T, KB><<<GRID_K(c.dims.N, (k_coarse_solve<T, V, T, KB>)), TPB, 0, s>>>(
+        Ainv, c.dims, nb, rc.full, rc.scale, zc);
+  else
+    k_coarse_solve<T, V, V, KB><<<GRID_K(c.dims.N, (k_coarse_solve<T, V, V, KB>)), TPB, 0, s>>>(
+        Ainv, c.dims, nb, rc.part, nullptr, zc);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
+                              double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
+                              V *rv_out, cudaStream_t s) {
+  const Dims dd = flat_dims(N);
+  if (smooth)
+    k_update_xr<T, V, KB, true><<<RED_GRID(N, (k_update_xr<T, V, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+        dd, nb, x, r, p, q, alpha, partial, invd_ptr<T>(*smooth), z, (T)c0, scale, rv_out, gx);
+  else
+    k_update_xr<T, V, KB, false><<<RED_GRID(N, (k_update_xr<T, V, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+        dd, nb, x, r, p, q, alpha, partial, nullptr, nullptr, (T)0, nullptr, nullptr, gx);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::scale_to(long long N, int nb, const T *r, const float *scale, V *rv_out, cudaStream_t s) {
+  k_scale_to<T, V, KB><<<GRID_K(N, (k_scale_to<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, r, scale, rv_out);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s) {
+  k_dot<T, T, KB><<<RED_GRID(N, (k_dot<T, T, KB>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(flat_dims(N), nb, a, b,
+                                                                                     partial, gx);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::dot_z(long long N, int nb, const T *a, const V *b, double *partial, int gx, cudaStream_t s) {
+  k_dot<T, V, KB><<<RED_GRID(N, (k_dot<T, V, KB>), (Lanes<V, KB>::LPN)), TPB, 0, s>>>(flat_dims(N), nb, a, b,
+                                                                                     partial, gx);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::p_update(long long N, int nb, T *p, const V *z, const double *beta, cudaStream_t s) {
+  k_p_update<T, V, KB><<<GRID_K(N, (k_p_update<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z, beta);
+}
+
+template <typename T, typename V, int KB>
+void Ops<T, V, KB>::copy_z(long long N, int nb, T *dst, const V *src, cudaStream_t s) {
+  if (std::is_same<T, V>::value)
+    cudaMemcpyAsync(dst, src, sizeof(T) * N * KB * nb, cudaMemcpyDeviceToDevice, s);
+  else
+    k_copy_z<T, V, KB><<<GRID_K(N, (k_copy_z<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, dst, src);
+}
+
+#define DC_OPS_INSTANTIATE(T, V)                                                                            \
+  template struct Ops<T, V, 1>;                                                                             \
+  template struct Ops<T, V, 2>;                                                                             \
+  template struct Ops<T, V, 4>;                                                                             \
+  template struct Ops<T, V, 8>;                                                                             \
+  template struct Ops<T, V, 16>;                                                                            \
+  template struct Ops<T, V, 32>;
+
+}  // namespace dc

@@ -1,12 +1,7 @@
-// Stencil, multigrid-transfer, PCG-vector and reduction kernels of the nodal
-// DC engine.  Every kernel here is bandwidth-bound except the fp64 stencil,
-// which on this part is bounded by fp64 issue rate (see the design notes).
-//
-// Thread mapping of every "node" kernel: a thread owns W consecutive RHS lanes
-// (16 bytes) of one node, KB/W threads share a node, and a 1D grid sweeps the
-// flat (RHS block, node) index with the RHS block slowest.  Lane l of node n
-// in RHS block b is element (b*N + n)*KB + l, so a warp's loads are contiguous.
-#include "dc_internal.h"
+// Scalar, coefficient, coarsest-level, Neumann and layout kernels of the
+// nodal DC engine (the node kernels and their launchers are in
+// dc_kernels.cuh, instantiated by dc_ops_*.cu), plus the launch bookkeeping.
+#include "dc_kernels.cuh"
 
 #include <cstdio>
 #include <algorithm>
@@ -19,463 +14,8 @@ namespace dc {
 
 namespace {
 
-constexpr int TPB = 256;
-
-// floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
-__device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
-  if (d == 1) return n;
-  unsigned q = __umulhi((unsigned)n, m);
-  q -= (q * (unsigned)d > (unsigned)n) ? 1u : 0u;
-  return (int)q;
-}
-
-__device__ __forceinline__ void node_ijk(int n, const Dims &d, int &i, int &j, int &k) {
-  const int nxy = d.Nx * d.Ny;
-  k = fast_div(n, nxy, d.mxy);
-  const int r = n - k * nxy;
-  j = fast_div(r, d.Nx, d.mx);
-  i = r - j * d.Nx;
-}
-
-template <typename C> struct CoefT;
-template <> struct CoefT<double> { using type = Coef64; };
-template <> struct CoefT<float> { using type = Coef32; };
-
-// Vector width per thread: 16-byte accesses (4 fp32 / 2 fp64 RHS lanes of one node).
-template <typename T, int KB> struct VWidth {
-  static constexpr int v = (sizeof(T) == 4) ? (KB >= 4 ? 4 : KB) : (KB >= 2 ? 2 : 1);
-};
-
-template <typename T, int W> struct alignas(sizeof(T) * W) Vec {
-  T a[W];
-};
-
-template <typename T, int W>
-__device__ __forceinline__ Vec<T, W> ldv(const T *p) {
-  return *reinterpret_cast<const Vec<T, W> *>(p);
-}
-template <typename T, int W>
-__device__ __forceinline__ void stv(T *p, const Vec<T, W> &v) {
-  *reinterpret_cast<Vec<T, W> *>(p) = v;
-}
-
-// Per-thread geometry of the "node x lane-group" mapping.  LPN threads share
-// one node (each owning W consecutive RHS lanes of one RHS block).  Kernels
-// sweep the RHS blocks one after the other (RHS block = slowest index of the
-// flat work index), so the L2 working set of the stencil's z-neighbour planes
-// is that of one RHS block at a time.
-template <typename T, int KB> struct Map {
-  static constexpr int W = VWidth<T, KB>::v;
-  static constexpr int LPN = KB / W;  // threads per node
-};
-
-
-template <typename T, int KB>
-__device__ __forceinline__ const typename CoefT<T>::type *coef_of(const void *c) {
-  return reinterpret_cast<const typename CoefT<T>::type *>(c);
-}
-
-// (A x) for the W lanes at element t of node n = (i, j, k).
-template <typename T, int KB, int W>
-__device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *__restrict__ coef,
-                                                  const T *__restrict__ x, long long t, int n, int i, int j, int k,
-                                                  const Dims &d) {
-  const auto c = coef[n];
-  Vec<T, W> acc = ldv<T, W>(x + t);
-#pragma unroll
-  for (int e = 0; e < W; ++e) acc.a[e] *= c.d;
-  const long long sx = KB, sy = (long long)d.Nx * KB, sz = (long long)d.Nx * d.Ny * KB;
-  auto sub = [&](T w, long long off) {
-    const Vec<T, W> v = ldv<T, W>(x + t + off);
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc.a[e] -= w * v.a[e];
-  };
-  if (i + 1 < d.Nx) sub(c.cx, sx);
-  if (i > 0) sub(coef[n - 1].cx, -sx);
-  if (j + 1 < d.Ny) sub(c.cy, sy);
-  if (j > 0) sub(coef[n - d.Nx].cy, -sy);
-  if (k + 1 < d.Nz) sub(c.cz, sz);
-  if (k > 0) sub(coef[n - d.Nx * d.Ny].cz, -sz);
-  return acc;
-}
-
-// Sweep over (RHS block b, node n, lane group q) with b slowest.  Defines W,
-// LPN, q and, per iteration, ng (flat node index over all RHS blocks), b, n and
-// t (offset of the thread's W lanes).
-#define SWEEP(NN, MAGIC, NB)                                                                   \
-  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;                                      \
-  const int q = threadIdx.x % LPN;                                                             \
-  const long long total_ = (long long)(NN) * (NB) * LPN;                                       \
-  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total_; g += (long long)gridDim.x * TPB)
-
-#define SWEEP_INDEX(NN, MAGIC)                        \
-  const int ng = (int)(g / LPN);                      \
-  const int b = fast_div(ng, (int)(NN), (MAGIC));     \
-  const int n = ng - b * (int)(NN);                   \
-  const long long t = (long long)ng * KB + q * W;     \
-  (void)b;                                            \
-  (void)n;
-
-// Reductions (per-RHS dot products) are bitwise reproducible: every thread
-// sums its own elements in sweep order, threads of one lane group are
-// combined by warp shuffles, and the warps' sums in warp order -- no
-// floating-point atomics, so a solve repeated on the same data (or recorded in
-// a CUDA graph) takes the same iterations and returns the same bits.
-// Block partials land in partial[(b * gridDim.x + blockIdx.x) * KB + lane].
-template <typename T, int KB>
-__device__ __forceinline__ void block_reduce(T (&acc)[Map<T, KB>::W], T *red, int b, double *partial) {
-  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
-#pragma unroll
-  for (int o = 16; o >= LPN; o >>= 1)
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane < LPN)
-#pragma unroll
-    for (int e = 0; e < W; ++e) red[warp * KB + lane * W + e] = acc[e];
-  __syncthreads();
-  if (threadIdx.x < KB) {
-    T v = (T)0;
-#pragma unroll
-    for (int w = 0; w < TPB / 32; ++w) v += red[w * KB + threadIdx.x];
-    partial[((long long)b * gridDim.x + blockIdx.x) * KB + threadIdx.x] = (double)v;
-  }
-  __syncthreads();
-}
-
-// Sweep of a reducing kernel: the RHS blocks one after the other (the whole
-// grid on one RHS block at a time, as in the flat sweep), each closed by the
-// block reduction of that RHS block's per-thread sums.
-// body(b, n, q, t, acc): RHS block, node, lane group, element offset, sums.
-template <typename T, int KB, typename Body>
-__device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, Body body) {
-  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
-  __shared__ T red[(TPB / 32) * KB];
-  const int q = threadIdx.x % LPN;
-  const long long per = (long long)N * LPN;
-  for (int b = 0; b < nb; ++b) {
-    T acc[W];
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] = (T)0;
-    const long long base = (long long)b * N;
-    for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < per; g += (long long)gridDim.x * TPB) {
-      const int n = (int)(g / LPN);
-      body(b, n, q, (base + n) * KB + q * W, acc);
-    }
-    block_reduce<T, KB>(acc, red, b, partial);
-  }
-}
-
-// The same body over the flat (RHS block, node, lane group) sweep, no reduction.
-template <typename T, int KB, typename Body>
-__device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body) {
-  constexpr int W = Map<T, KB>::W, LPN = Map<T, KB>::LPN;
-  const int q = threadIdx.x % LPN;
-  const long long total = (long long)N * nb * LPN;
-  T acc[W];
-  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total; g += (long long)gridDim.x * TPB) {
-    const int ng = (int)(g / LPN);
-    const int b = fast_div(ng, N, mn);
-    body(b, ng - b * N, q, (long long)ng * KB + q * W, acc);
-  }
-}
-
-// ---------------------------------------------------------------- stencil ops
-template <typename T, int KB, bool DOT>
-__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
-                                               T *__restrict__ y, Dims d, int nb, double *__restrict__ partial) {
-  constexpr int W = Map<T, KB>::W;
-  const auto *coef = coef_of<T, KB>(cf);
-  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
-    int i, j, k;
-    node_ijk(n, d, i, j, k);
-    const Vec<T, W> v = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
-    stv<T, W>(y + t, v);
-    if (DOT) {
-      const Vec<T, W> xv = ldv<T, W>(x + t);
-#pragma unroll
-      for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
-    }
-  };
-  if (DOT)
-    sweep_reduce<T, KB>(d.N, nb, partial, body);
-  else
-    sweep_flat<T, KB>(d.N, d.mn, nb, body);
-}
-
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, const T *__restrict__ r,
-                                                  const T *__restrict__ z, T *__restrict__ res, Dims d, int nb) {
-  const auto *coef = coef_of<T, KB>(cf);
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
-    int i, j, k;
-    node_ijk(n, d, i, j, k);
-    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, z, t, n, i, j, k, d);
-    Vec<T, W> rv = ldv<T, W>(r + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) rv.a[e] -= az.a[e];
-    stv<T, W>(res + t, rv);
-  }
-}
-
-// First Chebyshev step from z = 0: z = c0 * D^-1 r.
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, const T *__restrict__ r,
-                                                    T *__restrict__ z, Dims d, int nb, T c0) {
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
-    const T s = c0 * invd[n];
-    Vec<T, W> v = ldv<T, W>(r + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) v.a[e] *= s;
-    stv<T, W>(z + t, v);
-  }
-}
-
-// Chebyshev step in three-term form (x_{k+1} = x_k + c1 (x_k - x_{k-1}) + c2 D^-1 (r - A x_k)):
-//   PREV = 0: no momentum term (first step from a nonzero start, c1 = 0)
-//   PREV = 1: x_{k-1} read from zout (overwritten in place with x_{k+1})
-//   PREV = 2: x_{k-1} = 0 (second step of a zero-start sequence)
-// Four streams per RHS lane (x_k, r, x_{k-1} read; x_{k+1} write) instead of the
-// five of the d-vector form.  With DOT, also per-block partials of r . x_{k+1}.
-template <typename T, int KB, bool DOT, int PREV>
-__global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
-                                                   const T *__restrict__ r, const T *__restrict__ zin,
-                                                   T *zout, Dims d, int nb, T c1, T c2,
-                                                   double *__restrict__ partial) {
-  constexpr int W = Map<T, KB>::W;
-  const auto *coef = coef_of<T, KB>(cf);
-  auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
-    int i, j, k;
-    node_ijk(n, d, i, j, k);
-    const Vec<T, W> az = stencil_vec<T, KB, W>(coef, zin, t, n, i, j, k, d);
-    const Vec<T, W> rv = ldv<T, W>(r + t);
-    const Vec<T, W> zc = ldv<T, W>(zin + t);
-    Vec<T, W> zo;
-    if (PREV == 1) zo = ldv<T, W>(zout + t);
-    const T s = c2 * invd[n];
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      T mom = (T)0;
-      if (PREV == 1) mom = c1 * (zc.a[e] - zo.a[e]);
-      if (PREV == 2) mom = c1 * zc.a[e];
-      zo.a[e] = zc.a[e] + mom + s * (rv.a[e] - az.a[e]);
-      if (DOT) acc[e] += rv.a[e] * zo.a[e];
-    }
-    stv<T, W>(zout + t, zo);
-  };
-  if (DOT)
-    sweep_reduce<T, KB>(d.N, nb, partial, body);
-  else
-    sweep_flat<T, KB>(d.N, d.mn, nb, body);
-}
-
-// ---------------------------------------------------------------- transfers
-struct XferTab {
-  const int *fi;        // coarse node -> fine node, per axis at roff[a]
-  const void *wl, *wr;  // T weights of fine fi-1 / fi+1
-  const int *pl;        // fine node -> left coarse node, per axis at poff[a]
-  const void *pw;       // T weight on pl
-  long long roff[3], poff[3];
-};
-
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_restrict(const T *__restrict__ res, T *__restrict__ rc, Dims f, Dims c,
-                                                  int nb, XferTab tb) {
-  const T *wl = (const T *)tb.wl, *wr = (const T *)tb.wr;
-  SWEEP(c.N, c.mn, nb) {
-    SWEEP_INDEX(c.N, c.mn)
-    int I, J, K;
-    node_ijk(n, c, I, J, K);
-    const int fx = tb.fi[tb.roff[0] + I], fy = tb.fi[tb.roff[1] + J], fz = tb.fi[tb.roff[2] + K];
-    const T wx[3] = {wl[tb.roff[0] + I], (T)1, wr[tb.roff[0] + I]};
-    const T wy[3] = {wl[tb.roff[1] + J], (T)1, wr[tb.roff[1] + J]};
-    const T wz[3] = {wl[tb.roff[2] + K], (T)1, wr[tb.roff[2] + K]};
-    const long long fb = (long long)b * f.N * KB + q * W;
-    Vec<T, W> acc;
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc.a[e] = 0;
-#pragma unroll
-    for (int cz = 0; cz < 3; ++cz) {
-      if (wz[cz] == (T)0) continue;
-#pragma unroll
-      for (int cy = 0; cy < 3; ++cy) {
-        if (wy[cy] == (T)0) continue;
-        const T wyz = wy[cy] * wz[cz];
-        const long long row = ((long long)(fz + cz - 1) * f.Ny + (fy + cy - 1)) * f.Nx;
-#pragma unroll
-        for (int cx = 0; cx < 3; ++cx) {
-          if (wx[cx] == (T)0) continue;
-          const T w = wx[cx] * wyz;
-          const Vec<T, W> v = ldv<T, W>(res + fb + (row + fx + cx - 1) * KB);
-#pragma unroll
-          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
-        }
-      }
-    }
-    stv<T, W>(rc + t, acc);
-  }
-}
-
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_prolong_add(const T *__restrict__ zc, T *__restrict__ z, Dims f, Dims c,
-                                                     int nb, XferTab tb) {
-  const T *pw = (const T *)tb.pw;
-  SWEEP(f.N, f.mn, nb) {
-    SWEEP_INDEX(f.N, f.mn)
-    int i, j, k;
-    node_ijk(n, f, i, j, k);
-    const int I = tb.pl[tb.poff[0] + i], J = tb.pl[tb.poff[1] + j], K = tb.pl[tb.poff[2] + k];
-    const T ax = pw[tb.poff[0] + i], ay = pw[tb.poff[1] + j], az = pw[tb.poff[2] + k];
-    const T wx[2] = {ax, (T)1 - ax}, wy[2] = {ay, (T)1 - ay}, wz[2] = {az, (T)1 - az};
-    const long long cb = (long long)b * c.N * KB + q * W;
-    Vec<T, W> acc = ldv<T, W>(z + t);
-#pragma unroll
-    for (int bz = 0; bz < 2; ++bz) {
-      if (wz[bz] == (T)0) continue;
-#pragma unroll
-      for (int a = 0; a < 2; ++a) {
-        if (wy[a] == (T)0) continue;
-        const T wyz = wy[a] * wz[bz];
-        const long long row = ((long long)(K + bz) * c.Ny + (J + a)) * c.Nx;
-#pragma unroll
-        for (int e2 = 0; e2 < 2; ++e2) {
-          if (wx[e2] == (T)0) continue;
-          const T w = wx[e2] * wyz;
-          const Vec<T, W> v = ldv<T, W>(zc + cb + (row + I + e2) * KB);
-#pragma unroll
-          for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
-        }
-      }
-    }
-    stv<T, W>(z + t, acc);
-  }
-}
-
-// z_c = Ainv r_c on the coarsest level (dense, row-major Ainv[nc][nc]).
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv, Dims c, int nb,
-                                                      const T *__restrict__ rc, T *__restrict__ zc) {
-  const int nc = (int)c.N;
-  SWEEP(c.N, c.mn, nb) {
-    SWEEP_INDEX(c.N, c.mn)
-    const T *row = Ainv + (long long)n * nc;
-    const long long base = (long long)b * nc * KB + q * W;
-    Vec<T, W> acc;
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc.a[e] = 0;
-    for (int m = 0; m < nc; ++m) {
-      const T w = row[m];
-      const Vec<T, W> v = ldv<T, W>(rc + base + (long long)m * KB);
-#pragma unroll
-      for (int e = 0; e < W; ++e) acc.a[e] += w * v.a[e];
-    }
-    stv<T, W>(zc + t, acc);
-  }
-}
-
-// ---------------------------------------------------------------- PCG vectors
-// x += a p ; r -= a q ; partial |r|^2 (a per RHS).  With SMOOTH, also the first
-// Chebyshev step of the fine level on the new residual: z = d = c0 D^-1 r.
-template <typename T, int KB, bool SMOOTH>
-__global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict__ x, T *__restrict__ r,
-                                                   const T *__restrict__ p, const T *__restrict__ qv,
-                                                   const double *__restrict__ alpha, double *__restrict__ partial,
-                                                   const T *__restrict__ invd, T *__restrict__ z, T c0) {
-  constexpr int W = Map<T, KB>::W;
-  sweep_reduce<T, KB>(d.N, nb, partial, [&](int b, int n, int q, long long t, T(&acc)[W]) {
-    Vec<T, W> xv = ldv<T, W>(x + t), rv = ldv<T, W>(r + t);
-    const Vec<T, W> pv = ldv<T, W>(p + t), qq = ldv<T, W>(qv + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      const T a = (T)alpha[b * KB + q * W + e];
-      xv.a[e] += a * pv.a[e];
-      rv.a[e] -= a * qq.a[e];
-      acc[e] += rv.a[e] * rv.a[e];
-    }
-    stv<T, W>(x + t, xv);
-    stv<T, W>(r + t, rv);
-    if (SMOOTH) {
-      const T s = c0 * invd[n];
-#pragma unroll
-      for (int e = 0; e < W; ++e) rv.a[e] *= s;
-      stv<T, W>(z + t, rv);
-    }
-  });
-}
-
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict__ a, const T *__restrict__ bb,
-                                             double *__restrict__ partial) {
-  constexpr int W = Map<T, KB>::W;
-  sweep_reduce<T, KB>(d.N, nb, partial, [&](int, int, int, long long t, T(&acc)[W]) {
-    const Vec<T, W> av = ldv<T, W>(a + t), bv = ldv<T, W>(bb + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) acc[e] += av.a[e] * bv.a[e];
-  });
-}
-
-// p = z + beta p
-template <typename T, int KB>
-__global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, T *__restrict__ p, const T *__restrict__ z,
-                                                  const double *__restrict__ beta) {
-  SWEEP(d.N, d.mn, nb) {
-    SWEEP_INDEX(d.N, d.mn)
-    Vec<T, W> pv = ldv<T, W>(p + t);
-    const Vec<T, W> zv = ldv<T, W>(z + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + (T)beta[b * KB + q * W + e] * pv.a[e];
-    stv<T, W>(p + t, pv);
-  }
-}
-
-// ---------------------------------------------------------------- refinement
-template <int KB>
-__global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ coef, const double *__restrict__ bvec,
-                                                     const double *__restrict__ x, double *__restrict__ r64,
-                                                     float *__restrict__ r32, Dims d, int nb,
-                                                     const int *__restrict__ active, double *__restrict__ partial) {
-  using T = double;
-  constexpr int W = Map<T, KB>::W;
-  sweep_reduce<T, KB>(d.N, nb, partial, [&](int b, int n, int q, long long t, T(&acc)[W]) {
-    int i, j, k;
-    node_ijk(n, d, i, j, k);
-    const Vec<T, W> ax = stencil_vec<T, KB, W>(coef, x, t, n, i, j, k, d);
-    Vec<T, W> rv = ldv<T, W>(bvec + t);
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      rv.a[e] -= ax.a[e];
-      acc[e] += rv.a[e] * rv.a[e];
-      r32[t + e] = active[b * KB + q * W + e] ? (float)rv.a[e] : 0.0f;
-    }
-    stv<T, W>(r64 + t, rv);
-  });
-}
-
-__global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total4, double *__restrict__ x64,
-                                                       const float *__restrict__ d32) {
-  // total4 = number of 4-element groups (the blocked arrays are padded to KB >= 1 lanes; tail handled by caller)
-  for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < total4; t += (long long)gridDim.x * TPB) {
-    const float4 dv = reinterpret_cast<const float4 *>(d32)[t];
-    double2 a = reinterpret_cast<double2 *>(x64)[2 * t], b = reinterpret_cast<double2 *>(x64)[2 * t + 1];
-    a.x += dv.x;
-    a.y += dv.y;
-    b.x += dv.z;
-    b.y += dv.w;
-    reinterpret_cast<double2 *>(x64)[2 * t] = a;
-    reinterpret_cast<double2 *>(x64)[2 * t + 1] = b;
-  }
-}
-
 __global__ void k_fill_int(int *__restrict__ a, int n, int v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
-}
-
-__global__ void k_ir_accumulate_tail(long long start, long long total, double *__restrict__ x64,
-                                     const float *__restrict__ d32) {
-  for (long long t = start + (long long)blockIdx.x * TPB + threadIdx.x; t < total; t += (long long)gridDim.x * TPB)
-    x64[t] += (double)d32[t];
 }
 
 // ---------------------------------------------------------------- PCG scalars
@@ -500,6 +40,14 @@ __device__ __forceinline__ double block_sum_partial(const double *p, int gx, int
     for (int w = 0; w < SCAL_T / 32; ++w) t += red[w];
   __syncthreads();
   return t;  // valid in thread 0
+}
+
+// Per-RHS scale of the multigrid input: 1/|r|_2 (1 for a zero or non-finite
+// norm), so that the V-cycle's vectors stay O(1) whatever the residual's size.
+// PCG is invariant under a per-iteration positive scaling of the
+// preconditioner (alpha and beta absorb it), so this only affects rounding.
+__device__ __forceinline__ float rss(double rr) {
+  return (rr > 0.0 && isfinite(rr)) ? (float)(1.0 / sqrt(rr)) : 1.0f;
 }
 
 __global__ void __launch_bounds__(SCAL_T) k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
@@ -528,12 +76,14 @@ __global__ void __launch_bounds__(SCAL_T) k_pcg_beta(int K, int KB, int gx, cons
                                                      double *__restrict__ rr_out, const double *__restrict__ bb,
                                                      const double *__restrict__ tol2, int *__restrict__ active,
                                                      double *__restrict__ beta, int *__restrict__ n_active,
-                                                     int first) {
+                                                     int first, const float *rz_div, float *scale) {
   const int r = blockIdx.x;
-  const double rzn = block_sum_partial(part_rz, gx, KB, r);
+  double rzn = block_sum_partial(part_rz, gx, KB, r);
   const double rr = block_sum_partial(part_rr, gx, KB, r);
   if (threadIdx.x == 0) {
+    if (rz_div) rzn /= (double)rz_div[r];  // read before scale (possibly the same array) is renewed
     rr_out[r] = rr;
+    if (scale) scale[r] = rss(rr);
     int act = active[r];
     if (act && !(rr > tol2[r] * bb[r])) act = 0;
     if (act && !isfinite(rr)) act = 0;
@@ -548,9 +98,12 @@ __global__ void __launch_bounds__(SCAL_T) k_pcg_beta(int K, int KB, int gx, cons
 
 // per-RHS sums of partials into out (used for |b|^2 and the outer residual norms)
 __global__ void __launch_bounds__(SCAL_T) k_sum_partials(int K, int KB, int gx, const double *__restrict__ part,
-                                                         double *__restrict__ out) {
+                                                         double *__restrict__ out, float *__restrict__ scale) {
   const double v = block_sum_partial(part, gx, KB, blockIdx.x);
-  if (threadIdx.x == 0) out[blockIdx.x] = v;
+  if (threadIdx.x == 0) {
+    out[blockIdx.x] = v;
+    if (scale) scale[blockIdx.x] = rss(v);
+  }
 }
 
 // Outer (refinement) convergence: active = rr > rtol2*bb ; counts ; max relative residual.
@@ -893,54 +446,58 @@ __global__ void k_convert_d2f(const double *__restrict__ a, long long n, float *
 }
 
 // ---------------------------------------------------------------- layout conversion
+// Column-major (K, N) <-> RHS-blocked [nb][N][KB] transposes through a
+// 32 x 32 shared-memory tile (rows = RHS, columns = nodes), so that both the
+// column-major side (contiguous in n) and the blocked side (contiguous in the
+// RHS lane) are accessed in full lines.  Lanes r >= K of the blocked array are
+// zero-filled by k_pack.
+constexpr int TT = 32;  // tile edge
+constexpr int TR = 8;   // tile rows per pass (blockDim = TT x TR)
+
 template <typename T>
-__global__ void k_pack(const double *__restrict__ src, long long N, int K, int KB, T *__restrict__ dst,
-                       long long total) {
-  // dst element t -> (b, n, l); rhs r = b*KB + l; src[r*N + n]
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-    const int l = (int)(t % KB);
-    const long long bn = t / KB;
-    const long long n = bn % N;
-    const int r = (int)(bn / N) * KB + l;
-    dst[t] = (r < K) ? (T)src[(long long)r * N + n] : (T)0;
+__global__ void __launch_bounds__(TT *TR) k_pack(const double *__restrict__ src, long long N, int K, int KB, int Kp,
+                                                  T *__restrict__ dst) {
+  __shared__ T tile[TT][TT + 1];
+  const long long n0 = (long long)blockIdx.x * TT;
+  const int r0 = blockIdx.y * TT;
+  for (int i = threadIdx.y; i < TT; i += TR) {
+    const int r = r0 + i;
+    const long long n = n0 + threadIdx.x;
+    tile[i][threadIdx.x] = (r < K && n < N) ? (T)src[(long long)r * N + n] : (T)0;
+  }
+  __syncthreads();
+  const int r = r0 + threadIdx.x;
+  if (r >= Kp) return;
+  const int b = r / KB, l = r % KB;
+  for (int j = threadIdx.y; j < TT; j += TR) {
+    const long long n = n0 + j;
+    if (n < N) dst[((long long)b * N + n) * KB + l] = tile[threadIdx.x][j];
   }
 }
 
 template <typename T>
-__global__ void k_unpack(const T *__restrict__ src, long long N, int K, int KB, double *__restrict__ dst) {
-  const long long total = N * K;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(e / N);
-    const long long n = e - (long long)r * N;
-    dst[e] = (double)src[((long long)(r / KB) * N + n) * KB + (r % KB)];
+__global__ void __launch_bounds__(TT *TR) k_unpack(const T *__restrict__ src, long long N, int K, int KB,
+                                                    double *__restrict__ dst) {
+  __shared__ double tile[TT][TT + 1];
+  const long long n0 = (long long)blockIdx.x * TT;
+  const int r0 = blockIdx.y * TT;
+  {
+    const int r = r0 + threadIdx.x;
+    const int b = r / KB, l = r % KB;
+    for (int j = threadIdx.y; j < TT; j += TR) {
+      const long long n = n0 + j;
+      if (r < K && n < N) tile[threadIdx.x][j] = (double)src[((long long)b * N + n) * KB + l];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < TT; i += TR) {
+    const int r = r0 + i;
+    const long long n = n0 + threadIdx.x;
+    if (r < K && n < N) dst[(long long)r * N + n] = tile[i][threadIdx.x];
   }
 }
 
-inline int grid_nodes(long long nodes, int LPN, int nb, int n_sm, int per_sm = 8) {
-  long long g = (nodes * (nb > 0 ? nb : 1) * LPN + TPB - 1) / TPB;
-  const long long cap = (long long)n_sm * per_sm;
-  if (g > cap) g = cap;
-  if (g < 1) g = 1;
-  return (int)g;
-}
-
-inline int grid_flat(long long total, int n_sm) {
-  long long g = (total + TPB - 1) / TPB;
-  long long cap = (long long)n_sm * 16;
-  if (g > cap) g = cap;
-  if (g < 1) g = 1;
-  return (int)g;
-}
-
-inline Dims flat_dims(long long N) {
-  Dims d{};
-  d.Nx = 1;
-  d.Ny = 1;
-  d.Nz = (int)N;
-  d.N = N;
-  d.mn = div_magic((unsigned)N);
-  return d;
-}
+}  // namespace
 
 // Resident blocks per SM of a kernel (cached).  Grids are capped at what the
 // GPU holds at once: a grid-stride sweep whose blocks do not all fit would be
@@ -958,7 +515,6 @@ int resident_blocks(const void *func) {
   return n;
 }
 
-}  // namespace
 
 int g_n_sm = 152;
 std::atomic<long long> &launch_counter() {
@@ -972,146 +528,6 @@ int node_grid(long long nodes, int KB, int nb, int per_sm) {
   return grid_nodes(nodes, KB / W, nb, g_n_sm, per_sm);
 }
 
-// ------------------------------------------------------------------ launchers
-template <typename T>
-static const void *coef_ptr(const Level &L) {
-  return std::is_same<T, double>::value ? (const void *)L.d_coef64 : (const void *)L.d_coef32;
-}
-template <typename T>
-static const T *invd_ptr(const Level &L) {
-  return reinterpret_cast<const T *>(std::is_same<T, double>::value ? (const void *)L.d_invd64
-                                                                    : (const void *)L.d_invd32);
-}
-
-#define GRID_K(NODES, KERNEL) \
-  count_launch(dim3(grid_nodes((NODES), Map<T, KB>::LPN, nb, g_n_sm, resident_blocks((const void *)(KERNEL)))))
-
-template <typename T, int KB>
-void Ops<T, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
-  if (partial)
-    k_apply<T, KB, true><<<count_launch(dim3(gx)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nb, partial);
-  else
-    k_apply<T, KB, false><<<GRID_K(L.dims.N, (k_apply<T, KB, false>)), TPB, 0, s>>>(coef_ptr<T>(L), x, y, L.dims, nb, nullptr);
-}
-
-template <typename T, int KB>
-int Ops<T, KB>::red_blocks_per_sm() {
-  int m = resident_blocks((const void *)k_apply<T, KB, true>);
-  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 0>));
-  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 1>));
-  m = std::min(m, resident_blocks((const void *)k_cheb_step<T, KB, true, 2>));
-  m = std::min(m, resident_blocks((const void *)k_update_xr<T, KB, true>));
-  m = std::min(m, resident_blocks((const void *)k_update_xr<T, KB, false>));
-  m = std::min(m, resident_blocks((const void *)k_dot<T, KB>));
-  if (std::is_same<T, double>::value) m = std::min(m, resident_blocks((const void *)k_ir_residual<KB>));
-  return m;
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::residual(const Level &L, const T *r, const T *z, T *res, int nb, cudaStream_t s) {
-  k_residual<T, KB><<<GRID_K(L.dims.N, (k_residual<T, KB>)), TPB, 0, s>>>(coef_ptr<T>(L), r, z, res, L.dims, nb);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::cheb_first(const Level &L, const T *r, T *z, int nb, double c0, cudaStream_t s) {
-  k_cheb_first<T, KB><<<GRID_K(L.dims.N, (k_cheb_first<T, KB>)), TPB, 0, s>>>(invd_ptr<T>(L), r, z, L.dims, nb, (T)c0);
-}
-
-template <typename T, int KB>
-template <bool DOT, int PREV>
-void Ops<T, KB>::cheb_launch(const Level &L, const T *r, const T *zin, T *zout, int nb, double c1, double c2,
-                             double *partial, int gx, cudaStream_t s) {
-  const dim3 g = DOT ? count_launch(dim3(gx)) : GRID_K(L.dims.N, (k_cheb_step<T, KB, DOT, PREV>));
-  k_cheb_step<T, KB, DOT, PREV><<<g, TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, zin, zout, L.dims, nb, (T)c1,
-                                                  (T)c2, partial);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::cheb_step(const Level &L, const T *r, const T *zin, T *zout, int prev, int nb, double c1, double c2,
-                           double *partial, int gx, cudaStream_t s) {
-  if (partial) {
-    if (prev == 1) cheb_launch<true, 1>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
-    else if (prev == 2) cheb_launch<true, 2>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
-    else cheb_launch<true, 0>(L, r, zin, zout, nb, c1, c2, partial, gx, s);
-  } else {
-    if (prev == 1) cheb_launch<false, 1>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
-    else if (prev == 2) cheb_launch<false, 2>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
-    else cheb_launch<false, 0>(L, r, zin, zout, nb, c1, c2, nullptr, gx, s);
-  }
-}
-
-template <typename T>
-static XferTab make_tab(const Level &f) {
-  XferTab tb;
-  const bool dbl = std::is_same<T, double>::value;
-  tb.fi = f.d_r_fi;
-  tb.wl = dbl ? (const void *)f.d_r_wl : (const void *)f.d_r_wl32;
-  tb.wr = dbl ? (const void *)f.d_r_wr : (const void *)f.d_r_wr32;
-  tb.pl = f.d_pl_idx;
-  tb.pw = dbl ? (const void *)f.d_pl_w : (const void *)f.d_pl_w32;
-  for (int a = 0; a < 3; ++a) {
-    tb.roff[a] = f.r_off[a];
-    tb.poff[a] = f.pl_off[a];
-  }
-  return tb;
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::restrict_(const Level &f, const Level &c, const T *res, T *rc, int nb, cudaStream_t s) {
-  k_restrict<T, KB><<<GRID_K(c.dims.N, (k_restrict<T, KB>)), TPB, 0, s>>>(res, rc, f.dims, c.dims, nb, make_tab<T>(f));
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::prolong_add(const Level &f, const Level &c, const T *zc, T *z, int nb, cudaStream_t s) {
-  k_prolong_add<T, KB><<<GRID_K(f.dims.N, (k_prolong_add<T, KB>)), TPB, 0, s>>>(zc, z, f.dims, c.dims, nb, make_tab<T>(f));
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::coarse_solve(const T *Ainv, const Level &c, const T *rc, T *zc, int nb, cudaStream_t s) {
-  k_coarse_solve<T, KB><<<GRID_K(c.dims.N, (k_coarse_solve<T, KB>)), TPB, 0, s>>>(Ainv, c.dims, nb, rc, zc);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
-                           double *partial, int gx, const Level *smooth, double c0, T *z, cudaStream_t s) {
-  const Dims dd = flat_dims(N);
-  if (smooth)
-    k_update_xr<T, KB, true><<<count_launch(dim3(gx)), TPB, 0, s>>>(dd, nb, x, r, p, q, alpha, partial,
-                                                                     invd_ptr<T>(*smooth), z, (T)c0);
-  else
-    k_update_xr<T, KB, false><<<count_launch(dim3(gx)), TPB, 0, s>>>(dd, nb, x, r, p, q, alpha, partial, nullptr,
-                                                                      nullptr, (T)0);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s) {
-  k_dot<T, KB><<<count_launch(dim3(gx)), TPB, 0, s>>>(flat_dims(N), nb, a, b, partial);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::p_update(long long N, int nb, T *p, const T *z, const double *beta, cudaStream_t s) {
-  k_p_update<T, KB><<<GRID_K(N, (k_p_update<T, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z, beta);
-}
-
-template <typename T, int KB>
-void Ops<T, KB>::copy(long long N, int nb, T *dst, const T *src, cudaStream_t s) {
-  cudaMemcpyAsync(dst, src, sizeof(T) * N * KB * nb, cudaMemcpyDeviceToDevice, s);
-}
-
-template <int KB>
-void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
-                 const int *active, double *partial, int gx, cudaStream_t s) {
-  k_ir_residual<KB><<<count_launch(dim3(gx)), TPB, 0, s>>>(L.d_coef64, b, x, r64, r32, L.dims, nb, active, partial);
-}
-
-template <int KB>
-void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s) {
-  const long long total = N * KB * nb;
-  const long long t4 = total / 4;
-  if (t4 > 0) k_ir_accumulate<<<count_launch(grid_flat(t4, g_n_sm)), TPB, 0, s>>>(t4, x64, d32);
-  if (t4 * 4 < total) k_ir_accumulate_tail<<<count_launch(1), TPB, 0, s>>>(t4 * 4, total, x64, d32);
-}
-
 void fill_int(int *a, int n, int v, cudaStream_t s) {
   if (n > 0) k_fill_int<<<count_launch((n + TPB - 1) / TPB), TPB, 0, s>>>(a, n, v);
 }
@@ -1123,13 +539,13 @@ void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, c
 
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
               const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
-              cudaStream_t s) {
+              cudaStream_t s, const float *rz_div, float *scale_out) {
   k_pcg_beta<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta,
-                                                      n_active, first);
+                                                      n_active, first, rz_div, scale_out);
 }
 
-void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s) {
-  k_sum_partials<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part, out);
+void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s, float *scale) {
+  k_sum_partials<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part, out, scale);
 }
 
 void outer_check(int K, const double *rr, const double *bb, double rtol2, int *active, int *n_active,
@@ -1196,25 +612,17 @@ void convert_d2f(const double *a, long long n, float *o, cudaStream_t s) {
 
 template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s) {
-  const long long total = N * (long long)KB * nb;
-  k_pack<T><<<count_launch(grid_flat(total, g_n_sm)), TPB, 0, s>>>(src, N, K, KB, dst, total);
+  const int Kp = KB * nb;
+  const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((Kp + TT - 1) / TT));
+  k_pack<T><<<count_launch(grid), dim3(TT, TR), 0, s>>>(src, N, K, KB, Kp, dst);
 }
 
 template <typename T>
 void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s) {
-  k_unpack<T><<<count_launch(grid_flat(N * K, g_n_sm)), TPB, 0, s>>>(src, N, K, KB, dst);
+  const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((K + TT - 1) / TT));
+  k_unpack<T><<<count_launch(grid), dim3(TT, TR), 0, s>>>(src, N, K, KB, dst);
 }
 
-#define DC_INST(T, KB) template struct Ops<T, KB>;
-DC_INST(float, 1) DC_INST(float, 2) DC_INST(float, 4) DC_INST(float, 8) DC_INST(float, 16) DC_INST(float, 32)
-DC_INST(double, 1) DC_INST(double, 2) DC_INST(double, 4) DC_INST(double, 8) DC_INST(double, 16) DC_INST(double, 32)
-#undef DC_INST
-#define DC_INST_IR(KB)                                                                                       \
-  template void ir_residual<KB>(const Level &, const double *, const double *, double *, float *, int,      \
-                                const int *, double *, int, cudaStream_t);                                  \
-  template void ir_accumulate<KB>(long long, int, double *, const float *, cudaStream_t);
-DC_INST_IR(1) DC_INST_IR(2) DC_INST_IR(4) DC_INST_IR(8) DC_INST_IR(16) DC_INST_IR(32)
-#undef DC_INST_IR
 template void pack_colmajor<float>(const double *, long long, int, int, int, float *, cudaStream_t);
 template void pack_colmajor<double>(const double *, long long, int, int, int, double *, cudaStream_t);
 template void unpack_colmajor<float>(const float *, long long, int, int, double *, cudaStream_t);

@@ -60,7 +60,8 @@ class DCEngine:
     bface : packed Robin face weights (``boundary.robin_face_weights``) or None (Neumann)
     """
 
-    def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1):
+    def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1,
+                 mg_storage=16, smoother=1):
         if not torch.cuda.is_available():
             raise RuntimeError("the DC engine needs a CUDA device")
         L = lib()
@@ -80,6 +81,8 @@ class DCEngine:
                           hz.ctypes.data_as(dp), bf.ctypes.data_as(dp) if bf is not None else None,
                           C.byref(self._h)))
         check(L.dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
+        check(L.dc_set_mg_storage(self._h, int(mg_storage)))
+        check(L.dc_set_smoother(self._h, int(smoother)))
         self.robin = bface is not None
         self._ws = {}
         self._model_set = False
@@ -104,6 +107,15 @@ class DCEngine:
         """Force the RHS-block width (1..32 lanes per node; 0 = automatic)."""
         check(lib().dc_set_rhs_block(self._h, int(kb)))
         self._ws.clear()
+
+    def set_mg_storage(self, bits):
+        """Multigrid vector storage of the mixed solve: 16 (fp16) or 32 bits."""
+        check(lib().dc_set_mg_storage(self._h, int(bits)))
+        self._ws.clear()
+
+    def set_smoother(self, kind):
+        """Chebyshev smoother of the first (1) or fourth (4) kind."""
+        check(lib().dc_set_smoother(self._h, int(kind)))
 
     def set_model(self, sigma):
         sigma = _dev64(sigma, (self.nC,), "sigma")
@@ -133,7 +145,7 @@ class DCEngine:
         check(lib().dc_solve_workspace_bytes(self._h, MODES[mode], int(k), C.byref(b)))
         return b.value
 
-    def solve(self, b, mode="mixed", rtol=1e-9, maxit=2000, inner_rtol=1e-4, inner_maxit=200, ws=None,
+    def solve(self, b, mode="mixed", rtol=1e-9, maxit=2000, inner_rtol=3e-5, inner_maxit=200, ws=None,
               raise_on_fail=True):
         """x = A^-1 b for b of shape (k, nN) or (nN,). Returns (x, SolveInfo)."""
         b = _dev64(b, None, "b")
