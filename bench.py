@@ -51,6 +51,8 @@ def _args():
     ap.add_argument("--workload", default="forward", choices=["forward", "differentiation", "gauss_newton", "batched"],
                     help="forward: the headline 1M-cell line; differentiation: the 96x96x48 gradient checks")
     ap.add_argument("--fd-directions", type=int, default=32)
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="set up the forward workload, run one mixed solve and exit (for ncu captures; no timing)")
     return ap.parse_args()
 
 
@@ -190,8 +192,9 @@ def run_reference(args):
 
 
 def _traffic_per_unit():
-    """DRAM bytes per (node x RHS) of the fine-level fp32 stencil step from the committed ncu summary."""
-    p = ROOT / "profiles" / "cheb_step_fp32_dc3d.md"
+    """DRAM bytes per (node x RHS) of the fine-level Chebyshev step (fp16 multigrid storage) from the
+    committed ncu summary."""
+    p = ROOT / "profiles" / "cheb_step_fp16_dc3d.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -353,7 +356,7 @@ def run_gb300(args):
                 "d2h_bytes_per_step": d2h,
                 "path": "Simulation3DNodal.dpred(m): host model -> exp -> H2D -> set_model -> solve -> gather -> D2H"},
         "roofline": {
-            "kernel": "k_cheb_step<float,32> (fine-level Chebyshev stencil step)",
+            "kernel": "k_cheb_step<float,__half,*,32> (fine-level Chebyshev stencil step, fp16 multigrid storage)",
             "bound": "hbm",
             "achieved": achieved,
             "peak": peak,
@@ -542,8 +545,29 @@ def run_batched(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile_solve(args):
+    """One mixed-precision solve of the forward workload (the first --sources
+    sources), nothing else: a short program for ncu to capture."""
+    import numpy as np
+    import torch
+
+    from simpeg_gb300 import maps
+    from simpeg_gb300.resistivity import Simulation3DNodal
+
+    torch.cuda.set_device(0)
+    mesh, sigma, survey = _workload(args.n_side, args.sources)
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+    sim.model = np.log(sigma)
+    sim._ensure_model()
+    _, info = sim.engine.solve(sim.getRHS(), mode="mixed", rtol=RTOL)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_solve": str(info), "sources": survey.nSrc}), flush=True)
+
+
 def main():
     args = _args()
+    if args.profile_solve:
+        return run_profile_solve(args)
     if args.workload == "batched" and args.impl != "reference":
         return run_batched(args)
     if args.workload == "gauss_newton" and args.impl != "reference":

@@ -70,12 +70,16 @@ int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int 
  * lanes).  Set by the autotuner. */
 int dc_set_rhs_block(dc_handle *h, int kb);
 
-/* Storage of the multigrid vectors inside the mixed-precision solve: 16
- * (fp16, default; the V-cycle input is scaled to unit norm per RHS and every
- * operation is done in fp32) or 32 bits.  The preconditioner only steers the
- * fp32 PCG, which the fp64 refinement corrects, so this changes iteration
- * counts, not the accuracy the solve reaches.  The fp64 solve keeps fp64. */
-int dc_set_mg_storage(dc_handle *h, int bits);
+/* Storage of the multigrid vectors inside the mixed-precision solve:
+ * DC_MG_FP16 (default), DC_MG_BF16 or DC_MG_FP32.  With 16-bit storage the
+ * V-cycle input is the PCG residual scaled to unit norm per RHS and every
+ * operation is done in fp32.  The preconditioner only steers the fp32 PCG,
+ * which the fp64 refinement corrects, so this changes iteration counts, not
+ * the accuracy the solve reaches.  The fp64 solve keeps fp64. */
+#define DC_MG_FP32 0
+#define DC_MG_FP16 1
+#define DC_MG_BF16 2
+int dc_set_mg_storage(dc_handle *h, int storage);
 
 /* Multigrid smoother: Chebyshev polynomial of D^-1 A of the first kind on
  * [lmax/cheb_ratio, lmax] (kind 1, default) or of the fourth kind on

@@ -23,6 +23,9 @@ DC_ERR_NOMEM = 5
 DC_ERR_STATE = 6
 DC_MODE_FP64 = 0
 DC_MODE_MIXED = 1
+DC_MG_FP32 = 0
+DC_MG_FP16 = 1
+DC_MG_BF16 = 2
 
 
 class DCError(RuntimeError):

@@ -4,6 +4,7 @@
 #include "../../include/dcgpu.h"
 #include "dc_internal.h"
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -222,7 +223,7 @@ struct dc_handle {
   double cheb_ratio = 30.0;
   int coarse_max = 200;
   int check_every = 1;
-  bool mg_half = true;  // mixed solve: fp16 multigrid vectors (dc_set_mg_storage)
+  int mg_storage = DC_MG_FP16;  // mixed solve: storage of the multigrid vectors (dc_set_mg_storage)
   int smoother_kind = 1;  // Chebyshev polynomials of the first or fourth kind (dc_set_smoother)
   int kb_force = 0;  // RHS-block width override (0: pick_kb)
   bool built = false;
@@ -431,8 +432,9 @@ struct SolveWS {
   double *p64, *q64, *z64;
   MGWork<float> mg32;
   MGWork<__half> mg16;
+  MGWork<__nv_bfloat16> mgb16;
   MGWork<double> mg64;
-  bool half;  // mixed solve with fp16 multigrid vectors
+  int storage;  // mixed solve: DC_MG_FP32 / DC_MG_FP16 / DC_MG_BF16 multigrid vectors
   Scal sc;
   size_t bytes;
 };
@@ -441,13 +443,15 @@ struct SolveWS {
 // this kind launches: gx, the stride of the partial arrays, covers every
 // reduction kernel's own resident-capped grid.
 template <int KB>
-int red_per_sm_kb(int mode, bool half) {
+int red_per_sm_kb(int mode, int storage) {
   if (mode == DC_MODE_FP64) return Ops<double, double, KB>::red_blocks_per_sm();
-  const int m = half ? Ops<float, __half, KB>::red_blocks_per_sm() : Ops<float, float, KB>::red_blocks_per_sm();
+  const int m = storage == DC_MG_FP16   ? Ops<float, __half, KB>::red_blocks_per_sm()
+                : storage == DC_MG_BF16 ? Ops<float, __nv_bfloat16, KB>::red_blocks_per_sm()
+                                        : Ops<float, float, KB>::red_blocks_per_sm();
   return std::max(m, ir_blocks_per_sm<KB>());
 }
 
-int red_per_sm(int KB, int mode, bool half) {
+int red_per_sm(int KB, int mode, int half) {
   switch (KB) {
     case 32: return red_per_sm_kb<32>(mode, half);
     case 16: return red_per_sm_kb<16>(mode, half);
@@ -468,7 +472,7 @@ void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
   w.nb = (k + w.KB - 1) / w.KB;
   w.Kp = w.nb * w.KB;
   const long long N = h->lv[0].dims.N;
-  w.gx = node_grid(N, w.KB, w.nb, red_per_sm(w.KB, mode, mode == DC_MODE_MIXED && h->mg_half));
+  w.gx = node_grid(N, w.KB, w.nb, red_per_sm(w.KB, mode, h->mg_storage));
   Carve c{base};
   const size_t n = (size_t)N * w.Kp;
   w.B64 = c.take<double>(n);
@@ -479,10 +483,13 @@ void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
     w.r32 = c.take<float>(n);
     w.p32 = c.take<float>(n);
     w.q32 = c.take<float>(n);
-    w.half = h->mg_half;
-    if (w.half) {
+    w.storage = h->mg_storage;
+    if (w.storage == DC_MG_FP16) {
       w.zv = c.take<__half>(n);
       carve_mg(c, h, w.Kp, w.mg16, true);
+    } else if (w.storage == DC_MG_BF16) {
+      w.zv = c.take<__nv_bfloat16>(n);
+      carve_mg(c, h, w.Kp, w.mgb16, true);
     } else {
       w.zv = c.take<float>(n);
       carve_mg(c, h, w.Kp, w.mg32);
@@ -792,12 +799,17 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     // one refinement sweep on stream so: inner fp32 PCG, accumulate, fp64 residual, new flags
     auto sweep = [&](cudaStream_t so, int inner_cap, int *it) -> int {
       CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
-      int rc = w.half ? pcg<float, __half, KB>(h, w.d32, w.r32, w.p32, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
-                                               w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
-                                               device ? 1 : 0)
-                      : pcg<float, float, KB>(h, w.d32, w.r32, w.p32, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
-                                              w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
-                                              device ? 1 : 0);
+      int rc;
+      if (w.storage == DC_MG_FP16)
+        rc = pcg<float, __half, KB>(h, w.d32, w.r32, w.p32, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
+                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
+      else if (w.storage == DC_MG_BF16)
+        rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, w.p32, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16, w.sc, nb,
+                                           gx, w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
+                                           device ? 1 : 0);
+      else
+        rc = pcg<float, float, KB>(h, w.d32, w.r32, w.p32, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
+                                   w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
       ir_accumulate<KB>(N, nb, w.X64, w.d32, so);
       ir_residual<KB>(F, w.B64, w.X64, nullptr, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, so);
@@ -977,10 +989,11 @@ int dc_set_rhs_block(dc_handle *h, int kb) {
   return 0;
 }
 
-int dc_set_mg_storage(dc_handle *h, int bits) {
+int dc_set_mg_storage(dc_handle *h, int storage) {
   if (!h) return fail(DC_ERR_ARG, "null handle");
-  if (bits != 16 && bits != 32) return fail(DC_ERR_ARG, "multigrid storage must be 16 or 32 bits");
-  h->mg_half = bits == 16;
+  if (storage != DC_MG_FP32 && storage != DC_MG_FP16 && storage != DC_MG_BF16)
+    return fail(DC_ERR_ARG, "multigrid storage must be DC_MG_FP32, DC_MG_FP16 or DC_MG_BF16");
+  h->mg_storage = storage;
   return 0;
 }
 

@@ -18,6 +18,7 @@
 // R is the type of a smoother's right-hand side: the PCG residual (T) on the
 // finest level, the restricted residual (V) below it.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>

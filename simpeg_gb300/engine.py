@@ -16,6 +16,7 @@ from . import _lib
 from ._lib import check, lib
 
 MODES = {"fp64": _lib.DC_MODE_FP64, "mixed": _lib.DC_MODE_MIXED}
+MG_STORAGE = {"fp32": _lib.DC_MG_FP32, "fp16": _lib.DC_MG_FP16, "bf16": _lib.DC_MG_BF16}
 
 
 def _stream():
@@ -61,7 +62,7 @@ class DCEngine:
     """
 
     def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1,
-                 mg_storage=16, smoother=1):
+                 mg_storage="fp16", smoother=1):
         if not torch.cuda.is_available():
             raise RuntimeError("the DC engine needs a CUDA device")
         L = lib()
@@ -81,7 +82,7 @@ class DCEngine:
                           hz.ctypes.data_as(dp), bf.ctypes.data_as(dp) if bf is not None else None,
                           C.byref(self._h)))
         check(L.dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
-        check(L.dc_set_mg_storage(self._h, int(mg_storage)))
+        check(L.dc_set_mg_storage(self._h, MG_STORAGE[mg_storage]))
         check(L.dc_set_smoother(self._h, int(smoother)))
         self.robin = bface is not None
         self._ws = {}
@@ -108,9 +109,9 @@ class DCEngine:
         check(lib().dc_set_rhs_block(self._h, int(kb)))
         self._ws.clear()
 
-    def set_mg_storage(self, bits):
-        """Multigrid vector storage of the mixed solve: 16 (fp16) or 32 bits."""
-        check(lib().dc_set_mg_storage(self._h, int(bits)))
+    def set_mg_storage(self, storage):
+        """Multigrid vector storage of the mixed solve: "fp16" (default), "bf16" or "fp32"."""
+        check(lib().dc_set_mg_storage(self._h, MG_STORAGE[storage]))
         self._ws.clear()
 
     def set_smoother(self, kind):

@@ -76,3 +76,26 @@ def test_solve_matches_direct(cuda, kind, mode, k):
     assert info.max_rel_res <= 1e-11
     err = np.linalg.norm(X - X0, axis=1) / np.linalg.norm(X0, axis=1)
     assert err.max() < 1e-8, (err.max(), info)
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("k", [3, 32, 40])
+def test_mixed_solve_every_multigrid_storage(cuda, storage, k):
+    """The multigrid storage type changes the preconditioner only: every
+    choice reaches the requested fp64 residual and the direct solution."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = _mesh("padded")
+    sigma = _sigma(mesh, seed=7)
+    A = _oracle(mesh, sigma).getA().tocsc()
+    eng = DCEngine(mesh.h, robin_face_weights(mesh), coarse_max=64, mg_storage=storage)
+    eng.set_model(torch.from_numpy(sigma).to(cuda))
+    rng = np.random.default_rng(3)
+    B = rng.standard_normal((k, mesh.n_nodes)) * 10.0 ** rng.uniform(-6, 3, (k, 1))  # RHS norms over 9 decades
+    X, info = eng.solve(torch.from_numpy(B).to(cuda), mode="mixed", rtol=1e-11)
+    X0 = spla.splu(A).solve(B.T).T
+    assert info.status == 0 and info.max_rel_res <= 1e-11
+    err = np.linalg.norm(X.cpu().numpy() - X0, axis=1) / np.linalg.norm(X0, axis=1)
+    assert err.max() < 1e-8, (storage, err.max(), info)
