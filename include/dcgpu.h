@@ -87,6 +87,16 @@ int dc_set_mg_storage(dc_handle *h, int storage);
  * D^-1 A; degrees nu_pre / nu_post (dc_set_params). */
 int dc_set_smoother(dc_handle *h, int kind);
 
+/* Finest-level smoothing of the mixed solve with 16-bit multigrid storage:
+ * 1 stages the iterate, residual and coefficients in shared memory with bulk
+ * asynchronous copies (slabs of node rows marched through the z planes),
+ * 0 (default) uses the direct-load kernel; a value 10 * rows + depth
+ * (12, 13, 22, 23) forces the slab height and copy depth.  Same arithmetic
+ * either way.  Measured on the 1M-node, 256-RHS solve: 182 ms staged (best
+ * layout) vs 164 ms direct, the per-plane CTA barrier of the slab march
+ * costing more than the latency it hides. */
+int dc_set_staging(dc_handle *h, int enable);
+
 /* Number of multigrid levels and nodes of level `lvl`. */
 int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3);
 

@@ -225,6 +225,8 @@ struct dc_handle {
   int check_every = 1;
   int mg_storage = DC_MG_FP16;  // mixed solve: storage of the multigrid vectors (dc_set_mg_storage)
   int smoother_kind = 1;  // Chebyshev polynomials of the first or fourth kind (dc_set_smoother)
+  bool bulk_staging = false;  // finest-level smoothing with bulk-copy staged shared-memory tiles (dc_set_staging)
+  int bulk_shape = 0;        // forced slab layout of the staged kernel (10 * rows + copy depth; 0 = automatic)
   int kb_force = 0;  // RHS-block width override (0: pick_kb)
   bool built = false;
   // cached internal workspace
@@ -370,6 +372,7 @@ template <typename T>
 struct MGWork {
   std::vector<T *> r, z, z2, res;
   T *r0 = nullptr;  // finest-level V-cycle input in the storage type (scaled PCG residual), when T differs
+  int *status = nullptr;  // PCG status word (copy timeouts of the staged kernels set bit 8)
 };
 
 struct Scal {
@@ -501,6 +504,7 @@ void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
     carve_mg(c, h, w.Kp, w.mg64);
   }
   carve_scal(c, w.Kp, w.gx, w.sc);
+  w.mg32.status = w.mg16.status = w.mgb16.status = w.mg64.status = w.sc.status;
   w.bytes = c.used + 256;
 }
 
@@ -516,11 +520,14 @@ const double *ainv<double>(const dc_handle *h) { return h->d_Ainv64; }
 // stencil timing is on (dc_stencil_timing).
 template <typename T, typename V, int KB>
 void timed_cheb(const dc_handle *hc, int l, const Level &F, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb,
-                double c1, double c2, double *partial, int gx, cudaStream_t s) {
+                double c1, double c2, double *partial, int gx, int *status, cudaStream_t s) {
   dc_handle *h = const_cast<dc_handle *>(hc);
   const bool rec = h->prof && l == 0 && sizeof(T) == 4 && h->prof_used + 2 <= (int)h->prof_ev.size();
   if (rec) cudaEventRecord(h->prof_ev[h->prof_used], s);
-  Ops<T, V, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s);
+  // finest level, 16-bit storage, no partials: x_k staged in shared memory by bulk copies
+  const bool staged = h->bulk_staging && l == 0 && !partial && r.part && sizeof(V) == 2 &&
+                      Ops<T, V, KB>::cheb_bulk(F, r.part, zin, zout, prev, nb, c1, c2, status, h->bulk_shape, s);
+  if (!staged) Ops<T, V, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s);
   if (rec) {
     cudaEventRecord(h->prof_ev[h->prof_used + 1], s);
     h->prof_used += 2;
@@ -566,7 +573,7 @@ void vcycle(const dc_handle *h, int l, Rhs<T, V> r, V *z, const MGWork<V> &w, in
   for (int it = 1; it < h->nu_pre; ++it) {
     V *out = other(cur);
     const SmoothStep &st = sm.pre[it];
-    timed_cheb<T, V, KB>(h, l, F, r, cur, out, st.prev, nb, st.c1, st.c2, nullptr, 0, s);
+    timed_cheb<T, V, KB>(h, l, F, r, cur, out, st.prev, nb, st.c1, st.c2, nullptr, 0, w.status, s);
     cur = out;
   }
   // coarse-grid correction
@@ -581,7 +588,8 @@ void vcycle(const dc_handle *h, int l, Rhs<T, V> r, V *z, const MGWork<V> &w, in
     const bool last = it + 1 == h->nu_post;
     V *out = other(cur);
     const SmoothStep &st = sm.post[it];
-    timed_cheb<T, V, KB>(h, l, F, r, cur, out, st.prev, nb, st.c1, st.c2, last ? dot_partial : nullptr, gx, s);
+    timed_cheb<T, V, KB>(h, l, F, r, cur, out, st.prev, nb, st.c1, st.c2, last ? dot_partial : nullptr, gx, w.status,
+                         s);
     cur = out;
   }
   if (cur != z) cudaMemcpyAsync(z, cur, sizeof(V) * F.dims.N * KB * nb, cudaMemcpyDeviceToDevice, s);
@@ -728,7 +736,8 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, V *z, const MGWork<V> &w, const Sc
       CK(cudaEventSynchronize(h->ev));
       if (h->h_mail[1] != 0) {
         *iters = it + 1;
-        return fail(DC_ERR_BREAKDOWN, "PCG breakdown: non-positive or non-finite p.Ap");
+        return fail(DC_ERR_BREAKDOWN, (h->h_mail[1] & 8) ? "multigrid smoothing: a shared-memory copy did not complete"
+                                                           : "PCG breakdown: non-positive or non-finite p.Ap");
       }
       if (h->h_mail[0] == 0) {
         ++it;
@@ -1001,6 +1010,13 @@ int dc_set_smoother(dc_handle *h, int kind) {
   if (!h) return fail(DC_ERR_ARG, "null handle");
   if (kind != 1 && kind != 4) return fail(DC_ERR_ARG, "smoother kind must be 1 or 4");
   h->smoother_kind = kind;
+  return 0;
+}
+
+int dc_set_staging(dc_handle *h, int enable) {
+  if (!h) return fail(DC_ERR_ARG, "null handle");
+  h->bulk_staging = enable != 0;
+  h->bulk_shape = enable > 1 ? enable : 0;
   return 0;
 }
 

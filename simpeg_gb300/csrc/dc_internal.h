@@ -112,6 +112,11 @@ template <typename T, typename V, int KB> struct Ops {
   // With partial (finest level only): also per-block partials of r . zout.
   static void cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb, double c1,
                         double c2, double *partial, int gx, cudaStream_t s);
+  // The same step (no partials) with x_k staged in shared memory by bulk asynchronous copies, for r and
+  // the iterates in V; false when it does not apply (then use cheb_step).  Copy timeouts set bit 8 of *status.
+  // shape = 10 * slab rows + copy depth to force one layout (0: automatic).
+  static bool cheb_bulk(const Level &L, const V *r, const V *zin, V *zout, int prev, int nb, double c1, double c2,
+                        int *status, int shape, cudaStream_t s);
   static void restrict_(const Level &f, const Level &c, const V *res, V *rc, int nb, cudaStream_t s);
   static void prolong_add(const Level &f, const Level &c, const V *zc, V *z, int nb, cudaStream_t s);
   static void coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V *zc, int nb, cudaStream_t s);

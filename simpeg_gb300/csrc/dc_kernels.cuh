@@ -339,6 +339,200 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
     sweep_flat<T, KB, W>(d.N, d.mn, nb, body);
 }
 
+// ---------------------------------------------------------------- staged stencil
+// Bulk asynchronous copies (cp.async.bulk, the Blackwell TMA engine) into
+// shared memory, completed on mbarriers.  Every wait is bounded: a wait that
+// gives up records bit 8 in the status word and the kernel drains its copies
+// (again with a bound) before returning.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// orders this thread's earlier generic-proxy shared accesses before later async-proxy (bulk copy) ones
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar` (each try_wait itself suspends for a
+// hardware-defined interval, so the bound is a time bound of seconds).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+constexpr int BULK_T = 512;  // threads of the staged kernel
+
+// Bytes of shared memory k_cheb_bulk needs: x_k rows (4 plane slots of TY+2
+// rows), r and x_{k-1} rows (NA slots of TY rows) and coefficient rows (NA+1
+// slots of TY+1 rows) for Nx nodes, KB lanes of V, plus 4+NA mbarriers.
+inline size_t cheb_bulk_smem(int Nx, int KB, size_t vbytes, int TY, int NA, bool prev) {
+  const size_t row = (size_t)Nx * KB * vbytes;
+  return (4 * (size_t)(TY + 2) + (size_t)NA * TY * (prev ? 2 : 1)) * row +
+         (size_t)(NA + 1) * (TY + 1) * Nx * sizeof(Coef32) + (4 + (size_t)NA) * 8;
+}
+
+// Chebyshev step (PREV as in k_cheb_step, no dot partials) on the finest
+// level with every stream staged in shared memory.  One CTA owns RHS block b
+// and a slab of TY node rows (all x, all KB lanes) and marches through the z
+// planes: while it updates plane k, the bulk-copy engine brings in x_k of
+// plane k+2 (rows j0-1 .. j0+TY, four plane slots) and r, x_{k-1} and the
+// coefficients of planes up to k+NA-1 (NA slots), so the DRAM streams stay in flight
+// independently of the threads' registers; all stencil, coefficient and
+// vector reads then come from shared memory and x_{k+1} is written straight
+// from registers (1/diag is recomputed from the staged diagonal: a 1/diag row
+// is not a multiple of 16 bytes).  Rows and planes beyond the mesh are redirected to the node
+// itself with weight 0 (c+* is zero on the last node of an axis).  The node
+// rows of one plane (and RHS block) are contiguous, so every copy is one
+// contiguous range.
+template <typename T, typename V, int KB, int PREV>
+__global__ void __launch_bounds__(BULK_T) k_cheb_bulk(const Coef32 *__restrict__ coef,
+                                                      const V *__restrict__ r, const V *__restrict__ zin, V *zout,
+                                                      Dims d, int TY, int NA, T c1, T c2,
+                                                      int *__restrict__ status) {
+  static_assert(sizeof(T) == 4, "staged smoothing is for the fp32 inner solve");
+  constexpr int W = Lanes<V, KB>::W, LPN = KB / W;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int Nx = d.Nx, Ny = d.Ny, Nz = d.Nz;
+  const long long N = d.N, NxNy = (long long)Nx * Ny;
+  const int nslab = (Ny + TY - 1) / TY;
+  const int b = blockIdx.x / nslab, slab = blockIdx.x % nslab;
+  const int j0 = slab * TY, j1 = min(j0 + TY, Ny);
+  const int jlo = max(j0 - 1, 0), jhi = min(j1, Ny - 1);
+  const int zrows = TY + 2, crows = TY + 1;
+  const size_t row = (size_t)Nx * KB;  // elements per node row
+  V *zb = reinterpret_cast<V *>(smem);
+  V *rb = zb + 4 * (size_t)zrows * row;
+  V *pb = rb + (size_t)NA * TY * row;
+  Coef32 *cb = reinterpret_cast<Coef32 *>(pb + (PREV == 1 ? (size_t)NA * TY * row : 0));
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(cb + (size_t)(NA + 1) * crows * Nx);
+  const long long base = (long long)b * N * KB;
+  const unsigned zbytes = (unsigned)((size_t)(jhi - jlo + 1) * row * sizeof(V));
+  const unsigned rbytes = (unsigned)((size_t)(j1 - j0) * row * sizeof(V));
+  const unsigned cbytes = (unsigned)((size_t)(j1 - jlo) * Nx * sizeof(Coef32));
+  auto issue_z = [&](int k) {
+    unsigned long long *bb = bar + (k & 3);
+    mbar_expect_tx(bb, zbytes);
+    bulk_g2s(zb + (size_t)(k & 3) * zrows * row + (size_t)(jlo - (j0 - 1)) * row,
+             zin + base + ((long long)k * NxNy + (long long)jlo * Nx) * KB, zbytes, bb);
+  };
+  // r, x_{k-1} and coefficients (rows jlo .. j1-1) of plane k
+  auto issue_aux = [&](int k) {
+    const int sa = k % NA;
+    unsigned long long *bb = bar + 4 + sa;
+    const long long node0 = (long long)k * NxNy + (long long)j0 * Nx;
+    mbar_expect_tx(bb, (PREV == 1 ? 2 * rbytes : rbytes) + cbytes);
+    bulk_g2s(rb + (size_t)sa * TY * row, r + base + node0 * KB, rbytes, bb);
+    if (PREV == 1) bulk_g2s(pb + (size_t)sa * TY * row, zout + base + node0 * KB, rbytes, bb);
+    bulk_g2s(cb + (size_t)(k % (NA + 1)) * crows * Nx + (size_t)(jlo - (j0 - 1)) * Nx,
+             coef + (long long)k * NxNy + (long long)jlo * Nx, cbytes, bb);
+  };
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 4 + NA; ++i) mbar_init(bar + i, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    issue_z(0);
+    if (Nz > 1) issue_z(1);
+    for (int k = 0; k < NA - 1 && k < Nz; ++k) issue_aux(k);
+  }
+  int issued_z = Nz > 1 ? 2 : 1, issued_aux = min(NA - 1, Nz);
+  bool failed = false;
+  for (int k = 0; k < Nz; ++k) {
+    // slots refilled here were last read in iteration k-1 (closed by its __syncthreads)
+    if (threadIdx.x == 0) {
+      fence_proxy_async();
+      if (k + 2 < Nz) issue_z(k + 2);
+      if (k + NA - 1 < Nz) issue_aux(k + NA - 1);
+    }
+    if (k + 2 < Nz) issued_z = k + 3;
+    if (k + NA - 1 < Nz) issued_aux = k + NA;
+    bool ok = mbar_wait(bar + (k & 3), (k >> 2) & 1);
+    if (k + 1 < Nz) ok = ok && mbar_wait(bar + ((k + 1) & 3), ((k + 1) >> 2) & 1);
+    ok = ok && mbar_wait(bar + 4 + k % NA, (k / NA) & 1);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const V *z0 = zb + (size_t)(k & 3) * zrows * row;
+    const V *zm = k > 0 ? zb + (size_t)((k + 3) & 3) * zrows * row : z0;
+    const V *zp = k + 1 < Nz ? zb + (size_t)((k + 1) & 3) * zrows * row : z0;
+    const V *rs = rb + (size_t)(k % NA) * TY * row;
+    const V *ps = pb + (size_t)(k % NA) * TY * row;
+    const Coef32 *c0 = cb + (size_t)(k % (NA + 1)) * crows * Nx;                      // row 0 = j0 - 1
+    const Coef32 *cm = k > 0 ? cb + (size_t)((k + NA) % (NA + 1)) * crows * Nx : c0;  // plane k - 1
+    const int items = (j1 - j0) * Nx * LPN;
+    for (int it = threadIdx.x; it < items; it += BULK_T) {
+      const int q = it % LPN, rem = it / LPN;
+      const int jj = fast_div(rem, Nx, d.mx), i = rem - jj * Nx, j = j0 + jj;
+      const bool hx = i > 0, px = i + 1 < Nx, hy = j > 0, py = j + 1 < Ny, hz = k > 0, pz = k + 1 < Nz;
+      const int co = (jj + 1) * Nx + i;  // own node in the coefficient slots
+      const Coef32 c = c0[co];
+      const T cxp = px ? c.cx : (T)0, cyp = py ? c.cy : (T)0, czp = pz ? c.cz : (T)0;
+      const T cxm = hx ? c0[co - 1].cx : (T)0, cym = hy ? c0[co - Nx].cy : (T)0, czm = hz ? cm[co].cz : (T)0;
+      const size_t so = ((size_t)(jj + 1) * Nx + i) * KB + q * W;
+      const Vec<T, W> v0 = ld<T, W>(z0 + so);
+      const Vec<T, W> vxp = ld<T, W>(z0 + so + (px ? KB : 0));
+      const Vec<T, W> vxm = ld<T, W>(z0 + so - (hx ? KB : 0));
+      const Vec<T, W> vyp = ld<T, W>(z0 + so + (py ? row : 0));
+      const Vec<T, W> vym = ld<T, W>(z0 + so - (hy ? row : 0));
+      const Vec<T, W> vzp = ld<T, W>(zp + so);
+      const Vec<T, W> vzm = ld<T, W>(zm + so);
+      const size_t ro = ((size_t)jj * Nx + i) * KB + q * W;
+      const Vec<T, W> rv = ld<T, W>(rs + ro);
+      Vec<T, W> zo;
+      if (PREV == 1) zo = ld<T, W>(ps + ro);
+      const T sd = c2 / c.d;
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        const T az = c.d * v0.a[e] - cxp * vxp.a[e] - cxm * vxm.a[e] - cyp * vyp.a[e] - cym * vym.a[e] -
+                     czp * vzp.a[e] - czm * vzm.a[e];
+        T mom = (T)0;
+        if (PREV == 1) mom = c1 * (v0.a[e] - zo.a[e]);
+        if (PREV == 2) mom = c1 * v0.a[e];
+        zo.a[e] = v0.a[e] + mom + sd * (rv.a[e] - az);
+      }
+      st<T, W>(zout + base + ((long long)k * NxNy + (long long)j * Nx + i) * KB + q * W, zo);
+    }
+    __syncthreads();
+  }
+  if (failed) {
+    if (threadIdx.x == 0) {
+      atomicOr(status, 8);
+      // drain: the copies issued into this CTA's shared memory must land before it exits;
+      // wait for the latest issued phase of every slot
+      for (int k = max(issued_z - 4, 0); k < issued_z; ++k) mbar_wait(bar + (k & 3), (k >> 2) & 1);
+      for (int k = max(issued_aux - NA, 0); k < issued_aux; ++k) mbar_wait(bar + 4 + k % NA, (k / NA) & 1);
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------- transfers
 struct XferTab {
   const int *fi;        // coarse node -> fine node, per axis at roff[a]
@@ -669,6 +863,63 @@ void Ops<T, V, KB>::cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout
       else if (prev == 2) cheb_launch<T, V, KB, V, false, 2>(L, rp, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s);
       else cheb_launch<T, V, KB, V, false, 0>(L, rp, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s);
     }
+  }
+}
+
+// Staged Chebyshev step (k_cheb_bulk) when it applies: RHS and iterates in
+// the multigrid storage type, node rows a multiple of 16 bytes and a slab of
+// at least one row fitting in shared memory.  Returns false otherwise (the
+// caller then uses cheb_step).
+template <typename T, typename V, int KB>
+bool Ops<T, V, KB>::cheb_bulk(const Level &L, const V *r, const V *zin, V *zout, int prev, int nb, double c1,
+                              double c2, int *status, int shape, cudaStream_t s) {
+  if constexpr (sizeof(T) != 4 || sizeof(V) != 2 || (KB * sizeof(V)) % 16 != 0) {
+    return false;
+  } else {
+    if (!status) return false;
+    static int max_smem = -1;
+    if (max_smem < 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const size_t budget = (size_t)max_smem;
+    // slab height and copy depth: the forced pair if given, else the first that fits
+    int TY = 0, NA = 0;
+    const int cand[4][2] = {{2, 3}, {1, 3}, {2, 2}, {1, 2}};
+    for (auto &cnd : cand) {
+      if (shape > 0 && cnd[0] * 10 + cnd[1] != shape) continue;
+      if (cheb_bulk_smem(L.dims.Nx, KB, sizeof(V), cnd[0], cnd[1], true) <= budget) {
+        TY = cnd[0];
+        NA = cnd[1];
+        break;
+      }
+    }
+    if (TY == 0) return false;
+    const size_t smem = cheb_bulk_smem(L.dims.Nx, KB, sizeof(V), TY, NA, prev == 1);
+    // the shared-memory limit is raised once per kernel, outside any stream capture
+    static bool configured = false, usable = false;
+    if (!configured) {
+      usable = true;
+      for (const void *kern : {(const void *)k_cheb_bulk<T, V, KB, 0>, (const void *)k_cheb_bulk<T, V, KB, 1>,
+                               (const void *)k_cheb_bulk<T, V, KB, 2>})
+        usable = usable && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget) ==
+                               cudaSuccess;
+      if (!usable) cudaGetLastError();
+      configured = true;
+    }
+    if (!usable) return false;
+    const dim3 grid(count_launch(dim3((unsigned)(nb * ((L.dims.Ny + TY - 1) / TY)))));
+    if (prev == 1)
+      k_cheb_bulk<T, V, KB, 1><<<grid, BULK_T, smem, s>>>(L.d_coef32, r, zin, zout, L.dims, TY, NA, (T)c1,
+                                                          (T)c2, status);
+    else if (prev == 2)
+      k_cheb_bulk<T, V, KB, 2><<<grid, BULK_T, smem, s>>>(L.d_coef32, r, zin, zout, L.dims, TY, NA, (T)c1,
+                                                          (T)c2, status);
+    else
+      k_cheb_bulk<T, V, KB, 0><<<grid, BULK_T, smem, s>>>(L.d_coef32, r, zin, zout, L.dims, TY, NA, (T)c1,
+                                                          (T)c2, status);
+    return true;
   }
 }
 

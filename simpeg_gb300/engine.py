@@ -118,6 +118,11 @@ class DCEngine:
         """Chebyshev smoother of the first (1) or fourth (4) kind."""
         check(lib().dc_set_smoother(self._h, int(kind)))
 
+    def set_staging(self, enable):
+        """Finest-level smoothing staged through shared memory by bulk copies (True) or direct loads;
+        an int 10 * rows + depth forces the slab layout."""
+        check(lib().dc_set_staging(self._h, int(enable)))
+
     def set_model(self, sigma):
         sigma = _dev64(sigma, (self.nC,), "sigma")
         check(lib().dc_set_model(self._h, _ptr(sigma), _stream()))
