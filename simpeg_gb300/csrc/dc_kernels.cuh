@@ -195,23 +195,37 @@ __device__ __forceinline__ void block_reduce(T (&acc)[W], T *red, int b, double 
   __syncthreads();
 }
 
+// Software prefetch into L2 of the element offset a thread will touch in its
+// next grid-stride iteration (one thread per 128-byte line), so the DRAM
+// requests of two iterations are in flight at once without extra registers.
+__device__ __forceinline__ void pf_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+template <typename S>
+__device__ __forceinline__ void pf_line(const S *base, long long t) {
+  if ((threadIdx.x & 7) == 0) pf_l2(base + t);
+}
+struct NoPf {
+  __device__ __forceinline__ void operator()(long long) const {}
+};
+
 // Sweep of a reducing kernel: the RHS blocks one after the other (the whole
 // grid on one RHS block at a time, as in the flat sweep), each closed by the
 // block reduction of that RHS block's per-thread sums.
 // body(b, n, q, t, acc): RHS block, node, lane group, element offset, sums.
-template <typename T, int KB, int W, typename Body>
-__device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int gs, Body body) {
+template <typename T, int KB, int W, typename Body, typename Pf = NoPf>
+__device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int gs, Body body, Pf pf = Pf()) {
   constexpr int LPN = KB / W;
   __shared__ T red[(TPB / 32) * KB];
   const int q = threadIdx.x % LPN;
   const long long per = (long long)N * LPN;
+  const long long stride = (long long)gridDim.x * TPB;
   for (int b = 0; b < nb; ++b) {
     T acc[W];
 #pragma unroll
     for (int e = 0; e < W; ++e) acc[e] = (T)0;
     const long long base = (long long)b * N;
-    for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < per; g += (long long)gridDim.x * TPB) {
+    for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < per; g += stride) {
       const int n = (int)(g / LPN);
+      if (g + stride < per) pf((base + (g + stride) / LPN) * KB + q * W);
       body(b, n, q, (base + n) * KB + q * W, acc);
     }
     block_reduce<T, KB, W>(acc, red, b, partial, gs);
@@ -219,15 +233,17 @@ __device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int
 }
 
 // The same body over the flat (RHS block, node, lane group) sweep, no reduction.
-template <typename T, int KB, int W, typename Body>
-__device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body) {
+template <typename T, int KB, int W, typename Body, typename Pf = NoPf>
+__device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body, Pf pf = Pf()) {
   constexpr int LPN = KB / W;
   const int q = threadIdx.x % LPN;
   const long long total = (long long)N * nb * LPN;
+  const long long stride = (long long)gridDim.x * TPB;
   T acc[W];
-  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total; g += (long long)gridDim.x * TPB) {
+  for (long long g = (long long)blockIdx.x * TPB + threadIdx.x; g < total; g += stride) {
     const int ng = (int)(g / LPN);
     const int b = fast_div(ng, N, mn);
+    if (g + stride < total) pf(((g + stride) / LPN) * KB + q * W);
     body(b, ng - b * N, q, (long long)ng * KB + q * W, acc);
   }
 }
@@ -251,10 +267,14 @@ __global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, cons
       for (int e = 0; e < W; ++e) acc[e] += v.a[e] * xv.a[e];
     }
   };
+  // prefetch pays where load latency bounds the kernel (fp32 stencils), not in the fp64-issue-bound ones
+  auto pf = [&](long long tn) {
+    if constexpr (sizeof(T) == 4) pf_line(x, tn);
+  };
   if (DOT)
-    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body);
+    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body, pf);
   else
-    sweep_flat<T, KB, W>(d.N, d.mn, nb, body);
+    sweep_flat<T, KB, W>(d.N, d.mn, nb, body, pf);
 }
 
 // res = r - A z
@@ -333,10 +353,17 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
       }
     }
   };
+  auto pf = [&](long long tn) {
+    if constexpr (sizeof(T) == 4) {
+      pf_line(zin, tn);
+      pf_line(r, tn);
+      if (PREV == 1) pf_line(zout, tn);
+    }
+  };
   if (DOT)
-    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body);
+    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body, pf);
   else
-    sweep_flat<T, KB, W>(d.N, d.mn, nb, body);
+    sweep_flat<T, KB, W>(d.N, d.mn, nb, body, pf);
 }
 
 // ---------------------------------------------------------------- staged stencil
