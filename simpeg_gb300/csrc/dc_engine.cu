@@ -216,6 +216,7 @@ struct dc_handle {
   int nc = 0;
   double *d_Ainv64 = nullptr, *d_dense = nullptr, *d_work = nullptr;
   float *d_Ainv32 = nullptr;
+  Coef32 *d_cdf_hi = nullptr, *d_cdf_lo = nullptr;  // finest-level fp64 coefficients as double-float pairs
   int *d_flag = nullptr;
   unsigned long long *d_lmax = nullptr;
   bool model_set = false;
@@ -480,7 +481,8 @@ void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
   const size_t n = (size_t)N * w.Kp;
   w.B64 = c.take<double>(n);
   w.X64 = c.take<double>(n);
-  w.R64 = mode == DC_MODE_MIXED ? nullptr : c.take<double>(n);  // the fp64 PCG residual
+  // fp64 mode: the PCG residual; mixed mode: b as a double-float pair (x64 is one too)
+  w.R64 = c.take<double>(n);
   if (mode == DC_MODE_MIXED) {
     w.d32 = c.take<float>(n);
     w.r32 = c.take<float>(n);
@@ -798,6 +800,10 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, nullptr,
                 0.0, 0.0, s);
   } else {
+    // Refinement in double-float: b and x as (hi, lo) fp32 pairs in the B64-sized regions R64 and X64.
+    float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
+    float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
+    split_df(w.B64, (long long)N * Kp, bh, bl, s);
     // |b|^2, initial outer flags, r32 = b
     Ops<double, double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
@@ -820,8 +826,9 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
         rc = pcg<float, float, KB>(h, w.d32, w.r32, w.p32, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
-      ir_accumulate<KB>(N, nb, w.X64, w.d32, so);
-      ir_residual<KB>(F, w.B64, w.X64, nullptr, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, so);
+      ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, so);
+      ir_residual_df<KB>(F, h->d_cdf_hi, h->d_cdf_lo, bh, bl, xh, xl, w.r32, nb, w.sc.active_out, w.sc.part_a, gx,
+                         so);
       sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, so);
       outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel,
                   w.sc.tol2, inner_rtol * inner_rtol, kSafety2, so);
@@ -859,7 +866,11 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       if (outer >= max_outer && !fixed) status = DC_ERR_NOT_CONVERGED;
     }
   }
-  unpack_colmajor<double>(w.X64, N, k, KB, x, s);
+  if (mode == DC_MODE_MIXED)
+    unpack_colmajor_df(reinterpret_cast<const float *>(w.X64), reinterpret_cast<const float *>(w.X64) + (size_t)N * Kp,
+                       N, k, KB, x, s);
+  else
+    unpack_colmajor<double>(w.X64, N, k, KB, x, s);
   if (!h->robin) neumann_shift(b, N, k, x, s);
   if (fixed || device) {  // the convergence state stays on the device (dc_solve_check)
     if (st) {
@@ -961,6 +972,8 @@ void dc_destroy(dc_handle *h) {
   cudaFree(h->d_Q);
   cudaFree(h->d_Ainv64);
   cudaFree(h->d_Ainv32);
+  cudaFree(h->d_cdf_hi);
+  cudaFree(h->d_cdf_lo);
   cudaFree(h->d_dense);
   cudaFree(h->d_work);
   cudaFree(h->d_flag);
@@ -1056,6 +1069,12 @@ int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
     if (!(lm > 0.0) || !std::isfinite(lm)) return fail(DC_ERR_ARG, "conductivity must be positive and finite");
     L.lmax = lm;
   }
+  if (!h->d_cdf_hi) {
+    int rc;
+    if ((rc = dalloc(&h->d_cdf_hi, L0.dims.N))) return rc;
+    if ((rc = dalloc(&h->d_cdf_lo, L0.dims.N))) return rc;
+  }
+  coef_split_df(L0, h->d_cdf_hi, h->d_cdf_lo, s);
   CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), s));
   dense_assemble(h->lv.back(), h->d_dense, s);
   // The Neumann operator is singular (constants); its coarsest matrix is

@@ -138,9 +138,16 @@ template <int KB>
 void ir_residual(const Level &L, const double *b, const double *x, double *r64, float *r32, int nb,
                  const int *active, double *partial, int gx, cudaStream_t s);
 template <int KB>
-void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s);
-template <int KB>
 int ir_blocks_per_sm();
+// Double-float (fp32 pair) refinement of the mixed solve: hi/lo splits of fp64
+// vectors and coefficients, b - A x and x += d in double-float arithmetic.
+void split_df(const double *a, long long n, float *hi, float *lo, cudaStream_t s);
+void coef_split_df(const Level &L, Coef32 *hi, Coef32 *lo, cudaStream_t s);
+template <int KB>
+void ir_residual_df(const Level &L, const Coef32 *ch, const Coef32 *cl, const float *bh, const float *bl,
+                    const float *xh, const float *xl, float *r32, int nb, const int *active, double *partial, int gx,
+                    cudaStream_t s);
+void ir_accumulate_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s);
 
 void fill_int(int *a, int n, int v, cudaStream_t s);
 // alpha = rz / (p.q) per active RHS; also zeroes *n_active for the pcg_beta of the same iteration
@@ -180,6 +187,7 @@ template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s);
 template <typename T>
 void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s);
+void unpack_colmajor_df(const float *hi, const float *lo, long long N, int K, int KB, double *dst, cudaStream_t s);
 
 // ---- dc_sens.cu -------------------------------------------------------------
 void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const double *w, const double *x,

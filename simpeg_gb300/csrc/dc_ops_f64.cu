@@ -1,7 +1,6 @@
-// Instantiation of the node kernels for the fp64 solve (T = V = double) and
-// the fp64 refinement kernels of the mixed-precision solve: the residual
-// b - A x of the fp64 operator with its per-RHS norms, and the solution
-// accumulation x64 += d32.
+// Instantiation of the node kernels for the fp64 solve (T = V = double), the
+// fp64 true-residual kernel, and the double-float refinement kernels of the
+// mixed-precision solve (b - A x and x += d with fp32 pairs).
 #include "dc_kernels.cuh"
 
 namespace dc {
@@ -32,25 +31,122 @@ __global__ void __launch_bounds__(TPB) k_ir_residual(const Coef64 *__restrict__ 
   });
 }
 
-__global__ void __launch_bounds__(TPB) k_ir_accumulate(long long total4, double *__restrict__ x64,
-                                                       const float *__restrict__ d32) {
-  // total4 = number of 4-element groups (the blocked arrays are padded to KB >= 1 lanes; tail handled by caller)
-  for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < total4; t += (long long)gridDim.x * TPB) {
-    const float4 dv = reinterpret_cast<const float4 *>(d32)[t];
-    double2 a = reinterpret_cast<double2 *>(x64)[2 * t], b = reinterpret_cast<double2 *>(x64)[2 * t + 1];
-    a.x += dv.x;
-    a.y += dv.y;
-    b.x += dv.z;
-    b.y += dv.w;
-    reinterpret_cast<double2 *>(x64)[2 * t] = a;
-    reinterpret_cast<double2 *>(x64)[2 * t + 1] = b;
+
+// ---------------------------------------------------------------- double-float refinement
+// The refinement residual of the mixed solve in double-float arithmetic: every
+// fp64 quantity is an unevaluated sum hi + lo of two fp32 numbers (about 48
+// significant bits), so b - A x runs on the fp32 pipes instead of the fp64
+// ones, which on this part issue 1/64 as fast.  Error-free transformations:
+// Knuth's two-sum and the fused-multiply-add product error (Dekker, "A
+// floating-point technique for extending the available precision", 1971).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (sh, sl) += (ph, pl), renormalised
+__device__ __forceinline__ void df_acc(float &sh, float &sl, float ph, float pl) {
+  float s, e;
+  two_sum(sh, ph, s, e);
+  e += sl + pl;
+  sh = s + e;
+  sl = e - (sh - s);
+}
+
+// (ph, pl) = (ah, al) * (bh, bl) up to the al * bl term
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &ph, float &pl) {
+  ph = ah * bh;
+  pl = fmaf(ah, bh, -ph);
+  pl = fmaf(ah, bl, fmaf(al, bh, pl));
+}
+
+__global__ void k_split_df(const double *__restrict__ a, long long n, float *__restrict__ hi, float *__restrict__ lo) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = a[i];
+    const float h = (float)v;
+    hi[i] = h;
+    lo[i] = (float)(v - (double)h);
   }
 }
 
-__global__ void k_ir_accumulate_tail(long long start, long long total, double *__restrict__ x64,
-                                     const float *__restrict__ d32) {
-  for (long long t = start + (long long)blockIdx.x * TPB + threadIdx.x; t < total; t += (long long)gridDim.x * TPB)
-    x64[t] += (double)d32[t];
+__global__ void k_coef_split_df(const Coef64 *__restrict__ c, long long n, Coef32 *__restrict__ hi,
+                                Coef32 *__restrict__ lo) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const Coef64 v = c[i];
+    Coef32 h{(float)v.cx, (float)v.cy, (float)v.cz, (float)v.d};
+    Coef32 l{(float)(v.cx - (double)h.cx), (float)(v.cy - (double)h.cy), (float)(v.cz - (double)h.cz),
+             (float)(v.d - (double)h.d)};
+    hi[i] = h;
+    lo[i] = l;
+  }
+}
+
+// r32 = (float)(b - A x) for active RHS (0 otherwise), per-block partials of |r|^2
+template <int KB>
+__global__ void __launch_bounds__(TPB) k_ir_residual_df(const Coef32 *__restrict__ ch, const Coef32 *__restrict__ cl,
+                                                        const float *__restrict__ bh, const float *__restrict__ bl,
+                                                        const float *__restrict__ xh, const float *__restrict__ xl,
+                                                        float *__restrict__ r32, Dims d, int nb,
+                                                        const int *__restrict__ active, double *__restrict__ partial,
+                                                        int gs) {
+  using T = float;
+  constexpr int W = Lanes<T, KB>::W;
+  sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
+    int i, j, k;
+    node_ijk(n, d, i, j, k);
+    const bool hx = i > 0, px = i + 1 < d.Nx, hy = j > 0, py = j + 1 < d.Ny, hz = k > 0, pz = k + 1 < d.Nz;
+    const int sy = d.Nx, sz = d.Nx * d.Ny;
+    const Coef32 c0h = ch[n], c0l = cl[n];
+    // couplings (hi, lo), zero off the mesh; neighbour element offsets (0 off the mesh)
+    const float wh[6] = {px ? c0h.cx : 0.f, hx ? ch[n - 1].cx : 0.f, py ? c0h.cy : 0.f,
+                         hy ? ch[hy ? n - sy : n].cy : 0.f, pz ? c0h.cz : 0.f, hz ? ch[hz ? n - sz : n].cz : 0.f};
+    const float wl[6] = {px ? c0l.cx : 0.f, hx ? cl[n - 1].cx : 0.f, py ? c0l.cy : 0.f,
+                         hy ? cl[hy ? n - sy : n].cy : 0.f, pz ? c0l.cz : 0.f, hz ? cl[hz ? n - sz : n].cz : 0.f};
+    const long long off[6] = {px ? (long long)KB : 0,       hx ? -(long long)KB : 0,
+                              py ? (long long)sy * KB : 0,  hy ? -(long long)sy * KB : 0,
+                              pz ? (long long)sz * KB : 0,  hz ? -(long long)sz * KB : 0};
+    const Vec<T, W> b0h = ld<T, W>(bh + t), b0l = ld<T, W>(bl + t);
+    const Vec<T, W> x0h = ld<T, W>(xh + t), x0l = ld<T, W>(xl + t);
+    float rh[W], rl[W];
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      rh[e] = b0h.a[e];
+      rl[e] = b0l.a[e];
+      float ph, pl;
+      df_mul(c0h.d, c0l.d, x0h.a[e], x0l.a[e], ph, pl);
+      df_acc(rh[e], rl[e], -ph, -pl);
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const Vec<T, W> vh = ld<T, W>(xh + t + off[m]), vl = ld<T, W>(xl + t + off[m]);
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        float ph, pl;
+        df_mul(wh[m], wl[m], vh.a[e], vl.a[e], ph, pl);
+        df_acc(rh[e], rl[e], ph, pl);
+      }
+    }
+    Vec<T, W> out;
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const float rv = rh[e] + rl[e];
+      acc[e] += rv * rv;
+      out.a[e] = active[b * KB + q * W + e] ? rv : 0.0f;
+    }
+    st<T, W>(r32 + t, out);
+  });
+}
+
+// (xh, xl) += d, exactly rounded to double-float
+__global__ void __launch_bounds__(TPB) k_ir_accumulate_df(long long n, float *__restrict__ xh, float *__restrict__ xl,
+                                                          const float *__restrict__ d32) {
+  for (long long i = (long long)blockIdx.x * TPB + threadIdx.x; i < n; i += (long long)gridDim.x * TPB) {
+    float h = xh[i], l = xl[i];
+    df_acc(h, l, d32[i], 0.0f);
+    xh[i] = h;
+    xl[i] = l;
+  }
 }
 
 }  // namespace
@@ -64,25 +160,41 @@ void ir_residual(const Level &L, const double *b, const double *x, double *r64, 
       L.d_coef64, b, x, r64, r32, L.dims, nb, active, partial, gx);
 }
 
+
+void split_df(const double *a, long long n, float *hi, float *lo, cudaStream_t s) {
+  k_split_df<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(a, n, hi, lo);
+}
+
+void coef_split_df(const Level &L, Coef32 *hi, Coef32 *lo, cudaStream_t s) {
+  k_coef_split_df<<<count_launch(grid_flat(L.dims.N, g_n_sm)), TPB, 0, s>>>(L.d_coef64, L.dims.N, hi, lo);
+}
+
 template <int KB>
-void ir_accumulate(long long N, int nb, double *x64, const float *d32, cudaStream_t s) {
-  const long long total = N * KB * nb;
-  const long long t4 = total / 4;
-  if (t4 > 0) k_ir_accumulate<<<count_launch(grid_flat(t4, g_n_sm)), TPB, 0, s>>>(t4, x64, d32);
-  if (t4 * 4 < total) k_ir_accumulate_tail<<<count_launch(1), TPB, 0, s>>>(t4 * 4, total, x64, d32);
+void ir_residual_df(const Level &L, const Coef32 *ch, const Coef32 *cl, const float *bh, const float *bl,
+                    const float *xh, const float *xl, float *r32, int nb, const int *active, double *partial, int gx,
+                    cudaStream_t s) {
+  k_ir_residual_df<KB><<<RED_GRID(L.dims.N, k_ir_residual_df<KB>, (Lanes<float, KB>::LPN)), TPB, 0, s>>>(
+      ch, cl, bh, bl, xh, xl, r32, L.dims, nb, active, partial, gx);
+}
+
+void ir_accumulate_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s) {
+  k_ir_accumulate_df<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(n, xh, xl, d32);
 }
 
 // resident blocks per SM of the fp64 reduction kernels the mixed solve also runs
 template <int KB>
 int ir_blocks_per_sm() {
-  return std::max(resident_blocks((const void *)k_ir_residual<KB>), resident_blocks((const void *)k_dot<double, double, KB>));
+  return std::max({resident_blocks((const void *)k_ir_residual<KB>), resident_blocks((const void *)k_ir_residual_df<KB>),
+                   resident_blocks((const void *)k_dot<double, double, KB>)});
 }
 
 #define DC_INST_IR(KB)                                                                                       \
   template void ir_residual<KB>(const Level &, const double *, const double *, double *, float *, int,      \
                                 const int *, double *, int, cudaStream_t);                                  \
-  template void ir_accumulate<KB>(long long, int, double *, const float *, cudaStream_t);                  \
-  template int ir_blocks_per_sm<KB>();
+  template int ir_blocks_per_sm<KB>();                                                                       \
+  template void ir_residual_df<KB>(const Level &, const Coef32 *, const Coef32 *, const float *, const float *,    \
+                                   const float *, const float *, float *, int, const int *, double *, int,         \
+                                   cudaStream_t);
 DC_INST_IR(1) DC_INST_IR(2) DC_INST_IR(4) DC_INST_IR(8) DC_INST_IR(16) DC_INST_IR(32)
 #undef DC_INST_IR
 

@@ -497,6 +497,31 @@ __global__ void __launch_bounds__(TT *TR) k_unpack(const T *__restrict__ src, lo
   }
 }
 
+// The same transpose for a double-float (hi, lo) blocked array: dst = hi + lo in fp64.
+__global__ void __launch_bounds__(TT *TR) k_unpack_df(const float *__restrict__ hi, const float *__restrict__ lo,
+                                                     long long N, int K, int KB, double *__restrict__ dst) {
+  __shared__ double tile[TT][TT + 1];
+  const long long n0 = (long long)blockIdx.x * TT;
+  const int r0 = blockIdx.y * TT;
+  {
+    const int r = r0 + threadIdx.x;
+    const int b = r / KB, l = r % KB;
+    for (int j = threadIdx.y; j < TT; j += TR) {
+      const long long n = n0 + j;
+      if (r < K && n < N) {
+        const long long e = ((long long)b * N + n) * KB + l;
+        tile[threadIdx.x][j] = (double)hi[e] + (double)lo[e];
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < TT; i += TR) {
+    const int r = r0 + i;
+    const long long n = n0 + threadIdx.x;
+    if (r < K && n < N) dst[(long long)r * N + n] = tile[i][threadIdx.x];
+  }
+}
+
 }  // namespace
 
 // Resident blocks per SM of a kernel (cached).  Grids are capped at what the
@@ -615,6 +640,11 @@ void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst
   const int Kp = KB * nb;
   const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((Kp + TT - 1) / TT));
   k_pack<T><<<count_launch(grid), dim3(TT, TR), 0, s>>>(src, N, K, KB, Kp, dst);
+}
+
+void unpack_colmajor_df(const float *hi, const float *lo, long long N, int K, int KB, double *dst, cudaStream_t s) {
+  const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((K + TT - 1) / TT));
+  k_unpack_df<<<count_launch(grid), dim3(TT, TR), 0, s>>>(hi, lo, N, K, KB, dst);
 }
 
 template <typename T>
