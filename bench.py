@@ -479,7 +479,8 @@ def run_gauss_newton(args):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         res[precision] = (p.cpu().numpy(), info["g"].cpu().numpy(), info["jtj_diag"].cpu().numpy())
-        out[precision] = {"seconds": dt, "cg_rel_res": info["cg_rel_res"][-1]}
+        out[precision] = {"seconds": dt, "cg_rel_res": info["cg_rel_res"][-1],
+                          "phases_seconds": {k: round(v, 3) for k, v in info["seconds"].items()}}
         del sim, dmis, reg, p, info
         torch.cuda.empty_cache()
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))

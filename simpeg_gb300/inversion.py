@@ -135,14 +135,26 @@ def inexact_gauss_newton_direction(dmis, reg, beta, m, cg_maxiter=10, cg_rtol=0.
 
     Returns (p, info) with p a device tensor and info a dict of the pieces
     (gradient, JtJ diagonal, CG residual history)."""
+    import time
+
     sim = dmis.simulation
+    secs = {}
+
+    def lap(name, t0):
+        torch.cuda.synchronize()
+        secs[name] = time.perf_counter() - t0
+        return time.perf_counter()
+
+    t = time.perf_counter()
     sim.model = m
     sim._ensure_model()
     dev = sim.device
     mt = torch.as_tensor(np.asarray(m, dtype=np.float64), device=dev)
     sim.fields(m)
+    t = lap("fields", t)
     g = dmis.deriv_dev(m) + beta * reg.deriv_dev(mt)
-    info = {"g": g}
+    t = lap("gradient", t)
+    info = {"g": g, "seconds": secs}
     if precondition:
         jtj = torch.as_tensor(sim.getJtJdiag(m, W=_Diag(dmis.W)), device=dev)
         dA = jtj + beta * reg.diag_deriv2()
@@ -150,6 +162,7 @@ def inexact_gauss_newton_direction(dmis, reg, beta, m, cg_maxiter=10, cg_rtol=0.
         info["jtj_diag"] = jtj
     else:
         Minv = torch.ones_like(g)
+    t = lap("jtj_diag", t)
 
     def H(v):
         return dmis.deriv2_dev(m, v) + beta * reg.deriv2_dev(v)
@@ -175,6 +188,7 @@ def inexact_gauss_newton_direction(dmis, reg, beta, m, cg_maxiter=10, cg_rtol=0.
         rz_new = float((r * z).sum())
         pvec = z + (rz_new / rz) * pvec
         rz = rz_new
+    lap("cg", t)
     info["cg_rel_res"] = hist
     return x, info
 

@@ -131,14 +131,16 @@ class SurveyTables:
         self.P = sp.vstack(rows, format="csr") if rows else sp.csr_matrix((0, self.nN * max(self.nSrc, 1)))
         self.P.sum_duplicates()
         self.nD = self.P.shape[0]
-        PT = self.P.T.tocsr()
-        PT.sum_duplicates()
-        nz = np.flatnonzero(np.diff(PT.indptr))
-        self.PT_out = nz.astype(np.int64)
-        sub = PT[nz]
-        self.PT_ptr = sub.indptr.astype(np.int64)
-        self.PT_idx = sub.indices.astype(np.int64)
-        self.PT_w = sub.data.astype(np.float64)
+        # transpose restricted to its nonzero rows, built from P's entries (sorted by
+        # column, then datum) without materialising the nSrc*nN-row CSR
+        Pc = self.P.tocoo()
+        order = np.lexsort((Pc.row, Pc.col))
+        cols, data_idx, vals = Pc.col[order].astype(np.int64), Pc.row[order].astype(np.int64), Pc.data[order]
+        self.PT_out, starts = np.unique(cols, return_index=True)
+        self.PT_out = self.PT_out.astype(np.int64)
+        self.PT_ptr = np.r_[starts, cols.size].astype(np.int64)
+        self.PT_idx = data_idx
+        self.PT_w = vals.astype(np.float64)
         self.P_ptr = self.P.indptr.astype(np.int64)
         self.P_idx = self.P.indices.astype(np.int64)
         self.P_w = self.P.data.astype(np.float64)
