@@ -13,8 +13,10 @@
 // One CTA owns a 2x2x2 tile of cells (27 nodes): it stages every electrode's
 // pole solution on those nodes in shared memory (relative to the tile centre,
 // in fp32, so gradients keep fp32 relative accuracy), then streams the data,
-// accumulating W_d^2 J_dc^2 per cell in fp64.  Cost: nE pole solves plus
-// O(nD * nC) fp32 arithmetic with no J in memory.
+// accumulating W_d^2 J_dc^2 per cell in fp32 per thread (sums of positive
+// terms; the per-thread sums are combined in fp64).  All per-datum arithmetic
+// is fp32: on this part fp64 issues at 1/64 of the fp32 rate.  Cost: nE pole
+// solves plus O(nD * nC) fp32 arithmetic with no J in memory.
 #include "../../include/dcgpu.h"
 #include "dc_internal.h"
 
@@ -23,7 +25,7 @@
 namespace dc {
 namespace {
 
-constexpr int JTPB = 256;
+constexpr int JTPB = 512;
 
 struct JtjData {
   const int *sa, *sb, *rm, *rn;        // electrode indices (-1 = none)
@@ -65,25 +67,25 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
   // cell geometry of the 8 tile cells
   bool have[8];
   float wx[8], wy[8], wz[8];
-  double sg[8];
+  float sg[8];
   int bnd[8];
   for (int c = 0; c < 8; ++c) {
     const int ci = i0 + (c & 1), cj = j0 + ((c >> 1) & 1), ck = k0 + (c >> 2);
     have[c] = ci < nx && cj < ny && ck < nz;
     wx[c] = wy[c] = wz[c] = 0.f;
-    sg[c] = 0.0;
+    sg[c] = 0.f;
     bnd[c] = 0;
     if (have[c]) {
       const double V = hx[ci] * hy[cj] * hz[ck];
       wx[c] = (float)(0.25 * V / (hx[ci] * hx[ci]));
       wy[c] = (float)(0.25 * V / (hy[cj] * hy[cj]));
       wz[c] = (float)(0.25 * V / (hz[ck] * hz[ck]));
-      sg[c] = dsig ? dsig[ci + (long long)nx * (cj + (long long)ny * ck)] : 1.0;
+      sg[c] = dsig ? (float)dsig[ci + (long long)nx * (cj + (long long)ny * ck)] : 1.f;
       if (bface) bnd[c] = (ci == 0) | ((ci == nx - 1) << 1) | ((cj == 0) << 2) | ((cj == ny - 1) << 3) |
                           ((ck == 0) << 4) | ((ck == nz - 1) << 5);
     }
   }
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int d = threadIdx.x; d < D.nD; d += JTPB) {
     const int sa = D.sa[d], sb = D.sb[d], rm = D.rm[d], rn = D.rn[d];
     const float ia = (float)D.ia[d], ib = sb >= 0 ? (float)D.ib[d] : 0.f;
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
       u[j] = ia * pa[j] + ib * pb[j];
       l[j] = wm * pm[j] + wn * pn[j];
     }
-    const double w2 = D.w2[d];
+    const float w2 = (float)D.w2[d];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       if (!have[c]) continue;
@@ -111,7 +113,7 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
           sy += (u[id(p, 1, q)] - u[id(p, 0, q)]) * (l[id(p, 1, q)] - l[id(p, 0, q)]);
           sz += (u[id(p, q, 1)] - u[id(p, q, 0)]) * (l[id(p, q, 1)] - l[id(p, q, 0)]);
         }
-      double a = (double)(wx[c] * sx + wy[c] * sy + wz[c] * sz);
+      float a = wx[c] * sx + wy[c] * sy + wz[c] * sz;
       if (bnd[c]) {
         // Robin part: absolute potentials on the boundary faces of the cell
         const double ur = (double)ia * ref[sa] + (sb >= 0 ? (double)ib * ref[sb] : 0.0);
@@ -121,14 +123,16 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
           return ((double)u[j] + ur) * ((double)l[j] + lr);
         };
         const int ci = i0 + a0, cj = j0 + b0, ck = k0 + c0;
-        if (bnd[c] & 1) a += bface[bo0 + cj + (long long)ny * ck] * (ul(0, 0, 0) + ul(0, 1, 0) + ul(0, 0, 1) + ul(0, 1, 1));
-        if (bnd[c] & 2) a += bface[bo1 + cj + (long long)ny * ck] * (ul(1, 0, 0) + ul(1, 1, 0) + ul(1, 0, 1) + ul(1, 1, 1));
-        if (bnd[c] & 4) a += bface[bo2 + ci + (long long)nx * ck] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 0, 1) + ul(1, 0, 1));
-        if (bnd[c] & 8) a += bface[bo3 + ci + (long long)nx * ck] * (ul(0, 1, 0) + ul(1, 1, 0) + ul(0, 1, 1) + ul(1, 1, 1));
-        if (bnd[c] & 16) a += bface[bo4 + ci + (long long)nx * cj] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 1, 0) + ul(1, 1, 0));
-        if (bnd[c] & 32) a += bface[bo5 + ci + (long long)nx * cj] * (ul(0, 0, 1) + ul(1, 0, 1) + ul(0, 1, 1) + ul(1, 1, 1));
+        double ab = 0.0;
+        if (bnd[c] & 1) ab += bface[bo0 + cj + (long long)ny * ck] * (ul(0, 0, 0) + ul(0, 1, 0) + ul(0, 0, 1) + ul(0, 1, 1));
+        if (bnd[c] & 2) ab += bface[bo1 + cj + (long long)ny * ck] * (ul(1, 0, 0) + ul(1, 1, 0) + ul(1, 0, 1) + ul(1, 1, 1));
+        if (bnd[c] & 4) ab += bface[bo2 + ci + (long long)nx * ck] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 0, 1) + ul(1, 0, 1));
+        if (bnd[c] & 8) ab += bface[bo3 + ci + (long long)nx * ck] * (ul(0, 1, 0) + ul(1, 1, 0) + ul(0, 1, 1) + ul(1, 1, 1));
+        if (bnd[c] & 16) ab += bface[bo4 + ci + (long long)nx * cj] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 1, 0) + ul(1, 1, 0));
+        if (bnd[c] & 32) ab += bface[bo5 + ci + (long long)nx * cj] * (ul(0, 0, 1) + ul(1, 0, 1) + ul(0, 1, 1) + ul(1, 1, 1));
+        a += (float)ab;
       }
-      const double jv = sg[c] * a;
+      const float jv = sg[c] * a;
       acc[c] += w2 * jv * jv;
     }
   }
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
-    double v = acc[c];
+    double v = (double)acc[c];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp][c] = v;
