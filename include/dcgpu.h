@@ -75,7 +75,10 @@ int dc_set_rhs_block(dc_handle *h, int kb);
  * V-cycle input is the PCG residual scaled to unit norm per RHS and every
  * operation is done in fp32.  The preconditioner only steers the fp32 PCG,
  * which the fp64 refinement corrects, so this changes iteration counts, not
- * the accuracy the solve reaches.  The fp64 solve keeps fp64. */
+ * the accuracy the solve reaches.  The fp64 solve keeps fp64.  fp16 can
+ * overflow for extreme conductivity contrasts (e.g. 1e-8 S/m air cells); a
+ * dc_solve that breaks down with 16-bit storage is solved once more with
+ * fp32 storage (in the handle's own workspace when the caller's is too small). */
 #define DC_MG_FP32 0
 #define DC_MG_FP16 1
 #define DC_MG_BF16 2

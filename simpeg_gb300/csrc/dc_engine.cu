@@ -1112,6 +1112,9 @@ int dc_solve_workspace_bytes(dc_handle *h, int mode, int k, size_t *bytes) {
   return 0;
 }
 
+static int solve_once(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit,
+                      double inner_rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream);
+
 int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit, double inner_rtol,
              int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream) {
   if (!h || !b || !x || k < 1) return fail(DC_ERR_ARG, "bad argument");
@@ -1142,6 +1145,26 @@ int dc_solve(dc_handle *h, int mode, const double *b, double *x, int k, double r
   if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
   if (!(inner_rtol > 0.0)) inner_rtol = kInnerRtol;
   if (inner_maxit < 1) inner_maxit = 200;
+  int rc = solve_once(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, ws, ws_bytes, stats, stream);
+  if (rc == DC_ERR_BREAKDOWN && mode == DC_MODE_MIXED && h->mg_storage != DC_MG_FP32) {
+    // 16-bit multigrid vectors can overflow for extreme conductivity contrasts
+    // (e.g. 1e-8 S/m air cells): solve once more with fp32 multigrid storage,
+    // in the handle's own workspace when the caller's is too small for it.
+    const int keep = h->mg_storage;
+    h->mg_storage = DC_MG_FP32;
+    SolveWS w;
+    layout_ws(h, mode, k, nullptr, w);
+    const bool fits = ws && ws_bytes >= w.bytes;
+    rc = solve_once(h, mode, b, x, k, rtol, maxit, inner_rtol, inner_maxit, fits ? ws : nullptr, fits ? ws_bytes : 0,
+                    stats, stream);
+    h->mg_storage = keep;
+  }
+  return rc;
+}
+
+// One solve of k <= 1024 RHS (dc_solve without the chunking and the fp32 retry).
+static int solve_once(dc_handle *h, int mode, const double *b, double *x, int k, double rtol, int maxit,
+                      double inner_rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_stats *stats, void *stream) {
   cudaStream_t s = (cudaStream_t)stream;
   SolveWS w;
   layout_ws(h, mode, k, nullptr, w);

@@ -125,3 +125,30 @@ def test_staged_smoothing_matches_direct_loads(cuda, k):
     (xs, its), (xd, itd) = out[True], out[False]
     assert abs(its - itd) <= 1
     np.testing.assert_allclose(xs, xd, rtol=0, atol=1e-9 * np.abs(xd).max())
+
+
+def test_fp16_multigrid_overflow_falls_back_to_fp32(cuda):
+    """1e-8 S/m air cells overflow fp16 multigrid vectors; the solve retries
+    with fp32 storage and still reaches the tolerance and the direct solution."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = TensorMesh([[(5.0, 4, -1.3), (5.0, 16), (5.0, 4, 1.3)], [(5.0, 4, -1.3), (5.0, 16), (5.0, 4, 1.3)],
+                       [(5.0, 4, -1.3), (5.0, 10), (5.0, 4, 1.3)]], origin="CCN")
+    nx, ny, nz = mesh.shape_cells
+    s = np.full((nx, ny, nz), 1e-2)
+    s[:, :, -4:] = 1e-8
+    s[8:14, 8:14, 3:7] = 10.0
+    sigma = s.ravel(order="F")
+    A = _oracle(mesh, sigma).getA().tocsc()
+    rng = np.random.default_rng(4)
+    B = np.zeros((12, mesh.n_nodes))
+    B[np.arange(12), rng.integers(0, mesh.n_nodes, 12)] = 1.0
+    eng = DCEngine(mesh.h, robin_face_weights(mesh), coarse_max=64, mg_storage="fp16")
+    eng.set_model(torch.from_numpy(sigma).to(cuda))
+    X, info = eng.solve(torch.from_numpy(B).to(cuda), mode="mixed", rtol=1e-10)
+    assert info.status == 0 and info.max_rel_res <= 1e-10
+    X0 = spla.splu(A).solve(B.T).T
+    err = np.linalg.norm(X.cpu().numpy() - X0, axis=1) / np.linalg.norm(X0, axis=1)
+    assert err.max() < 1e-7, err.max()
