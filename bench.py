@@ -411,7 +411,7 @@ def run_gb300(args):
         "rel_err_vs_fp64_1e-13": err,
         "e2e": {"value": world * K * e2e_steps / e2e_s, "unit": "source-solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "path": "Simulation3DNodal.dpred(m): host model -> exp -> H2D -> set_model -> solve -> gather -> D2H"},
+                "path": "Simulation3DNodal.dpred(m): host model -> H2D -> exp map on device -> set_model -> solve -> gather -> D2H"},
         "roofline": {
             "kernel": "k_cheb_step<float,__half,*,32> (fine-level Chebyshev stencil step, fp16 multigrid storage)",
             "bound": "hbm",

@@ -33,6 +33,10 @@ class IdentityMap:
     def _transform(self, m):
         return np.asarray(m, dtype=np.float64).ravel()
 
+    def transform_dev(self, m):
+        """The map applied to a device (torch) model vector, elementwise."""
+        return m
+
     def diag_deriv(self, m):
         """Diagonal of d(map(m))/dm."""
         return np.ones(np.asarray(m).size)
@@ -69,6 +73,9 @@ class ExpMap(IdentityMap):
     def _transform(self, m):
         return np.exp(np.asarray(m, dtype=np.float64).ravel())
 
+    def transform_dev(self, m):
+        return m.exp()
+
     def diag_deriv(self, m):
         return np.exp(np.asarray(m, dtype=np.float64).ravel())
 
@@ -85,6 +92,9 @@ class ReciprocalMap(IdentityMap):
 
     def _transform(self, m):
         return 1.0 / np.asarray(m, dtype=np.float64).ravel()
+
+    def transform_dev(self, m):
+        return 1.0 / m
 
     def diag_deriv(self, m):
         m = np.asarray(m, dtype=np.float64).ravel()
@@ -114,6 +124,11 @@ class ComboMap(IdentityMap):
         for mp in reversed(self.maps):
             x = mp._transform(x)
         return x
+
+    def transform_dev(self, m):
+        for mp in reversed(self.maps):
+            m = mp.transform_dev(m)
+        return m
 
     def diag_deriv(self, m):
         x = np.asarray(m, dtype=np.float64).ravel()

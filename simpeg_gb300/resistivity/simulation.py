@@ -209,13 +209,23 @@ class Simulation3DNodal:
     # ------------------------------------------------------------ device state
     def _ensure_model(self):
         if self._sigma_dev is None:
-            s = self.sigma
-            if s.size != self.nC:
-                raise NotImplementedError(
-                    "Anisotropic conductivity is not supported for Robin boundary conditions")
-            if np.any(~np.isfinite(s)) or np.any(s <= 0):
-                raise ValueError("conductivity must be positive and finite")
-            self._sigma_dev = torch.from_numpy(np.ascontiguousarray(s)).to(self.device)
+            mp = self.sigmaMap
+            if (self._sigma is None and self._rho is None and self._model is not None and mp is not None
+                    and hasattr(mp, "transform_dev") and np.size(self._model) == self.nC):
+                # the model goes to the device once and is mapped there (elementwise maps)
+                m = torch.from_numpy(np.ascontiguousarray(self._model, dtype=np.float64).ravel()).to(self.device)
+                s = mp.transform_dev(m)
+                if not bool(((s > 0) & torch.isfinite(s)).all()):
+                    raise ValueError("conductivity must be positive and finite")
+                self._sigma_dev = s.contiguous()
+            else:
+                s = self.sigma
+                if s.size != self.nC:
+                    raise NotImplementedError(
+                        "Anisotropic conductivity is not supported for Robin boundary conditions")
+                if np.any(~np.isfinite(s)) or np.any(s <= 0):
+                    raise ValueError("conductivity must be positive and finite")
+                self._sigma_dev = torch.from_numpy(np.ascontiguousarray(s)).to(self.device)
             self.engine.set_model(self._sigma_dev)
         return self._sigma_dev
 
