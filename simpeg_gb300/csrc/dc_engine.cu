@@ -340,7 +340,7 @@ int build_hierarchy(dc_handle *h) {
   if ((rc = dalloc(&h->d_dense, nc2))) return rc;
   if ((rc = dalloc(&h->d_work, nc2))) return rc;
   if ((rc = dalloc(&h->d_flag, 1))) return rc;
-  if ((rc = dalloc(&h->d_lmax, 1))) return rc;
+  if ((rc = dalloc(&h->d_lmax, h->lv.size()))) return rc;  // one Gershgorin bound per level
   h->built = true;
   return 0;
 }
@@ -1058,16 +1058,18 @@ int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
   const long long nC = (long long)L0.nx * L0.ny * L0.nz;
   CK(cudaMemcpyAsync(L0.d_sigma, sigma_dev, sizeof(double) * nC, cudaMemcpyDeviceToDevice, s));
   for (size_t l = 0; l + 1 < h->lv.size(); ++l) coarsen_sigma(h->lv[l], h->lv[l + 1], s);
-  for (auto &L : h->lv) {
-    CK(cudaMemsetAsync(h->d_lmax, 0, sizeof(unsigned long long), s));
-    coef_build(L, h->robin, h->d_lmax, s);
-    unsigned long long bits = 0;
-    CK(cudaMemcpyAsync(&bits, h->d_lmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+  // coefficients of every level, then one read-back of the levels' Gershgorin bounds
+  const size_t nl = h->lv.size();
+  CK(cudaMemsetAsync(h->d_lmax, 0, sizeof(unsigned long long) * nl, s));
+  for (size_t l = 0; l < nl; ++l) coef_build(h->lv[l], h->robin, h->d_lmax + l, s);
+  std::vector<unsigned long long> bits(nl, 0);
+  CK(cudaMemcpyAsync(bits.data(), h->d_lmax, sizeof(unsigned long long) * nl, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (size_t l = 0; l < nl; ++l) {
     double lm;
-    std::memcpy(&lm, &bits, sizeof(lm));
+    std::memcpy(&lm, &bits[l], sizeof(lm));
     if (!(lm > 0.0) || !std::isfinite(lm)) return fail(DC_ERR_ARG, "conductivity must be positive and finite");
-    L.lmax = lm;
+    h->lv[l].lmax = lm;
   }
   if (!h->d_cdf_hi) {
     int rc;

@@ -185,3 +185,34 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, name), name
         assert ctypes.cast(getattr(L, name), ctypes.c_void_p).value
     assert declared == set(_lib.declared_symbols())
+
+
+def test_receiver_transpose_tables_equal_csr_transpose():
+    """PT (the adjoint scatter) built from sorted entries equals the CSR
+    transpose restricted to its nonzero rows."""
+    from simpeg_gb300.resistivity.electrodes import SurveyTables
+    from simpeg_gb300.workloads import block_model_survey
+
+    mesh, sigma, survey, _ = block_model_survey(seed=3)
+    t = SurveyTables(mesh, survey.source_list, mesh.n_nodes)
+    PT = t.P.T.tocsr()
+    PT.sum_duplicates()
+    nz = np.flatnonzero(np.diff(PT.indptr))
+    sub = PT[nz]
+    np.testing.assert_array_equal(t.PT_out, nz)
+    np.testing.assert_array_equal(t.PT_ptr, sub.indptr)
+    np.testing.assert_array_equal(t.PT_idx, sub.indices)
+    np.testing.assert_array_equal(t.PT_w, sub.data)
+
+
+def test_device_map_transforms_match_host():
+    """The elementwise device transforms of the maps equal their host transforms."""
+    import torch
+
+    from simpeg_gb300 import maps
+
+    rng = np.random.default_rng(0)
+    m = rng.uniform(0.1, 3.0, 50)
+    for mp in (maps.IdentityMap(nP=50), maps.ExpMap(nP=50), maps.ReciprocalMap(nP=50),
+               maps.ExpMap(nP=50) * maps.ReciprocalMap(nP=50)):
+        np.testing.assert_allclose(mp.transform_dev(torch.from_numpy(m)).numpy(), mp * m, rtol=1e-15)
