@@ -431,7 +431,8 @@ void carve_scal(Carve &c, int Kp, int gx, Scal &s) {
 struct SolveWS {
   int KB, nb, Kp, gx;
   double *B64, *X64, *R64;
-  float *d32, *r32, *p32, *q32;
+  float *d32, *r32, *q32;
+  void *pv;  // PCG search direction, multigrid storage type (the direction only steers the inner solve)
   void *zv;  // preconditioned vector, multigrid storage type
   double *p64, *q64, *z64;
   MGWork<float> mg32;
@@ -486,16 +487,18 @@ void layout_ws(const dc_handle *h, int mode, int k, char *base, SolveWS &w) {
   if (mode == DC_MODE_MIXED) {
     w.d32 = c.take<float>(n);
     w.r32 = c.take<float>(n);
-    w.p32 = c.take<float>(n);
     w.q32 = c.take<float>(n);
     w.storage = h->mg_storage;
     if (w.storage == DC_MG_FP16) {
+      w.pv = c.take<__half>(n);
       w.zv = c.take<__half>(n);
       carve_mg(c, h, w.Kp, w.mg16, true);
     } else if (w.storage == DC_MG_BF16) {
+      w.pv = c.take<__nv_bfloat16>(n);
       w.zv = c.take<__nv_bfloat16>(n);
       carve_mg(c, h, w.Kp, w.mgb16, true);
     } else {
+      w.pv = c.take<float>(n);
       w.zv = c.take<float>(n);
       carve_mg(c, h, w.Kp, w.mg32);
     }
@@ -658,7 +661,7 @@ int body_stream(dc_handle *h, int depth, cudaStream_t *out) {
 // `depth` selects the body stream of a LOOP_DEVICE loop (0 unless nested in a
 // refinement loop); total_max caps the iterations summed over sweeps.
 template <typename T, typename V, int KB>
-int pcg(dc_handle *h, T *x, T *r, T *p, T *q, V *z, const MGWork<V> &w, const Scal &sc, int nb, int gx,
+int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Scal &sc, int nb, int gx,
         const int *init_active, const double *tol2, int maxit, int total_max, int *iters, cudaStream_t s,
         int loop = LOOP_HOST, int depth = 0) {
   using O = Ops<T, V, KB>;
@@ -697,7 +700,7 @@ int pcg(dc_handle *h, T *x, T *r, T *p, T *q, V *z, const MGWork<V> &w, const Sc
   V *z1 = fused ? first_buffer(h, 0, z, w) : nullptr;
   // one PCG iteration on stream st
   auto iteration = [&](cudaStream_t st) {
-    O::apply(F, p, q, nb, sc.part_a, gx, st);
+    O::apply_v(F, p, q, nb, sc.part_a, gx, st);
     pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, sc.n_active, st);
     if (fused) {
       O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, c0, z1, scale, w.r0, st);
@@ -816,14 +819,14 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
       int rc;
       if (w.storage == DC_MG_FP16)
-        rc = pcg<float, __half, KB>(h, w.d32, w.r32, w.p32, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
+        rc = pcg<float, __half, KB>(h, w.d32, w.r32, (__half *)w.pv, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
                                     w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
       else if (w.storage == DC_MG_BF16)
-        rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, w.p32, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16, w.sc, nb,
+        rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, (__nv_bfloat16 *)w.pv, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16, w.sc, nb,
                                            gx, w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
                                            device ? 1 : 0);
       else
-        rc = pcg<float, float, KB>(h, w.d32, w.r32, w.p32, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
+        rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
       ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, so);

@@ -104,6 +104,8 @@ template <typename T, typename V, int KB> struct Ops {
   static int red_blocks_per_sm();
   // y = A x ; if partial: per-block partial sums of x.y
   static void apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
+  // q = A p with p stored as V (the PCG search direction), per-block partials of p.q
+  static void apply_v(const Level &L, const V *x, T *y, int nb, double *partial, int gx, cudaStream_t s);
   // res = r - A z
   static void residual(const Level &L, Rhs<T, V> r, const V *z, V *res, int nb, cudaStream_t s);
   // z = c0 D^-1 r (first Chebyshev step from zero)
@@ -122,16 +124,16 @@ template <typename T, typename V, int KB> struct Ops {
   static void coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V *zc, int nb, cudaStream_t s);
   // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = c0 D^-1 (scale r) on that level
   // and, when rv_out is set, rv_out = V(scale r).
-  static void update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
+  static void update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
                         double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
                         V *rv_out, cudaStream_t s);
   // rv_out = V(scale r)
   static void scale_to(long long N, int nb, const T *r, const float *scale, V *rv_out, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
   static void dot_z(long long N, int nb, const T *a, const V *b, double *partial, int gx, cudaStream_t s);
-  // p = z + beta p
-  static void p_update(long long N, int nb, T *p, const V *z, const double *beta, cudaStream_t s);
-  static void copy_z(long long N, int nb, T *dst, const V *src, cudaStream_t s);
+  // p = z + beta p (p and z in V)
+  static void p_update(long long N, int nb, V *p, const V *z, const double *beta, cudaStream_t s);
+  static void copy_z(long long N, int nb, V *dst, const V *src, cudaStream_t s);
 };
 
 template <int KB>

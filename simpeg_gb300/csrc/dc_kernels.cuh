@@ -249,12 +249,12 @@ __device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body
 }
 
 // ---------------------------------------------------------------- stencil ops
-// y = A x (PCG vectors, type T); with DOT also per-block partials of x.y.
-template <typename T, int KB, bool DOT>
-__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const T *__restrict__ x,
+// y = A x (y in T, x stored as S); with DOT also per-block partials of x.y.
+template <typename T, typename S, int KB, bool DOT>
+__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const S *__restrict__ x,
                                                T *__restrict__ y, Dims d, int nb, double *__restrict__ partial,
                                                int gs) {
-  constexpr int W = Lanes<T, KB>::W;
+  constexpr int W = Lanes<S, KB>::W;
   const auto *coef = coef_of<T, KB>(cf);
   auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv
 // Chebyshev step of the fine level on the new residual: z = c0 D^-1 (scale r).
 template <typename T, typename V, int KB, bool SMOOTH>
 __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict__ x, T *__restrict__ r,
-                                                   const T *__restrict__ p, const T *__restrict__ qv,
+                                                   const V *__restrict__ p, const T *__restrict__ qv,
                                                    const double *__restrict__ alpha, double *__restrict__ partial,
                                                    const T *__restrict__ invd, V *__restrict__ z, T c0,
                                                    const float *__restrict__ scale, V *__restrict__ rv_out, int gs) {
@@ -722,9 +722,9 @@ __global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict
   });
 }
 
-// p = z + beta p
+// p = z + beta p (p stored as V, like z)
 template <typename T, typename V, int KB>
-__global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, T *__restrict__ p, const V *__restrict__ z,
+__global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, V *__restrict__ p, const V *__restrict__ z,
                                                   const double *__restrict__ beta) {
   SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
     SWEEP_INDEX(d.N, d.mn)
@@ -733,15 +733,6 @@ __global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, T *__restrict_
 #pragma unroll
     for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + (T)beta[b * KB + q * W + e] * pv.a[e];
     st<T, W>(p + t, pv);
-  }
-}
-
-// p = z (type conversion copy)
-template <typename T, typename V, int KB>
-__global__ void __launch_bounds__(TPB) k_copy_z(Dims d, int nb, T *__restrict__ p, const V *__restrict__ z) {
-  SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
-    SWEEP_INDEX(d.N, d.mn)
-    st<T, W>(p + t, ld<T, W>(z + t));
   }
 }
 
@@ -816,16 +807,23 @@ XferTab make_tab(const Level &f) {
 template <typename T, typename V, int KB>
 void Ops<T, V, KB>::apply(const Level &L, const T *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
   if (partial)
-    k_apply<T, KB, true><<<RED_GRID(L.dims.N, (k_apply<T, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+    k_apply<T, T, KB, true><<<RED_GRID(L.dims.N, (k_apply<T, T, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
         coef_ptr<T>(L), x, y, L.dims, nb, partial, gx);
   else
-    k_apply<T, KB, false><<<GRID_KL(L.dims.N, (k_apply<T, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
+    k_apply<T, T, KB, false><<<GRID_KL(L.dims.N, (k_apply<T, T, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
         coef_ptr<T>(L), x, y, L.dims, nb, nullptr, 0);
 }
 
 template <typename T, typename V, int KB>
+void Ops<T, V, KB>::apply_v(const Level &L, const V *x, T *y, int nb, double *partial, int gx, cudaStream_t s) {
+  k_apply<T, V, KB, true><<<RED_GRID(L.dims.N, (k_apply<T, V, KB, true>), (Lanes<V, KB>::LPN)), TPB, 0, s>>>(
+      coef_ptr<T>(L), x, y, L.dims, nb, partial, gx);
+}
+
+template <typename T, typename V, int KB>
 int Ops<T, V, KB>::red_blocks_per_sm() {
-  int m = resident_blocks((const void *)k_apply<T, KB, true>);
+  int m = resident_blocks((const void *)k_apply<T, T, KB, true>);
+  m = std::max(m, resident_blocks((const void *)k_apply<T, V, KB, true>));
   m = std::max(m, resident_blocks((const void *)k_cheb_step<T, V, T, KB, true, 1>));
   m = std::max(m, resident_blocks((const void *)k_cheb_step<T, V, V, KB, true, 1>));
   m = std::max(m, resident_blocks((const void *)k_update_xr<T, V, KB, true>));
@@ -973,7 +971,7 @@ void Ops<T, V, KB>::coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V 
 }
 
 template <typename T, typename V, int KB>
-void Ops<T, V, KB>::update_xr(long long N, int nb, T *x, T *r, const T *p, const T *q, const double *alpha,
+void Ops<T, V, KB>::update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
                               double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
                               V *rv_out, cudaStream_t s) {
   const Dims dd = flat_dims(N);
@@ -1003,16 +1001,13 @@ void Ops<T, V, KB>::dot_z(long long N, int nb, const T *a, const V *b, double *p
 }
 
 template <typename T, typename V, int KB>
-void Ops<T, V, KB>::p_update(long long N, int nb, T *p, const V *z, const double *beta, cudaStream_t s) {
+void Ops<T, V, KB>::p_update(long long N, int nb, V *p, const V *z, const double *beta, cudaStream_t s) {
   k_p_update<T, V, KB><<<GRID_K(N, (k_p_update<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z, beta);
 }
 
 template <typename T, typename V, int KB>
-void Ops<T, V, KB>::copy_z(long long N, int nb, T *dst, const V *src, cudaStream_t s) {
-  if (std::is_same<T, V>::value)
-    cudaMemcpyAsync(dst, src, sizeof(T) * N * KB * nb, cudaMemcpyDeviceToDevice, s);
-  else
-    k_copy_z<T, V, KB><<<GRID_K(N, (k_copy_z<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, dst, src);
+void Ops<T, V, KB>::copy_z(long long N, int nb, V *dst, const V *src, cudaStream_t s) {
+  cudaMemcpyAsync(dst, src, sizeof(V) * N * KB * nb, cudaMemcpyDeviceToDevice, s);
 }
 
 #define DC_OPS_INSTANTIATE(T, V)                                                                            \

@@ -173,6 +173,26 @@ class DCEngine:
             check(rc)
         return x.reshape(b.shape), info
 
+    def solve_fixed(self, b, n_inner, n_outer, mode="mixed", rtol=1e-9, ws=None):
+        """Fixed-iteration solve (n_outer refinement sweeps of n_inner PCG iterations) with no host
+        synchronisation, so that it can be recorded into a CUDA graph; RHS that converge earlier are
+        frozen.  Returns (x, ws); ``check_fixed(ws, k, mode)`` reads the convergence state."""
+        b = _dev64(b, None, "b")
+        b2 = b.reshape(-1, self.nN)
+        k = b2.shape[0]
+        x = torch.empty_like(b2)
+        if ws is None:
+            ws = torch.empty(self.workspace_bytes(k, mode), dtype=torch.uint8, device=b.device)
+        check(lib().dc_solve_fixed(self._h, MODES[mode], _ptr(b2), _ptr(x), k, float(rtol), int(n_inner),
+                                   int(n_outer), _ptr(ws), ws.numel(), _stream()))
+        return x.reshape(b.shape), ws
+
+    def check_fixed(self, ws, k, mode="mixed"):
+        """(max relative residual, RHS above rtol) left in ws by solve_fixed."""
+        mr, na = C.c_double(), C.c_int()
+        check(lib().dc_solve_check(self._h, MODES[mode], int(k), _ptr(ws), C.byref(mr), C.byref(na), None, None))
+        return mr.value, na.value
+
     def stencil_timing(self, enable):
         """Start (True) or stop (False) event timing of the fine-level fp32 stencil launches.
 

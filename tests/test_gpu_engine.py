@@ -152,3 +152,25 @@ def test_fp16_multigrid_overflow_falls_back_to_fp32(cuda):
     X0 = spla.splu(A).solve(B.T).T
     err = np.linalg.norm(X.cpu().numpy() - X0, axis=1) / np.linalg.norm(X0, axis=1)
     assert err.max() < 1e-7, err.max()
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_fixed_iteration_solve_equals_adaptive(cuda, mode):
+    """With at least the adaptive solve's sweeps and iterations, the
+    fixed-iteration (graph-recordable) solve returns the same bits: converged
+    RHS are frozen, so the extra iterations change nothing."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = _mesh("padded")
+    sigma = _sigma(mesh, seed=9)
+    eng = DCEngine(mesh.h, robin_face_weights(mesh), coarse_max=64)
+    eng.set_model(torch.from_numpy(sigma).to(cuda))
+    rng = np.random.default_rng(6)
+    B = torch.from_numpy(rng.standard_normal((20, mesh.n_nodes))).to(cuda)
+    X, info = eng.solve(B, mode=mode, rtol=1e-10)
+    Xf, ws = eng.solve_fixed(B, n_inner=info.iterations + 5, n_outer=info.outer + 1, mode=mode, rtol=1e-10)
+    mr, na = eng.check_fixed(ws, 20, mode)
+    assert na == 0 and mr <= 1e-10
+    torch.testing.assert_close(Xf, X, rtol=0, atol=0)
