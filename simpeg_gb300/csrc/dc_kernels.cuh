@@ -902,12 +902,13 @@ bool Ops<T, V, KB>::cheb_bulk(const Level &L, const V *r, const V *zin, V *zout,
     return false;
   } else {
     if (!status) return false;
-    static int max_smem = -1;
-    if (max_smem < 0) {
-      int dev = 0;
+    // function-local statics: initialised once, thread-safe (server worker threads solve concurrently)
+    static const int max_smem = [] {
+      int dev = 0, v = 0;
       cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    }
+      cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      return v;
+    }();
     const size_t budget = (size_t)max_smem;
     // slab height and copy depth: the forced pair if given, else the first that fits
     int TY = 0, NA = 0;
@@ -922,17 +923,15 @@ bool Ops<T, V, KB>::cheb_bulk(const Level &L, const V *r, const V *zin, V *zout,
     }
     if (TY == 0) return false;
     const size_t smem = cheb_bulk_smem(L.dims.Nx, KB, sizeof(V), TY, NA, prev == 1);
-    // the shared-memory limit is raised once per kernel, outside any stream capture
-    static bool configured = false, usable = false;
-    if (!configured) {
-      usable = true;
+    // the shared-memory limit is raised once per kernel
+    static const bool usable = [budget] {
+      bool ok = true;
       for (const void *kern : {(const void *)k_cheb_bulk<T, V, KB, 0>, (const void *)k_cheb_bulk<T, V, KB, 1>,
                                (const void *)k_cheb_bulk<T, V, KB, 2>})
-        usable = usable && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget) ==
-                               cudaSuccess;
-      if (!usable) cudaGetLastError();
-      configured = true;
-    }
+        ok = ok && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget) == cudaSuccess;
+      if (!ok) cudaGetLastError();
+      return ok;
+    }();
     if (!usable) return false;
     const dim3 grid(count_launch(dim3((unsigned)(nb * ((L.dims.Ny + TY - 1) / TY)))));
     if (prev == 1)
