@@ -521,6 +521,18 @@ def run_gauss_newton(args):
     del truth
     torch.cuda.empty_cache()
     beta = 10.0
+    # untimed warm-up: one step of a 16x16x8-core problem per precision, so that first-call costs of
+    # the process (module loading of every kernel the step uses, torch's and this library's) are
+    # paid before either timed step, not by whichever precision runs first
+    wmesh, _, wm0, wsurvey = workloads.gauss_newton(seed=4, n_lines=2, src_per_line=4, n_rx=4, ncore_xy=16,
+                                                     ncore_z=8)
+    for precision in ("mixed", "fp64"):
+        wsim = Simulation3DNodal(wmesh, survey=wsurvey, sigmaMap=maps.ExpMap(wmesh), precision=precision,
+                                 rtol=RTOL)
+        inexact_gauss_newton_direction(L2DataMisfit(wsim, np.zeros(wsurvey.nD)), WeightedLeastSquares(wmesh, wsim),
+                                       beta, wm0, cg_maxiter=2)
+        del wsim
+    torch.cuda.synchronize()
     out = {"metric": "Gauss-Newton step (getJtJdiag + gradient + 10 CG iterations): mixed vs fp64",
            "workload": "dc3d_gauss_newton",
            "config": {"mesh_cells": list(mesh.shape_cells), "nodes": int(mesh.n_nodes), "sources": survey.nSrc,
