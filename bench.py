@@ -346,13 +346,17 @@ def run_gb300(args):
     ms_fp64, (U64, info64) = timed(lambda: fwd("fp64"), args.steps)
     ms_jt_fp64, _ = timed(lambda: jtvec("fp64", U64), args.steps)
 
-    # ---- accuracy against an fp64 solve at 1e-13 (the oracle at this size)
-    U_ref, _ = eng.solve(Q, mode="fp64", rtol=1e-13)
+    # ---- accuracy against an fp64 solve at 1e-13 (the oracle at this size).  1e-13 is at the
+    # rounding floor of the fp64 residual on this mesh: a solve that stops within 5e-13 is accepted.
+    U_ref, info_ref = eng.solve(Q, mode="fp64", rtol=1e-13, raise_on_fail=False)
     csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U_ref.view(-1), d_out)
     d_ref = d_out.cpu().numpy()
     PTv = torch.zeros(K, mesh.n_nodes, dtype=torch.float64, device=dev)
     csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], v_dev, PTv.view(-1), out_idx=tq["PT_out"])
-    Lam_ref, _ = eng.solve(PTv, mode="fp64", rtol=1e-13)
+    Lam_ref, info_lam = eng.solve(PTv, mode="fp64", rtol=1e-13, raise_on_fail=False)
+    oracle_res = max(info_ref.max_rel_res, info_lam.max_rel_res)
+    if not oracle_res <= 5e-13:
+        raise RuntimeError(f"fp64 oracle solve stopped at relative residual {oracle_res:.2e}")
     g_ref = eng.dadm_adj(U_ref, Lam_ref, None, scale=-1.0).cpu().numpy()
     del Lam_ref, PTv
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
@@ -409,6 +413,7 @@ def run_gb300(args):
         "mixed_solve": {"inner_iterations": info_mixed.iterations, "outer": info_mixed.outer,
                         "max_rel_res": info_mixed.max_rel_res, "levels": info_mixed.n_levels},
         "rel_err_vs_fp64_1e-13": err,
+        "oracle_max_rel_res": oracle_res,
         "e2e": {"value": world * K * e2e_steps / e2e_s, "unit": "source-solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "Simulation3DNodal.dpred(m): host model -> H2D -> exp map on device -> set_model -> solve -> gather -> D2H"},
@@ -442,7 +447,7 @@ def run_differentiation(args):
 
     Gradient of the L2 data misfit by the autograd backward (adjoint solve +
     dA/dsigma kernel), checked against central finite differences (step 1e-4)
-    on random unit directions, and against an fp64 Jtvec at rtol 1e-13 (the
+    on random unit directions, and against an fp64 Jtvec at rtol 5e-13 (the
     oracle at this size); run in fp64 and in mixed precision with forward
     recomputation.  Prints one JSON line.
     """
@@ -456,7 +461,8 @@ def run_differentiation(args):
     torch.cuda.set_device(0)
     mesh, m, survey = workloads.differentiation(seed=2)
     rng = np.random.default_rng(11)
-    ref = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="fp64", rtol=1e-13)
+    # fp64 reference at 5e-13 (a 1e-13 target sits at the fp64 residual's rounding floor on this mesh)
+    ref = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="fp64", rtol=5e-13)
     d_true = ref.dpred(m)
     dobs = torch.from_numpy(d_true * (1 + 0.03 * rng.standard_normal(d_true.size)))
     m0 = m + 0.1 * rng.standard_normal(m.size)

@@ -65,6 +65,19 @@ const char *dc_last_error(void);
 /* Smoother / hierarchy parameters (before dc_set_model).  Non-positive values keep defaults. */
 int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int coarse_max, int check_every);
 
+/* Multigrid coarsening (before the first dc_set_model).  merge = 0: full
+ * coarsening, every axis halved at every level.  merge in [1, 16]: selective
+ * coarsening -- per axis, adjacent cells are merged in pairs only while their
+ * combined width is at most merge x twice the narrowest cell of the level,
+ * narrowest pairs first, so stretched padding cells stay unmerged while the
+ * finer cells are coarsened (bounded coarse-cell aspect ratios, fewer PCG
+ * iterations on padded meshes).  A level that would lose under 10 % of its
+ * nodes that way is coarsened fully (on a padded mesh: every level below the
+ * first).  Default 1 (on a uniform mesh identical to full
+ * coarsening).  Solver option of the reference's solver_opts
+ * (simpeg/base/pde_simulation.py:493-511); no reference counterpart of its own. */
+int dc_set_coarsening(dc_handle *h, double merge);
+
 /* RHS-block width of the solver's interleaved layout: 1, 2, 4, 8, 16 or 32
  * lanes per node (0 = automatic: the widest that pads at most 1/8 of the
  * lanes).  Set by the autotuner. */

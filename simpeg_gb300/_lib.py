@@ -57,6 +57,7 @@ _SIG = {
     "dc_last_error": (C.c_char_p, []),
     "dc_set_params": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
     "dc_set_rhs_block": (C.c_int, [_VP, C.c_int]),
+    "dc_set_coarsening": (C.c_int, [_VP, C.c_double]),
     "dc_set_mg_storage": (C.c_int, [_VP, C.c_int]),
     "dc_set_smoother": (C.c_int, [_VP, C.c_int]),
     "dc_set_staging": (C.c_int, [_VP, C.c_int]),

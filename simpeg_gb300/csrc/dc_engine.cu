@@ -49,17 +49,37 @@ int upload(T **p, const std::vector<T> &v) {
   return 0;
 }
 
-// Coarse node set of one axis: every second fine node, plus the last one
-// (an odd cell count leaves one single-cell coarse cell at the end).
-Axis1D make_axis(const std::vector<double> &h, bool coarsen) {
+// Coarse node set of one axis.  Every coarse cell covers one or two adjacent
+// fine cells.  With wmax <= 0, every second fine node is kept, plus the last
+// one (full coarsening; an odd cell count leaves one single-cell coarse cell at
+// the end).  With wmax > 0, pairs of adjacent cells whose combined width is at
+// most wmax are merged, narrowest pairs first (ties: lower index first), and
+// every other cell stays a single-cell coarse cell: stretched padding cells
+// are left alone until the rest of the mesh has grown to their width, which
+// keeps the coarse cells' aspect ratios bounded (a geometric form of
+// semi-coarsening for the point smoother).
+Axis1D make_axis(const std::vector<double> &h, bool coarsen, double wmax) {
   Axis1D a;
   const int n = (int)h.size();
   a.nf = n + 1;
   std::vector<double> x(n + 1, 0.0);
   for (int i = 0; i < n; ++i) x[i + 1] = x[i] + h[i];
-  if (coarsen) {
+  if (coarsen && wmax <= 0.0) {
     for (int i = 0; i <= n; i += 2) a.r_fi.push_back(i);
     if (a.r_fi.back() != n) a.r_fi.push_back(n);
+  } else if (coarsen) {
+    std::vector<int> cand;
+    for (int i = 0; i + 1 < n; ++i)
+      if (h[i] + h[i + 1] <= wmax) cand.push_back(i);
+    std::stable_sort(cand.begin(), cand.end(), [&](int p, int q) { return h[p] + h[p + 1] < h[q] + h[q + 1]; });
+    std::vector<char> used(n, 0), starts(n, 0);
+    for (int i : cand)
+      if (!used[i] && !used[i + 1]) {
+        used[i] = used[i + 1] = 1;
+        starts[i] = 1;
+      }
+    for (int i = 0; i < n; i += starts[i] ? 2 : 1) a.r_fi.push_back(i);
+    a.r_fi.push_back(n);
   } else {
     for (int i = 0; i <= n; ++i) a.r_fi.push_back(i);
   }
@@ -223,6 +243,7 @@ struct dc_handle {
   int nu_pre = 3, nu_post = 3;
   double cheb_ratio = 30.0;
   int coarse_max = 200;
+  double coarsen_merge = 1.0;  // selective coarsening factor (dc_set_coarsening); 0 = full coarsening
   int check_every = 1;
   int mg_storage = DC_MG_FP16;  // mixed solve: storage of the multigrid vectors (dc_set_mg_storage)
   int smoother_kind = 1;  // Chebyshev polynomials of the first or fourth kind (dc_set_smoother)
@@ -280,7 +301,20 @@ int build_hierarchy(dc_handle *h) {
     if (!cz[0] && !cz[1] && !cz[2]) break;
     Level C;
     const std::vector<double> *hs[3] = {&L.hx, &L.hy, &L.hz};
-    for (int a = 0; a < 3; ++a) L.ax[a] = make_axis(*hs[a], cz[a]);
+    // selective coarsening: merge pairs up to coarsen_merge x twice the narrowest cell of the level.
+    // Once a narrow padding cell is left unmerged, the next levels lose under 10 % of their nodes
+    // this way and are coarsened fully: the selection acts where the fine cells are most anisotropic.
+    double wmax = 0.0;
+    if (h->coarsen_merge > 0.0) {
+      double hmin = INFINITY;
+      for (int a = 0; a < 3; ++a)
+        for (double w : *hs[a]) hmin = std::min(hmin, w);
+      wmax = h->coarsen_merge * 2.0 * hmin * (1.0 + 1e-9);  // widths equal up to rounding still merge
+      long long nc = 1;
+      for (int a = 0; a < 3; ++a) nc *= (long long)make_axis(*hs[a], cz[a], wmax).nc;
+      if (nc * 10 > L.dims.N * 9) wmax = 0.0;  // under 10 % fewer nodes: coarsen every axis fully instead
+    }
+    for (int a = 0; a < 3; ++a) L.ax[a] = make_axis(*hs[a], cz[a], wmax);
     C.hx = coarse_widths(L.hx, L.ax[0]);
     C.hy = coarse_widths(L.hy, L.ax[1]);
     C.hz = coarse_widths(L.hz, L.ax[2]);
@@ -1003,6 +1037,16 @@ int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int 
     h->coarse_max = coarse_max;
   }
   if (check_every > 0) h->check_every = check_every;
+  return 0;
+}
+
+int dc_set_coarsening(dc_handle *h, double merge) {
+  if (!h) return fail(DC_ERR_ARG, "handle is NULL");
+  if (!(merge == 0.0 || (merge >= 1.0 && merge <= 16.0)))
+    return fail(DC_ERR_ARG, "coarsening factor must be 0 (full coarsening) or in [1, 16]");
+  if (h->built && merge != h->coarsen_merge)
+    return fail(DC_ERR_STATE, "the coarsening must be set before the first dc_set_model");
+  h->coarsen_merge = merge;
   return 0;
 }
 

@@ -59,10 +59,12 @@ class DCEngine:
     ----------
     h : three arrays of cell widths (nx, ny, nz)
     bface : packed Robin face weights (``boundary.robin_face_weights``) or None (Neumann)
+    coarsening : selective coarsening factor of the multigrid hierarchy (``dc_set_coarsening``;
+        0 = halve every axis at every level)
     """
 
     def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1,
-                 mg_storage="fp16", smoother=1):
+                 mg_storage="fp16", smoother=1, coarsening=1.0):
         if not torch.cuda.is_available():
             raise RuntimeError("the DC engine needs a CUDA device")
         L = lib()
@@ -84,6 +86,7 @@ class DCEngine:
         check(L.dc_set_params(self._h, nu_pre, nu_post, cheb_ratio, coarse_max, check_every))
         check(L.dc_set_mg_storage(self._h, MG_STORAGE[mg_storage]))
         check(L.dc_set_smoother(self._h, int(smoother)))
+        check(L.dc_set_coarsening(self._h, float(coarsening)))
         self.robin = bface is not None
         self._ws = {}
         self._model_set = False
@@ -108,6 +111,10 @@ class DCEngine:
         """Force the RHS-block width (1..32 lanes per node; 0 = automatic)."""
         check(lib().dc_set_rhs_block(self._h, int(kb)))
         self._ws.clear()
+
+    def set_coarsening(self, merge):
+        """Selective coarsening factor (0 = full coarsening); before the first set_model."""
+        check(lib().dc_set_coarsening(self._h, float(merge)))
 
     def set_mg_storage(self, storage):
         """Multigrid vector storage of the mixed solve: "fp16" (default), "bf16" or "fp32"."""

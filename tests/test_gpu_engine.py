@@ -78,6 +78,90 @@ def test_solve_matches_direct(cuda, kind, mode, k):
     assert err.max() < 1e-8, (err.max(), info)
 
 
+def _coarse_shapes(h, merge, coarse_max):
+    """Cell counts per level under the rule of dc_set_coarsening, restated on the host."""
+    hs = [np.asarray(w, dtype=np.float64) for w in h]
+    shapes = []
+    while True:
+        shapes.append(tuple(w.size for w in hs))
+        N = int(np.prod([w.size + 1 for w in hs]))
+        cz = [w.size >= 4 for w in hs]
+        if N <= coarse_max or not any(cz):
+            return shapes
+
+        def starts(w, c, wmax):
+            n = w.size
+            if not c:
+                return list(range(n + 1))
+            if wmax <= 0:
+                fi = list(range(0, n + 1, 2))
+                return fi if fi[-1] == n else fi + [n]
+            pairs = sorted((i for i in range(n - 1) if w[i] + w[i + 1] <= wmax), key=lambda i: w[i] + w[i + 1])
+            used, first = np.zeros(n, bool), np.zeros(n, bool)
+            for i in pairs:
+                if not used[i] and not used[i + 1]:
+                    used[i] = used[i + 1] = first[i] = True
+            fi, i = [], 0
+            while i < n:
+                fi.append(i)
+                i += 2 if first[i] else 1
+            return fi + [n]
+
+        wmax = 0.0
+        if merge > 0:
+            wmax = merge * 2.0 * min(w.min() for w in hs) * (1 + 1e-9)
+            if np.prod([len(starts(w, c, wmax)) for w, c in zip(hs, cz)]) * 10 > N * 9:
+                wmax = 0.0
+        new = []
+        for w, c in zip(hs, cz):
+            fi = starts(w, c, wmax)
+            new.append(np.array([w[fi[I]:fi[I + 1]].sum() for I in range(len(fi) - 1)]))
+        hs = new
+
+
+@pytest.mark.parametrize("kind", ["uniform", "padded", "odd", "anisotropic"])
+@pytest.mark.parametrize("merge", [0.0, 1.0, 1.5])
+def test_coarsening_hierarchy_follows_rule(cuda, kind, merge):
+    """Level shapes of full (merge 0) and selective coarsening equal the
+    documented rule; on a uniform mesh both are the same hierarchy."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = _mesh(kind) if kind != "anisotropic" else \
+        TensorMesh([[(20.0, 12)], [(10.0, 16)], [(5.0, 24)]], origin="CCN")
+    eng = DCEngine(mesh.h, robin_face_weights(mesh), coarse_max=64, coarsening=merge)
+    eng.set_model(torch.from_numpy(_sigma(mesh)).to(cuda))
+    got = [cells for cells, _ in eng.levels()]
+    assert got == _coarse_shapes(mesh.h, merge, 64), (kind, merge, got)
+    if kind == "uniform":
+        assert got == _coarse_shapes(mesh.h, 0.0, 64)
+
+
+def test_selective_coarsening_same_solution_fewer_iterations(cuda):
+    """On a padded mesh (1.3x stretched padding) selective coarsening reaches
+    the same fp64 residual and solution in fewer PCG iterations."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = TensorMesh([[(5.0, 8, -1.3), (5.0, 32), (5.0, 8, 1.3)], [(5.0, 8, -1.3), (5.0, 32), (5.0, 8, 1.3)],
+                       [(5.0, 8, -1.3), (5.0, 24)]], origin="CCN")
+    sigma = _sigma(mesh, seed=5)
+    rng = np.random.default_rng(6)
+    B = torch.from_numpy(rng.standard_normal((16, mesh.n_nodes))).to(cuda)
+    out = {}
+    for merge in (0.0, 1.0):
+        eng = DCEngine(mesh.h, robin_face_weights(mesh), coarsening=merge)
+        eng.set_model(torch.from_numpy(sigma).to(cuda))
+        X, info = eng.solve(B, mode="mixed", rtol=1e-10)
+        assert info.status == 0 and info.max_rel_res <= 1e-10
+        out[merge] = (X.cpu().numpy(), info.iterations)
+    (X0, it0), (X1, it1) = out[0.0], out[1.0]
+    assert np.linalg.norm(X1 - X0) / np.linalg.norm(X0) < 1e-8
+    assert it1 < it0, (it0, it1)
+
+
 @pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
 @pytest.mark.parametrize("k", [3, 32, 40])
 def test_mixed_solve_every_multigrid_storage(cuda, storage, k):
