@@ -255,6 +255,24 @@ int dc_dadm_adj_noalloc(int nx, int ny, int nz, const double *h_dev, const doubl
 
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */
+/* Derived fields of Fields3DNodal (simpeg/electromagnetics/static/resistivity/
+ * fields.py:186-257) for k nodal potentials phi (column-major (N, k)), on the
+ * edges ordered as discretize orders them (all x-edges, then y-, then z-edges,
+ * each Fortran-ordered; column-major (nE, k)):
+ *   e = -G phi  (Fields3DNodal._e, fields.py:227-236)
+ *   j = MeI MeSigma e  (fields.py:214-225; the edge inner products are diagonal
+ *       on a tensor mesh: j = e * sum_c sigma_c V_c / sum_c V_c over the cells
+ *       holding the edge; uses the conductivity of dc_set_model).
+ * Either output may be NULL.  Needs dc_set_model. */
+int dc_edge_fields(dc_handle *h, const double *phi, int k, double *e, double *j, void *stream);
+
+/* charge = -eps0 G^T Me(1) e at the nodes ((N, k); fields.py:238-248) and
+ * charge_density = average of the cell's 8 node charges / V ((nC, k) or NULL;
+ * fields.py:250-253), from the edge field e ((nE, k)).  eps0 is the vacuum
+ * permittivity in F/m (the reference uses scipy.constants.epsilon_0). */
+int dc_node_charge(dc_handle *h, const double *e, int k, double eps0, double *charge, double *charge_density,
+                   void *stream);
+
 long long dc_kernel_launches(void);
 
 /* Event timing of the fine-level fp32 Chebyshev/stencil launches of h.

@@ -13,6 +13,8 @@ Follows, function by function:
 * ``Jvec``                   ``simulation.py:156-187``
 * ``Jtvec`` / ``_Jtvec``     ``simulation.py:189-263``
 * ``getJ``/``getJtJdiag``    ``simulation.py:115-121,137-154``
+* ``Fields3DNodal`` e, j, charge, charge_density
+                             ``resistivity/fields.py:214-253``
 
 The per-source loops are vectorised over sources (one multi-RHS solve), which
 changes only the floating-point summation order.  ``solver="cg"`` swaps the
@@ -239,6 +241,19 @@ class OracleDC3DNodal:
             start += k
         lam = self._solve(ptv)
         return -self.getADeriv(f, lam, adjoint=True)
+
+    def derived_fields(self, phi, eps0):
+        """e = -G phi, j = MeI MeSigma e, charge = -eps0 G^T Me(1) e, charge_density =
+        aveN2CC charge / V (``fields.py:214-253``) for phi (nN,) or (nN, k)."""
+        E1 = self.E @ np.ones(self.ops.nC)
+        e = -(self.G @ phi)
+        ratio = (self.E @ self.sigma) / E1
+        j = e * (ratio[:, None] if e.ndim == 2 else ratio)
+        me1e = e * (E1[:, None] if e.ndim == 2 else E1)
+        charge = -eps0 * (self.G.T @ me1e)
+        vol = self.ops.vol
+        dens = (self.ops.average_node_to_cell() @ charge) / (vol[:, None] if charge.ndim == 2 else vol)
+        return e, j, charge, dens
 
     def getJ(self, m, f=None):
         """Full J (nD, nP): one adjoint solve per datum (``_Jtvec(v=None)``)."""

@@ -94,6 +94,15 @@ class MeshOps:
         Ez = _kron3(sp.eye(nz), _adj(ny), _adj(nx))
         return (sp.vstack([Ex, Ey, Ez], format="csr") @ sp.diags(self.vol / 4.0)).tocsr()
 
+    def average_node_to_cell(self):
+        """(nC, nN): the mean of each cell's 8 corner nodes (discretize ``aveN2CC`` on a tensor mesh)."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+
+        def av(n):
+            return sp.diags([0.5, 0.5], [0, 1], shape=(n, n + 1))
+
+        return _kron3(av(nz), av(ny), av(nx)).tocsr()
+
     # ---- boundary ------------------------------------------------------
     def boundary_faces(self):
         """Centres, outward normals, areas, adjacent cell and 4 nodes of every boundary face."""

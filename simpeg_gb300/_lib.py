@@ -58,6 +58,8 @@ _SIG = {
     "dc_set_params": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
     "dc_set_rhs_block": (C.c_int, [_VP, C.c_int]),
     "dc_set_coarsening": (C.c_int, [_VP, C.c_double]),
+    "dc_edge_fields": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP, _VP]),
+    "dc_node_charge": (C.c_int, [_VP, _VP, C.c_int, C.c_double, _VP, _VP, _VP]),
     "dc_set_mg_storage": (C.c_int, [_VP, C.c_int]),
     "dc_set_smoother": (C.c_int, [_VP, C.c_int]),
     "dc_set_staging": (C.c_int, [_VP, C.c_int]),

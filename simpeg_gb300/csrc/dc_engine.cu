@@ -840,14 +840,13 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     // Refinement in double-float: b and x as (hi, lo) fp32 pairs in the B64-sized regions R64 and X64.
     float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
     float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
-    split_df(w.B64, (long long)N * Kp, bh, bl, s);
-    // |b|^2, initial outer flags, r32 = b
+    split_df(w.B64, (long long)N * Kp, bh, bl, w.r32, s);  // also r32 = fp32(b), the first residual
+    // |b|^2, initial outer flags
     Ops<double, double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
                 inner_rtol * inner_rtol, kSafety2, s);
-    convert_d2f(w.B64, (long long)N * Kp, w.r32, s);
     // one refinement sweep on stream so: inner fp32 PCG, accumulate, fp64 residual, new flags
     auto sweep = [&](cudaStream_t so, int inner_cap, int *it) -> int {
       CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
@@ -1421,6 +1420,24 @@ int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const d
   const Level &L0 = h->lv[0];
   edge_products(u, lam, k, L0.dims, h->d_P, h->d_Q, s);
   cell_gradient(L0, h->robin, h->d_P, h->d_Q, dsig, scale, g, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_edge_fields(dc_handle *h, const double *phi, int k, double *e, double *j, void *stream) {
+  if (!h || !phi || k < 1 || (!e && !j)) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  edge_fields(h->lv[0], phi, k, e, j, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_node_charge(dc_handle *h, const double *e, int k, double eps0, double *charge, double *charge_density,
+                   void *stream) {
+  if (!h || !e || k < 1 || !charge)
+    return fail(DC_ERR_ARG, "bad argument (charge is required: the density is computed from it)");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  node_charge(h->lv[0], e, k, eps0, charge, charge_density, (cudaStream_t)stream);
   CK(cudaGetLastError());
   return 0;
 }

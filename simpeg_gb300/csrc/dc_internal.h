@@ -143,7 +143,7 @@ template <int KB>
 int ir_blocks_per_sm();
 // Double-float (fp32 pair) refinement of the mixed solve: hi/lo splits of fp64
 // vectors and coefficients, b - A x and x += d in double-float arithmetic.
-void split_df(const double *a, long long n, float *hi, float *lo, cudaStream_t s);
+void split_df(const double *a, long long n, float *hi, float *lo, float *r32, cudaStream_t s);
 void coef_split_df(const Level &L, Coef32 *hi, Coef32 *lo, cudaStream_t s);
 template <int KB>
 void ir_residual_df(const Level &L, const Coef32 *ch, const Coef32 *cl, const float *bh, const float *bl,
@@ -183,7 +183,6 @@ void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, 
 void dense_pin0(double *A, int n, cudaStream_t s);
 void neumann_rhs(const double *b, long long N, int K, int KB, double *B, double *sums, cudaStream_t s);
 void neumann_shift(const double *b, long long N, int K, double *x, cudaStream_t s);
-void convert_d2f(const double *a, long long n, float *o, cudaStream_t s);
 
 template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s);
@@ -197,6 +196,11 @@ void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const
 void fill_sparse(long long nnz, const long long *idx, const double *val, double *y, cudaStream_t s);
 void scale_vec(long long n, double *y, double a, cudaStream_t s);
 void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s);
+// Fields3DNodal's derived fields for K potentials (column-major (N, K)): e, j on
+// the edges ((nE, K); either may be null; j needs L.d_sigma), the node charge
+// q ((N, K)) and, from it, the cell charge density ((nC, K); may be null).
+void edge_fields(const Level &L, const double *phi, int K, double *e, double *j, cudaStream_t s);
+void node_charge(const Level &L, const double *e, int K, double eps0, double *q, double *rho, cudaStream_t s);
 void cell_gradient(const Level &L, int robin, const double *P, const double *Q, const double *dsig, double scale,
                    double *g, cudaStream_t s);
 

@@ -134,13 +134,47 @@ __device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *
 
 // Right-hand side r (type R) of a smoothing kernel at element t, times the
 // per-lane scale when given (the finest level's PCG residual, see Rhs).
+// The W per-RHS parameters (alpha, beta, scale) of one thread's lanes, p
+// pointing at entry b * KB + q * W.  When W of them fill whole 16-byte words
+// they are read by 16-byte loads: the parameter arrays start 256-byte aligned
+// in the workspace and KB is a multiple of W, so p is 16-byte aligned then.
+template <typename T, int W, typename P>
+__device__ __forceinline__ Vec<T, W> lane_par(const P *__restrict__ p) {
+  Vec<T, W> v;
+  constexpr int PER = 16 / (int)sizeof(P);
+  if constexpr (W % PER == 0 && sizeof(P) == 8) {
+    const double2 *pu = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+    for (int i = 0; i < W / 2; ++i) {
+      const double2 u = __ldg(pu + i);
+      v.a[2 * i] = (T)u.x;
+      v.a[2 * i + 1] = (T)u.y;
+    }
+  } else if constexpr (W % PER == 0 && sizeof(P) == 4) {
+    const float4 *pu = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < W / 4; ++i) {
+      const float4 u = __ldg(pu + i);
+      v.a[4 * i] = (T)u.x;
+      v.a[4 * i + 1] = (T)u.y;
+      v.a[4 * i + 2] = (T)u.z;
+      v.a[4 * i + 3] = (T)u.w;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < W; ++e) v.a[e] = (T)p[e];
+  }
+  return v;
+}
+
 template <typename T, int KB, int W, typename R>
 __device__ __forceinline__ Vec<T, W> rhs_at(const R *__restrict__ r, const float *__restrict__ scale, long long t,
                                              int b, int q) {
   Vec<T, W> v = ld<T, W>(r + t);
   if (scale) {
+    const Vec<T, W> sv = lane_par<T, W>(scale + b * KB + q * W);
 #pragma unroll
-    for (int e = 0; e < W; ++e) v.a[e] *= (T)scale[b * KB + q * W + e];
+    for (int e = 0; e < W; ++e) v.a[e] *= sv.a[e];
   }
   return v;
 }
@@ -678,19 +712,20 @@ __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict
   sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
     Vec<T, W> xv = ld<T, W>(x + t), rv = ld<T, W>(r + t);
     const Vec<T, W> pv = ld<T, W>(p + t), qq = ld<T, W>(qv + t);
+    const Vec<T, W> av = lane_par<T, W>(alpha + b * KB + q * W);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const T a = (T)alpha[b * KB + q * W + e];
-      xv.a[e] += a * pv.a[e];
-      rv.a[e] -= a * qq.a[e];
+      xv.a[e] += av.a[e] * pv.a[e];
+      rv.a[e] -= av.a[e] * qq.a[e];
       acc[e] += rv.a[e] * rv.a[e];
     }
     st<T, W>(x + t, xv);
     st<T, W>(r + t, rv);
     if (SMOOTH) {
       if (scale) {
+        const Vec<T, W> sv = lane_par<T, W>(scale + b * KB + q * W);
 #pragma unroll
-        for (int e = 0; e < W; ++e) rv.a[e] *= (T)scale[b * KB + q * W + e];
+        for (int e = 0; e < W; ++e) rv.a[e] *= sv.a[e];
       }
       if (rv_out) st<T, W>(rv_out + t, rv);
       const T s = c0 * invd[n];
@@ -730,8 +765,9 @@ __global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, V *__restrict_
     SWEEP_INDEX(d.N, d.mn)
     Vec<T, W> pv = ld<T, W>(p + t);
     const Vec<T, W> zv = ld<T, W>(z + t);
+    const Vec<T, W> bv = lane_par<T, W>(beta + b * KB + q * W);
 #pragma unroll
-    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + (T)beta[b * KB + q * W + e] * pv.a[e];
+    for (int e = 0; e < W; ++e) pv.a[e] = zv.a[e] + bv.a[e] * pv.a[e];
     st<T, W>(p + t, pv);
   }
 }

@@ -61,12 +61,40 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
   pl = fmaf(ah, bl, fmaf(al, bh, pl));
 }
 
-__global__ void k_split_df(const double *__restrict__ a, long long n, float *__restrict__ hi, float *__restrict__ lo) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double v = a[i];
-    const float h = (float)v;
-    hi[i] = h;
-    lo[i] = (float)(v - (double)h);
+// (hi, lo) = double-float split of a (hi = fp32(a), lo = fp32(a - hi)); r32, if
+// given, also receives hi (the fp32 copy of a).  VEC: two elements per thread
+// by 16-byte loads and 8-byte stores (every pointer aligned for that).
+template <bool VEC>
+__global__ void k_split_df(const double *__restrict__ a, long long n, float *__restrict__ hi, float *__restrict__ lo,
+                           float *__restrict__ r32) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (VEC) {
+    const double2 *a2 = reinterpret_cast<const double2 *>(a);
+    float2 *h2 = reinterpret_cast<float2 *>(hi), *l2 = reinterpret_cast<float2 *>(lo);
+    float2 *r2 = reinterpret_cast<float2 *>(r32);
+    for (long long i = i0; i < n / 2; i += stride) {
+      const double2 v = a2[i];
+      const float2 h = make_float2((float)v.x, (float)v.y);
+      h2[i] = h;
+      l2[i] = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
+      if (r32) r2[i] = h;
+    }
+    if ((n & 1) && i0 == 0) {
+      const double v = a[n - 1];
+      const float h = (float)v;
+      hi[n - 1] = h;
+      lo[n - 1] = (float)(v - (double)h);
+      if (r32) r32[n - 1] = h;
+    }
+  } else {
+    for (long long i = i0; i < n; i += stride) {
+      const double v = a[i];
+      const float h = (float)v;
+      hi[i] = h;
+      lo[i] = (float)(v - (double)h);
+      if (r32) r32[i] = h;
+    }
   }
 }
 
@@ -161,8 +189,13 @@ void ir_residual(const Level &L, const double *b, const double *x, double *r64, 
 }
 
 
-void split_df(const double *a, long long n, float *hi, float *lo, cudaStream_t s) {
-  k_split_df<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(a, n, hi, lo);
+void split_df(const double *a, long long n, float *hi, float *lo, float *r32, cudaStream_t s) {
+  const bool vec = ((uintptr_t)a % 16 == 0) && ((uintptr_t)hi % 8 == 0) && ((uintptr_t)lo % 8 == 0) &&
+                   ((uintptr_t)r32 % 8 == 0);
+  if (vec)
+    k_split_df<true><<<count_launch(grid_flat(n / 2 + 1, g_n_sm)), TPB, 0, s>>>(a, n, hi, lo, r32);
+  else
+    k_split_df<false><<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(a, n, hi, lo, r32);
 }
 
 void coef_split_df(const Level &L, Coef32 *hi, Coef32 *lo, cudaStream_t s) {

@@ -196,3 +196,179 @@ void reg_apply(const Level &L, double as, double ax, double ay, double az, const
                                                                         out, dg, scale);
 }
 }  // namespace dc
+
+// ---------------------------------------------------------------- derived fields
+// Fields3DNodal's e, j, charge and charge_density
+// (simpeg/electromagnetics/static/resistivity/fields.py:186-257) from the nodal
+// potentials.  Edges are ordered as discretize orders them: all x-edges
+// (nx, ny+1, nz+1), then y-edges (nx+1, ny, nz+1), then z-edges
+// (nx+1, ny+1, nz), each Fortran-ordered.  The edge inner products are
+// diagonal on a tensor mesh: V_c / 4 from every cell c that holds the edge.
+namespace dc {
+namespace {
+struct EdgeGeo {
+  int nx, ny, nz;
+  long long nEx, nEy, nEz;
+};
+
+__host__ __device__ inline EdgeGeo edge_geo(int nx, int ny, int nz) {
+  EdgeGeo g{nx, ny, nz, (long long)nx * (ny + 1) * (nz + 1), (long long)(nx + 1) * ny * (nz + 1),
+            (long long)(nx + 1) * (ny + 1) * nz};
+  return g;
+}
+
+// Axis a (0..2) and cell-grid coordinates (i, j, k) of edge e; the edge runs from
+// node (i, j, k) one cell along a.
+__device__ inline void edge_ijk(const EdgeGeo &g, long long e, int &a, int &i, int &j, int &k) {
+  int ex = g.nx, ey = g.ny + 1;
+  if (e < g.nEx) {
+    a = 0;
+  } else if (e < g.nEx + g.nEy) {
+    a = 1;
+    e -= g.nEx;
+    ex = g.nx + 1;
+    ey = g.ny;
+  } else {
+    a = 2;
+    e -= g.nEx + g.nEy;
+    ex = g.nx + 1;
+    ey = g.ny + 1;
+  }
+  k = (int)(e / ((long long)ex * ey));
+  const long long r = e - (long long)k * ex * ey;
+  j = (int)(r / ex);
+  i = (int)(r - (long long)j * ex);
+}
+
+// Sum over the (up to 4) cells holding the edge of V_c (and of sigma_c V_c).
+__device__ inline void edge_cells(const double *hx, const double *hy, const double *hz, const double *sigma,
+                                  const EdgeGeo &g, int a, int i, int j, int k, double &vsum, double &svsum) {
+  vsum = 0.0;
+  svsum = 0.0;
+  // the edge lies along a; the cells are offset by 0 / -1 in the two other axes
+  for (int d1 = -1; d1 <= 0; ++d1)
+    for (int d2 = -1; d2 <= 0; ++d2) {
+      int ci = i, cj = j, ck = k;
+      if (a == 0) {
+        cj += d1;
+        ck += d2;
+      } else if (a == 1) {
+        ci += d1;
+        ck += d2;
+      } else {
+        ci += d1;
+        cj += d2;
+      }
+      if (ci < 0 || cj < 0 || ck < 0 || ci >= g.nx || cj >= g.ny || ck >= g.nz) continue;
+      const double V = hx[ci] * hy[cj] * hz[ck];
+      vsum += V;
+      if (sigma) svsum += sigma[ci + (long long)g.nx * (cj + (long long)g.ny * ck)] * V;
+    }
+}
+
+// e = -G phi; j = e * (sum sigma_c V_c) / (sum V_c)  (MeI MeSigma e)
+__global__ void k_edge_fields(const double *__restrict__ phi, int K, EdgeGeo g, const double *__restrict__ h,
+                              const double *__restrict__ sigma, double *__restrict__ e, double *__restrict__ jf) {
+  const double *hx = h, *hy = h + g.nx, *hz = h + g.nx + g.ny;
+  const long long nE = g.nEx + g.nEy + g.nEz;
+  const long long N = (long long)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+  const long long sy = g.nx + 1, sz = (long long)(g.nx + 1) * (g.ny + 1);
+  for (long long ed = (long long)blockIdx.x * blockDim.x + threadIdx.x; ed < nE; ed += (long long)gridDim.x * blockDim.x) {
+    int a, i, j, k;
+    edge_ijk(g, ed, a, i, j, k);
+    const long long n0 = i + sy * j + sz * k;
+    const long long n1 = n0 + (a == 0 ? 1 : (a == 1 ? sy : sz));
+    const double hinv = 1.0 / (a == 0 ? hx[i] : (a == 1 ? hy[j] : hz[k]));
+    double ratio = 0.0;
+    if (jf) {
+      double vs, svs;
+      edge_cells(hx, hy, hz, sigma, g, a, i, j, k, vs, svs);
+      ratio = svs / vs;
+    }
+    for (int r = 0; r < K; ++r) {
+      const double ev = -(phi[r * N + n1] - phi[r * N + n0]) * hinv;
+      if (e) e[r * nE + ed] = ev;
+      if (jf) jf[r * nE + ed] = ev * ratio;
+    }
+  }
+}
+
+// charge = -eps0 G^T diag(Me(1)) e at the nodes
+__global__ void k_node_charge(const double *__restrict__ e, int K, EdgeGeo g, const double *__restrict__ h,
+                              double eps0, double *__restrict__ q) {
+  const double *hx = h, *hy = h + g.nx, *hz = h + g.nx + g.ny;
+  const long long nE = g.nEx + g.nEy + g.nEz;
+  const int Nx = g.nx + 1, Ny = g.ny + 1, Nz = g.nz + 1;
+  const long long N = (long long)Nx * Ny * Nz;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(n / ((long long)Nx * Ny));
+    const long long rr = n - (long long)k * Nx * Ny;
+    const int j = (int)(rr / Nx), i = (int)(rr - (long long)j * Nx);
+    // incident edges: (edge index, coefficient of e in (G^T Me1 e)_n)
+    long long idx[6];
+    double w[6];
+    int m = 0;
+    auto add = [&](int a, int ei, int ej, int ek, double sign, double hlen) {
+      long long ed;
+      if (a == 0)
+        ed = ei + (long long)g.nx * (ej + (long long)Ny * ek);
+      else if (a == 1)
+        ed = g.nEx + ei + (long long)Nx * (ej + (long long)g.ny * ek);
+      else
+        ed = g.nEx + g.nEy + ei + (long long)Nx * (ej + (long long)Ny * ek);
+      double vs, svs;
+      edge_cells(hx, hy, hz, nullptr, g, a, ei, ej, ek, vs, svs);
+      idx[m] = ed;
+      w[m] = sign * 0.25 * vs / hlen;
+      ++m;
+    };
+    if (i < g.nx) add(0, i, j, k, -1.0, hx[i]);
+    if (i > 0) add(0, i - 1, j, k, 1.0, hx[i - 1]);
+    if (j < g.ny) add(1, i, j, k, -1.0, hy[j]);
+    if (j > 0) add(1, i, j - 1, k, 1.0, hy[j - 1]);
+    if (k < g.nz) add(2, i, j, k, -1.0, hz[k]);
+    if (k > 0) add(2, i, j, k - 1, 1.0, hz[k - 1]);
+    for (int r = 0; r < K; ++r) {
+      double acc = 0.0;
+      for (int t = 0; t < m; ++t) acc += w[t] * e[r * nE + idx[t]];
+      q[r * N + n] = -eps0 * acc;
+    }
+  }
+}
+
+// charge_density = (average of the cell's 8 node charges) / V_c
+__global__ void k_cell_charge_density(const double *__restrict__ q, int K, EdgeGeo g, const double *__restrict__ h,
+                                      double *__restrict__ rho) {
+  const double *hx = h, *hy = h + g.nx, *hz = h + g.nx + g.ny;
+  const long long nC = (long long)g.nx * g.ny * g.nz;
+  const long long N = (long long)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+  const long long sy = g.nx + 1, sz = (long long)(g.nx + 1) * (g.ny + 1);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nC; c += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(c / ((long long)g.nx * g.ny));
+    const long long rr = c - (long long)k * g.nx * g.ny;
+    const int j = (int)(rr / g.nx), i = (int)(rr - (long long)j * g.nx);
+    const long long n0 = i + sy * j + sz * k;
+    const double inv = 0.125 / (hx[i] * hy[j] * hz[k]);
+    for (int r = 0; r < K; ++r) {
+      const double *qr = q + r * N + n0;
+      const double s = qr[0] + qr[1] + qr[sy] + qr[sy + 1] + qr[sz] + qr[sz + 1] + qr[sz + sy] + qr[sz + sy + 1];
+      rho[r * nC + c] = s * inv;
+    }
+  }
+}
+}  // namespace
+
+void edge_fields(const Level &L, const double *phi, int K, double *e, double *j, cudaStream_t s) {
+  const EdgeGeo g = edge_geo(L.nx, L.ny, L.nz);
+  k_edge_fields<<<count_launch(dim3(grid_flat(g.nEx + g.nEy + g.nEz, g_n_sm))), TPB, 0, s>>>(phi, K, g, L.d_h,
+                                                                                          L.d_sigma, e, j);
+}
+
+void node_charge(const Level &L, const double *e, int K, double eps0, double *q, double *rho, cudaStream_t s) {
+  const EdgeGeo g = edge_geo(L.nx, L.ny, L.nz);
+  k_node_charge<<<count_launch(dim3(grid_flat(L.dims.N, g_n_sm))), TPB, 0, s>>>(e, K, g, L.d_h, eps0, q);
+  if (rho)
+    k_cell_charge_density<<<count_launch(dim3(grid_flat((long long)L.nx * L.ny * L.nz, g_n_sm))), TPB, 0, s>>>(
+        q, K, g, L.d_h, rho);
+}
+}  // namespace dc

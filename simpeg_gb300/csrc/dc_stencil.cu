@@ -440,11 +440,6 @@ __global__ void k_neumann_shift(const double *__restrict__ b, long long N, doubl
   for (long long n = threadIdx.x; n < N; n += TPB) c[n] += delta;
 }
 
-__global__ void k_convert_d2f(const double *__restrict__ a, long long n, float *__restrict__ o) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    o[i] = (float)a[i];
-}
-
 // ---------------------------------------------------------------- layout conversion
 // Column-major (K, N) <-> RHS-blocked [nb][N][KB] transposes through a
 // 32 x 32 shared-memory tile (rows = RHS, columns = nodes), so that both the
@@ -631,9 +626,6 @@ void neumann_shift(const double *b, long long N, int K, double *x, cudaStream_t 
   k_neumann_shift<<<count_launch(dim3(K)), TPB, 0, s>>>(b, N, x);
 }
 
-void convert_d2f(const double *a, long long n, float *o, cudaStream_t s) {
-  k_convert_d2f<<<count_launch(dim3(grid_flat(n, g_n_sm))), TPB, 0, s>>>(a, n, o);
-}
 
 template <typename T>
 void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst, cudaStream_t s) {

@@ -223,6 +223,34 @@ class DCEngine:
     def release_workspace(self):
         self._ws.clear()
 
+    @property
+    def n_edges(self):
+        nx, ny, nz = self.shape_cells
+        return nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+
+    def edge_fields(self, phi, e=True, j=True):
+        """(e, j) on the edges for potentials phi of shape (k, nN) or (nN,); either may be skipped."""
+        phi = _dev64(phi, None, "phi")
+        p2 = phi.reshape(-1, self.nN)
+        k = p2.shape[0]
+        eo = torch.empty(k, self.n_edges, dtype=torch.float64, device=phi.device) if e else None
+        jo = torch.empty(k, self.n_edges, dtype=torch.float64, device=phi.device) if j else None
+        check(lib().dc_edge_fields(self._h, _ptr(p2), k, _ptr(eo), _ptr(jo), _stream()))
+        shape = (self.n_edges,) if phi.dim() == 1 else (k, self.n_edges)
+        return (eo.reshape(shape) if e else None, jo.reshape(shape) if j else None)
+
+    def node_charge(self, e, eps0, density=False):
+        """Node charge (k, nN) (and cell charge density (k, nC)) from the edge field e (k, nE)."""
+        e = _dev64(e, None, "e")
+        e2 = e.reshape(-1, self.n_edges)
+        k = e2.shape[0]
+        q = torch.empty(k, self.nN, dtype=torch.float64, device=e.device)
+        rho = torch.empty(k, self.nC, dtype=torch.float64, device=e.device) if density else None
+        check(lib().dc_node_charge(self._h, _ptr(e2), k, float(eps0), _ptr(q), _ptr(rho), _stream()))
+        if e.dim() == 1:
+            return q.reshape(self.nN), (rho.reshape(self.nC) if density else None)
+        return q, rho
+
     def dadm_fwd(self, u, dsig, scale=1.0):
         u = _dev64(u, None, "u")
         u2 = u.reshape(-1, self.nN)

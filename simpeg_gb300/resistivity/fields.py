@@ -2,9 +2,12 @@
 
 Mirrors ``simpeg/electromagnetics/static/resistivity/fields.py:186-257`` and
 the ``Fields`` store of ``simpeg/fields.py:7-345``: the nodal potential of
-every source, indexed ``f[src, "phiSolution"]`` / ``f[:, "phi"]``.  The store
-stays on the GPU as a ``(nSrc, nN)`` float64 tensor (column-major (nN, nSrc));
-indexing copies the requested columns to the host as numpy arrays.
+every source, indexed ``f[src, "phiSolution"]`` / ``f[:, "phi"]``, and the
+fields derived from it on request: ``e = -G phi`` and ``j = MeI MeSigma e`` on
+the edges, ``charge`` on the nodes and ``charge_density`` on the cells
+(``dc_edge_fields`` / ``dc_node_charge`` kernels).  The store stays on the GPU
+as a ``(nSrc, nN)`` float64 tensor (column-major (nN, nSrc)); indexing copies
+the requested columns to the host as numpy arrays.
 """
 
 from __future__ import annotations
@@ -12,9 +15,18 @@ from __future__ import annotations
 import numpy as np
 
 
+_DERIVED = ("e", "j", "charge", "charge_density")
+
+
 class Fields3DNodal:
     knownFields = {"phiSolution": "N"}
-    aliasFields = {"phi": ["phiSolution", "N", "_phi"]}
+    aliasFields = {
+        "phi": ["phiSolution", "N", "_phi"],
+        "j": ["phiSolution", "E", "_j"],
+        "e": ["phiSolution", "E", "_e"],
+        "charge_density": ["phiSolution", "CC", "_charge_density"],
+        "charge": ["phiSolution", "N", "_charge"],
+    }
 
     def __init__(self, simulation, phi_dev):
         self.simulation = simulation
@@ -36,13 +48,37 @@ class Fields3DNodal:
                 return i
         raise KeyError("source is not part of the survey")
 
+    def _GLoc(self, fieldType):
+        """Grid location of a field (``fields.py:205-211``)."""
+        if fieldType == "phi":
+            return "N"
+        if fieldType in ("e", "j"):
+            return "E"
+        raise KeyError("Field type must be phi, e, j")
+
+    def _derived(self, idx, name):
+        """Derived field of the sources idx (list) on the device, (len(idx), n) (``fields.py:214-253``)."""
+        from scipy.constants import epsilon_0
+
+        eng = self.simulation.engine
+        phi = self.phi_dev[idx]
+        if name in ("e", "j"):
+            e, j = eng.edge_fields(phi, e=name == "e", j=name == "j")
+            return e if name == "e" else j
+        e, _ = eng.edge_fields(phi, e=True, j=False)
+        q, rho = eng.node_charge(e, epsilon_0, density=name == "charge_density")
+        return q if name == "charge" else rho
+
     def __getitem__(self, key):
         if not isinstance(key, tuple) or len(key) != 2:
             raise KeyError("index as f[src, 'phiSolution']")
         src, name = key
-        if name not in ("phiSolution", "phi"):
-            raise KeyError(f"field {name!r} is not stored on the GPU path (phi / phiSolution only)")
+        if name not in ("phiSolution", "phi") + _DERIVED:
+            raise KeyError(f"{name!r} is not a field of Fields3DNodal ({', '.join(('phi',) + _DERIVED)})")
         idx = self._src_index(src)
+        if name in _DERIVED:
+            out = self._derived(idx if isinstance(idx, list) else [idx], name).cpu().numpy()
+            return out.T.copy() if isinstance(idx, list) else out[0]
         if isinstance(idx, list):
             return self.phi_dev[idx].cpu().numpy().T.copy()
         return self.phi_dev[idx].cpu().numpy()

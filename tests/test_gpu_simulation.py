@@ -221,3 +221,23 @@ def test_analytic_halfspace_gpu(cuda, bc):
     d = sim.dpred()
     err = np.sqrt((((d - ana) / ana) ** 2).sum() / survey.nD)
     assert err < 0.05, err
+
+
+def test_derived_fields_vs_oracle(cuda, block_case):
+    """Fields3DNodal e, j, charge, charge_density (resistivity/fields.py:214-253):
+    the device kernels applied to the GPU potentials equal the oracle's sparse
+    operators applied to the same potentials (fp64, summation order only)."""
+    from scipy.constants import epsilon_0
+
+    mesh, survey, m, orc, _ = block_case
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), rtol=1e-10)
+    f = sim.fields(m)
+    phi = f[:, "phi"]
+    e0, j0, q0, rho0 = orc.derived_fields(phi, epsilon_0)
+    for name, ref in (("e", e0), ("j", j0), ("charge", q0), ("charge_density", rho0)):
+        got = f[:, name]
+        assert got.shape == ref.shape, name
+        assert _rel(got, ref) < 1e-12, (name, _rel(got, ref))
+    src = survey.source_list[3]
+    np.testing.assert_allclose(f[src, "e"], e0[:, 3], rtol=1e-12, atol=1e-12 * np.abs(e0).max())
+    assert f._GLoc("e") == "E" and f._GLoc("phi") == "N"

@@ -192,3 +192,86 @@ def test_oracle_reproduces_golden_fixture():
     np.testing.assert_allclose(o.Jvec(g["m"], g["v"], f=f), g["jvec"], rtol=1e-9, atol=1e-12 * np.abs(g["jvec"]).max())
     np.testing.assert_allclose(o.Jtvec(g["m"], g["w"], f=f), g["jtvec"], rtol=1e-9,
                                atol=1e-12 * np.abs(g["jtvec"]).max())
+
+
+def _ip_forward_setup():
+    """tests/em/static/test_IP_fwd.py:12-46: dipole source, dipole receivers over a
+    conductive-chargeable sphere (eta = 0.1) in a 0.01 S/m half-space."""
+    cs = 12.5
+    hx = [(cs, 2, -1.3), (cs, 21), (cs, 2, 1.3)]
+    hz = [(cs, 2, -1.3), (cs, 20)]
+    mesh = TensorMesh([hx, hx, hz], origin="CCN")
+    x = mesh.cell_centers_x[(mesh.cell_centers_x > -80.0) & (mesh.cell_centers_x < 80.0)]
+    y = mesh.cell_centers_y[(mesh.cell_centers_y > -80.0) & (mesh.cell_centers_y < 80.0)]
+    M = TensorMesh._ndgrid(x - 12.5, y, np.r_[0.0])
+    N = TensorMesh._ndgrid(x + 12.5, y, np.r_[0.0])
+    inside = np.linalg.norm(mesh.cell_centers - np.r_[0.0, 0.0, -100.0], axis=1) < 50.0
+    sigma_inf = np.full(mesh.n_cells, 1e-2)
+    eta = np.where(inside, 0.1, 0.0)
+    src = sources.Dipole([receivers.Dipole(M, N)], np.r_[-100.0, 0.0, 0.0], np.r_[100.0, 0.0, 0.0])
+    return mesh, Survey([src]), sigma_inf, eta
+
+
+def test_ip_oracle_is_the_linearised_dc_response():
+    """tests/em/static/test_IP_fwd.py:48-74: IP data vs DC(sigma0) - DC(sigma_inf),
+    sigma0 = sigma_inf (1 - eta); mean squared relative error < 0.05."""
+    from oracle.ip3d import OracleIP3DNodal
+
+    mesh, survey, sigma_inf, eta = _ip_forward_setup()
+    d0 = OracleDC3DNodal(mesh, survey, sigma=sigma_inf * (1.0 - eta)).dpred()
+    dinf = OracleDC3DNodal(mesh, survey, sigma=sigma_inf).dpred()
+    ip = OracleIP3DNodal(mesh, survey, sigma_inf, eta_map=maps.IdentityMap(mesh))
+    d = ip.dpred(eta)
+    full = d0 - dinf
+    err = np.linalg.norm((d - full) / full) ** 2 / full.size
+    assert err < 0.05, err
+
+
+def test_ip_oracle_adjoint_and_chargeability_scale():
+    """tests/em/static/test_IP_jvecjtvecadj.py:146-156 (adjoint, |w.Jv - v.Jtw| < 1e-8),
+    and apparent-chargeability data = IP voltage / DC voltage (simulation.py:44-61)."""
+    from oracle.ip3d import OracleIP3DNodal
+
+    mesh, survey, _ = _small_problem(seed=3)
+    sigma = np.exp(_small_problem(seed=3)[2])
+    ip = OracleIP3DNodal(mesh, survey, sigma, eta_map=maps.IdentityMap(mesh))
+    rng = np.random.default_rng(30)
+    m0 = np.full(mesh.n_cells, 0.1)
+    v = rng.uniform(size=mesh.n_cells)
+    w = rng.uniform(size=survey.nD)
+    assert abs(w @ ip.Jvec(m0, v) - v @ ip.Jtvec(m0, w)) < 1e-8
+    d_volt = ip.dpred(m0)
+    dc = OracleDC3DNodal(mesh, survey, sigma=sigma).dpred()
+    for src in survey.source_list:
+        for rx in src.receiver_list:
+            rx.data_type = "apparent_chargeability"
+    ip2 = OracleIP3DNodal(mesh, survey, sigma, eta_map=maps.IdentityMap(mesh))
+    np.testing.assert_allclose(ip2.dpred(m0), d_volt / dc, rtol=1e-12)
+    # linear in eta: the prediction is J eta exactly
+    np.testing.assert_allclose(ip2.dpred(2.0 * m0), 2.0 * ip2.dpred(m0), rtol=1e-12)
+
+
+def test_derived_fields_of_a_uniform_gradient():
+    """Fields3DNodal e, j, charge, charge_density (resistivity/fields.py:214-253) for
+    phi = -x on a non-uniform mesh: e = 1 on x-edges and 0 on the others, j = the
+    edge-averaged conductivity on x-edges, no charge at interior nodes (the field is
+    divergence-free there); charge only on the x = min / max faces, equal and opposite."""
+    mesh = TensorMesh([[(10.0, 2, -1.3), (10.0, 4), (10.0, 2, 1.3)], [(10.0, 5)], [(8.0, 4)]], origin="CCN")
+    sigma = np.random.default_rng(0).uniform(0.01, 0.1, mesh.n_cells)
+    src = sources.Pole([], np.r_[0.0, 0.0, 0.0])
+    o = OracleDC3DNodal(mesh, Survey([src]), sigma=sigma)
+    phi = -o.ops.nodes[:, 0]
+    e, j, q, rho = o.derived_fields(phi, 8.854187817e-12)
+    nx, ny, nz = mesh.shape_cells
+    nEx = nx * (ny + 1) * (nz + 1)
+    np.testing.assert_allclose(e[:nEx], 1.0, rtol=1e-12)
+    np.testing.assert_allclose(e[nEx:], 0.0, atol=1e-12)
+    E = o.E
+    np.testing.assert_allclose(j[:nEx], (E @ sigma)[:nEx] / (E @ np.ones(mesh.n_cells))[:nEx], rtol=1e-12)
+    q3 = q.reshape((nz + 1, ny + 1, nx + 1))
+    scale = np.abs(q).max()
+    assert scale > 0
+    np.testing.assert_allclose(q3[:, :, 1:-1], 0.0, atol=1e-12 * scale)
+    np.testing.assert_allclose(q3[:, :, 0].sum(), -q3[:, :, -1].sum(), rtol=1e-12)
+    rho3 = rho.reshape((nz, ny, nx))
+    assert np.all(np.abs(rho3[:, :, 1:-1]) <= 1e-12 * np.abs(rho).max())
