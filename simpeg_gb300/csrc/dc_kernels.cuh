@@ -35,6 +35,21 @@ namespace {
 
 constexpr int TPB = 256;
 
+// Minimum resident blocks per SM requested from the compiler (0 = no request)
+// for a Chebyshev step with fp32 arithmetic on 16-bit storage (and a 16-bit
+// right-hand side, as on the finest level).  Left to itself
+// the compiler gives the second step of a zero-start sequence (PREV = 2) 53
+// registers: 4 blocks of TPB per SM instead of 5, fewer loads in flight for a
+// kernel bound by load latency (5 blocks: 48 registers, no spill, 466 -> 440
+// us per finest-level launch at 1M nodes x 256 RHS).  The step without
+// momentum (PREV = 0) spills at 5 blocks and measured slower (396 -> 428 us),
+// the PCG apply with p.q partials did not change (403 -> 400 us at 4 blocks);
+// both are left to the compiler.
+template <typename T, typename S>
+constexpr int stencil_min_blocks(int want) {
+  return (sizeof(T) == 4 && sizeof(S) == 2) ? want : 0;
+}
+
 // floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
 __device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
   if (d == 1) return n;
@@ -352,7 +367,7 @@ __global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, 
 // five of the d-vector form.  With DOT (finest level), also per-block partials
 // of r . x_{k+1} with the unscaled PCG residual r.
 template <typename T, typename V, typename R, int KB, bool DOT, int PREV>
-__global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
+__global__ void __launch_bounds__(TPB, (stencil_min_blocks<T, V>(!DOT && PREV == 2 && sizeof(R) == 2 ? 5 : 0))) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
                                                    const R *__restrict__ r, const float *__restrict__ scale,
                                                    const V *__restrict__ zin, V *zout, Dims d, int nb, T c1, T c2,
                                                    double *__restrict__ partial, int gs) {
