@@ -202,16 +202,16 @@ int dc_csr_solve(dc_csr *h, const double *b, double *x, int k, double rtol, int 
   sum_partials(k, 1, gx, pb, bb, s);
   k_jacobi_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->dinv, r, z, pc);
   CK(cudaMemsetAsync(n_active, 0, sizeof(int), s));
-  pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, n_active, 1, s);
+  pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, nullptr, n_active, 1, s);
   O::copy_z(n, k, p, z, s);
   int it = 0;
   for (; it < maxit; ++it) {
     k_csr_apply_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->ptr, h->idx, h->val, p, q, pa);
-    pcg_alpha(k, 1, gx, pa, rz, active, al, status, n_active, s);
-    O::update_xr(n, k, x, r, p, q, al, pb, gx, nullptr, 0.0, nullptr, nullptr, nullptr, s);
+    pcg_alpha(k, 1, gx, pa, rz, active, al, nullptr, status, n_active, s);
+    O::update_xr(n, k, x, r, p, q, al, nullptr, pb, gx, nullptr, 0.0, nullptr, nullptr, nullptr, s);
     k_jacobi_dot<<<count_launch(grid), TPB, 0, s>>>(n, h->dinv, r, z, pc);
-    pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, n_active, 0, s);
-    O::p_update(n, k, p, z, be, s);
+    pcg_beta(k, 1, gx, pc, pb, rz, rr, bb, tol2, active, be, nullptr, n_active, 0, s);
+    O::p_update(n, k, p, z, be, nullptr, s);
     if ((it & 7) == 7 || it + 1 == maxit) {
       CK(cudaMemcpyAsync(h->h_mail, n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(h->h_mail + 1, status, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -413,6 +413,7 @@ struct MGWork {
 struct Scal {
   double *part_a, *part_b, *part_c;  // partials (gx * Kp each)
   double *rz, *rr, *bb, *alpha, *beta, *rr64, *bb64, *maxrel, *tol2;
+  float *alpha32, *beta32;  // alpha, beta in fp32 for the fp32-arithmetic vector kernels
   int *active, *active_out, *n_active, *n_active_out, *status;
   int *loop;  // device-loop counters: {iterations this sweep, iterations in total, sweeps, unused}
   float *scale;  // per-RHS scale of the V-cycle input (1/|r|_2 of the latest residual)
@@ -459,6 +460,8 @@ void carve_scal(Carve &c, int Kp, int gx, Scal &s) {
   s.status = c.take<int>(1);
   s.loop = c.take<int>(4);
   s.scale = c.take<float>(Kp);
+  s.alpha32 = c.take<float>(Kp);
+  s.beta32 = c.take<float>(Kp);
 }
 
 // Lays out (or, with base == nullptr, sizes) the whole solve workspace.
@@ -727,7 +730,7 @@ int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Sc
   vcycle<T, V, KB>(h, 0, rin, z, w, nb, s, false, sc.part_c, gx);
   if (!fused) O::dot_z(N, nb, r, z, sc.part_c, gx, s);
   CK(cudaMemsetAsync(sc.n_active, 0, sizeof(int), s));
-  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 1, s,
+  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.beta32, sc.n_active, 1, s,
            rz_div, scale);
   O::copy_z(N, nb, p, z, s);
   const double c0 = smoother(h->smoother_kind, F.lmax, h->cheb_ratio, h->nu_pre, h->nu_post).first;
@@ -735,19 +738,19 @@ int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Sc
   // one PCG iteration on stream st
   auto iteration = [&](cudaStream_t st) {
     O::apply_v(F, p, q, nb, sc.part_a, gx, st);
-    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.status, sc.n_active, st);
+    pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.alpha32, sc.status, sc.n_active, st);
     if (fused) {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, &F, c0, z1, scale, w.r0, st);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, &F, c0, z1, scale, w.r0, st);
       vcycle<T, V, KB>(h, 0, rin, z, w, nb, st, true, sc.part_c, gx);
     } else {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, nullptr, st);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, nullptr, st);
       if (split) O::scale_to(N, nb, r, scale, w.r0, st);
       vcycle<T, V, KB>(h, 0, rin, z, w, nb, st);
       O::dot_z(N, nb, r, z, sc.part_c, gx, st);
     }
-    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.n_active, 0, st,
+    pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.beta32, sc.n_active, 0, st,
              rz_div, scale);
-    O::p_update(N, nb, p, z, sc.beta, st);
+    O::p_update(N, nb, p, z, sc.beta, sc.beta32, st);
   };
   if (loop == LOOP_DEVICE) {
     int rc;

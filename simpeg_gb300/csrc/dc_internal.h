@@ -124,15 +124,18 @@ template <typename T, typename V, int KB> struct Ops {
   static void coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V *zc, int nb, cudaStream_t s);
   // x += a p ; r -= a q ; partial |r|^2.  With smooth != nullptr also z = c0 D^-1 (scale r) on that level
   // and, when rv_out is set, rv_out = V(scale r).
+  // alpha / beta per RHS in fp64 (used when T is double) and fp32 (used when T is float: no
+  // per-element fp64 -> fp32 conversion, which runs at GB300's fp64 rate)
   static void update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
-                        double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
-                        V *rv_out, cudaStream_t s);
+                        const float *alpha32, double *partial, int gx, const Level *smooth, double c0, V *z,
+                        const float *scale, V *rv_out, cudaStream_t s);
   // rv_out = V(scale r)
   static void scale_to(long long N, int nb, const T *r, const float *scale, V *rv_out, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);
   static void dot_z(long long N, int nb, const T *a, const V *b, double *partial, int gx, cudaStream_t s);
   // p = z + beta p (p and z in V)
-  static void p_update(long long N, int nb, V *p, const V *z, const double *beta, cudaStream_t s);
+  static void p_update(long long N, int nb, V *p, const V *z, const double *beta, const float *beta32,
+                       cudaStream_t s);
   static void copy_z(long long N, int nb, V *dst, const V *src, cudaStream_t s);
 };
 
@@ -153,12 +156,13 @@ void ir_accumulate_df(long long n, float *xh, float *xl, const float *d32, cudaS
 
 void fill_int(int *a, int n, int v, cudaStream_t s);
 // alpha = rz / (p.q) per active RHS; also zeroes *n_active for the pcg_beta of the same iteration
+// (alpha32, if given, receives alpha in fp32)
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
-               int *status, int *n_active, cudaStream_t s);
+               float *alpha32, int *status, int *n_active, cudaStream_t s);
 // rz = r.z (divided per RHS by rz_div when set: z came from the scaled input) ;
 // rr = |r|^2 ; active &= rr > tol2*bb ; beta ; counts active ; scale_out = 1/sqrt(rr) when set
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
-              const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
+              const double *bb, const double *tol2, int *active, double *beta, float *beta32, int *n_active, int first,
               cudaStream_t s, const float *rz_div = nullptr, float *scale_out = nullptr);
 // per-RHS sums of block partials; with scale, also scale = 1/sqrt(sum) (the V-cycle input scale)
 void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s, float *scale = nullptr);

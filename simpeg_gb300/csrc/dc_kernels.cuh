@@ -720,7 +720,7 @@ __global__ void __launch_bounds__(TPB) k_coarse_solve(const T *__restrict__ Ainv
 template <typename T, typename V, int KB, bool SMOOTH>
 __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict__ x, T *__restrict__ r,
                                                    const V *__restrict__ p, const T *__restrict__ qv,
-                                                   const double *__restrict__ alpha, double *__restrict__ partial,
+                                                   const T *__restrict__ alpha, double *__restrict__ partial,
                                                    const T *__restrict__ invd, V *__restrict__ z, T c0,
                                                    const float *__restrict__ scale, V *__restrict__ rv_out, int gs) {
   constexpr int W = Lanes<T, KB>::W;
@@ -775,7 +775,7 @@ __global__ void __launch_bounds__(TPB) k_dot(Dims d, int nb, const T *__restrict
 // p = z + beta p (p stored as V, like z)
 template <typename T, typename V, int KB>
 __global__ void __launch_bounds__(TPB) k_p_update(Dims d, int nb, V *__restrict__ p, const V *__restrict__ z,
-                                                  const double *__restrict__ beta) {
+                                                  const T *__restrict__ beta) {
   SWEEP(d.N, d.mn, nb, (Lanes<V, KB>::W)) {
     SWEEP_INDEX(d.N, d.mn)
     Vec<T, W> pv = ld<T, W>(p + t);
@@ -1020,17 +1020,30 @@ void Ops<T, V, KB>::coarse_solve(const T *Ainv, const Level &c, Rhs<T, V> rc, V 
         Ainv, c.dims, nb, rc.part, nullptr, zc);
 }
 
+// The per-RHS parameter array in the arithmetic type T.
+template <typename T>
+const T *param_of(const double *d, const float *f);
+template <>
+inline const double *param_of<double>(const double *d, const float *) {
+  return d;
+}
+template <>
+inline const float *param_of<float>(const double *, const float *f) {
+  return f;
+}
+
 template <typename T, typename V, int KB>
 void Ops<T, V, KB>::update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
-                              double *partial, int gx, const Level *smooth, double c0, V *z, const float *scale,
-                              V *rv_out, cudaStream_t s) {
+                              const float *alpha32, double *partial, int gx, const Level *smooth, double c0, V *z,
+                              const float *scale, V *rv_out, cudaStream_t s) {
   const Dims dd = flat_dims(N);
+  const T *a = param_of<T>(alpha, alpha32);
   if (smooth)
     k_update_xr<T, V, KB, true><<<RED_GRID(N, (k_update_xr<T, V, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
-        dd, nb, x, r, p, q, alpha, partial, invd_ptr<T>(*smooth), z, (T)c0, scale, rv_out, gx);
+        dd, nb, x, r, p, q, a, partial, invd_ptr<T>(*smooth), z, (T)c0, scale, rv_out, gx);
   else
     k_update_xr<T, V, KB, false><<<RED_GRID(N, (k_update_xr<T, V, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
-        dd, nb, x, r, p, q, alpha, partial, nullptr, nullptr, (T)0, nullptr, nullptr, gx);
+        dd, nb, x, r, p, q, a, partial, nullptr, nullptr, (T)0, nullptr, nullptr, gx);
 }
 
 template <typename T, typename V, int KB>
@@ -1051,8 +1064,10 @@ void Ops<T, V, KB>::dot_z(long long N, int nb, const T *a, const V *b, double *p
 }
 
 template <typename T, typename V, int KB>
-void Ops<T, V, KB>::p_update(long long N, int nb, V *p, const V *z, const double *beta, cudaStream_t s) {
-  k_p_update<T, V, KB><<<GRID_K(N, (k_p_update<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z, beta);
+void Ops<T, V, KB>::p_update(long long N, int nb, V *p, const V *z, const double *beta, const float *beta32,
+                             cudaStream_t s) {
+  k_p_update<T, V, KB><<<GRID_K(N, (k_p_update<T, V, KB>)), TPB, 0, s>>>(flat_dims(N), nb, p, z,
+                                                                       param_of<T>(beta, beta32));
 }
 
 template <typename T, typename V, int KB>

@@ -52,8 +52,8 @@ __device__ __forceinline__ float rss(double rr) {
 
 __global__ void __launch_bounds__(SCAL_T) k_pcg_alpha(int K, int KB, int gx, const double *__restrict__ part_pq,
                                                       const double *__restrict__ rz, const int *__restrict__ active,
-                                                      double *__restrict__ alpha, int *__restrict__ status,
-                                                      int *__restrict__ n_active) {
+                                                      double *__restrict__ alpha, float *__restrict__ alpha32,
+                                                      int *__restrict__ status, int *__restrict__ n_active) {
   const int r = blockIdx.x;
   const double pq = block_sum_partial(part_pq, gx, KB, r);
   if (threadIdx.x == 0) {
@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(SCAL_T) k_pcg_alpha(int K, int KB, int gx, con
         a = rz[r] / pq;
     }
     alpha[r] = a;
+    if (alpha32) alpha32[r] = (float)a;
   }
 }
 
@@ -75,8 +76,9 @@ __global__ void __launch_bounds__(SCAL_T) k_pcg_beta(int K, int KB, int gx, cons
                                                      const double *__restrict__ part_rr, double *__restrict__ rz,
                                                      double *__restrict__ rr_out, const double *__restrict__ bb,
                                                      const double *__restrict__ tol2, int *__restrict__ active,
-                                                     double *__restrict__ beta, int *__restrict__ n_active,
-                                                     int first, const float *rz_div, float *scale) {
+                                                     double *__restrict__ beta, float *__restrict__ beta32,
+                                                     int *__restrict__ n_active, int first, const float *rz_div,
+                                                     float *scale) {
   const int r = blockIdx.x;
   double rzn = block_sum_partial(part_rz, gx, KB, r);
   const double rr = block_sum_partial(part_rr, gx, KB, r);
@@ -91,6 +93,7 @@ __global__ void __launch_bounds__(SCAL_T) k_pcg_beta(int K, int KB, int gx, cons
     if (act && !first) bt = rz[r] != 0.0 ? rzn / rz[r] : 0.0;
     if (act) rz[r] = rzn;
     beta[r] = first ? 0.0 : bt;
+    if (beta32) beta32[r] = first ? 0.0f : (float)bt;
     active[r] = act;
     if (act) atomicAdd(n_active, 1);
   }
@@ -553,15 +556,16 @@ void fill_int(int *a, int n, int v, cudaStream_t s) {
 }
 
 void pcg_alpha(int K, int KB, int gx, const double *part_pq, const double *rz, const int *active, double *alpha,
-               int *status, int *n_active, cudaStream_t s) {
-  k_pcg_alpha<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, status, n_active);
+               float *alpha32, int *status, int *n_active, cudaStream_t s) {
+  k_pcg_alpha<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_pq, rz, active, alpha, alpha32, status,
+                                                       n_active);
 }
 
 void pcg_beta(int K, int KB, int gx, const double *part_rz, const double *part_rr, double *rz, double *rr,
-              const double *bb, const double *tol2, int *active, double *beta, int *n_active, int first,
-              cudaStream_t s, const float *rz_div, float *scale_out) {
+              const double *bb, const double *tol2, int *active, double *beta, float *beta32, int *n_active,
+              int first, cudaStream_t s, const float *rz_div, float *scale_out) {
   k_pcg_beta<<<count_launch(dim3(K)), SCAL_T, 0, s>>>(K, KB, gx, part_rz, part_rr, rz, rr, bb, tol2, active, beta,
-                                                      n_active, first, rz_div, scale_out);
+                                                      beta32, n_active, first, rz_div, scale_out);
 }
 
 void sum_partials(int K, int KB, int gx, const double *part, double *out, cudaStream_t s, float *scale) {
