@@ -844,8 +844,9 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
     float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
     split_df(w.B64, (long long)N * Kp, bh, bl, w.r32, s);  // also r32 = fp32(b), the first residual
-    // |b|^2, initial outer flags
-    Ops<double, double, KB>::dot(N, nb, w.B64, w.B64, w.sc.part_b, gx, s);
+    // |b|^2 from the fp32 copy of b (the stopping test needs it to ~1e-6 relatively; an fp64 dot runs at
+    // the fp64 rate), initial outer flags
+    Ops<float, float, KB>::dot(N, nb, w.r32, w.r32, w.sc.part_b, gx, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
     sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,

@@ -1,6 +1,7 @@
 // Instantiation of the node kernels for the fp64 solve (T = V = double), the
 // fp64 true-residual kernel, and the double-float refinement kernels of the
 // mixed-precision solve (b - A x and x += d with fp32 pairs).
+#include "dc_dfbits.h"
 #include "dc_kernels.cuh"
 
 namespace dc {
@@ -61,9 +62,23 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
   pl = fmaf(ah, bl, fmaf(al, bh, pl));
 }
 
-// (hi, lo) = double-float split of a (hi = fp32(a), lo = fp32(a - hi)); r32, if
-// given, also receives hi (the fp32 copy of a).  VEC: two elements per thread
-// by 16-byte loads and 8-byte stores (every pointer aligned for that).
+// hi = fp32(v), lo = fp32(v - hi) with fp64 instructions: a call of its own, so
+// that the compiler does not predicate these slow instructions into the common
+// path of split_one.
+__device__ __noinline__ void split_fp64(double v, float &h, float &l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// Double-float split of one value: by bits (split_df_bits) where that covers it.
+__device__ __forceinline__ void split_one(double v, float &h, float &l) {
+  if (__builtin_expect(split_df_bits(v, h, l), 1)) return;
+  split_fp64(v, h, l);
+}
+
+// (hi, lo) = double-float split of a; r32, if given, also receives hi (the fp32
+// copy of a).  VEC: two elements per thread by 16-byte loads and 8-byte stores
+// (every pointer aligned for that).
 template <bool VEC>
 __global__ void k_split_df(const double *__restrict__ a, long long n, float *__restrict__ hi, float *__restrict__ lo,
                            float *__restrict__ r32) {
@@ -75,24 +90,26 @@ __global__ void k_split_df(const double *__restrict__ a, long long n, float *__r
     float2 *r2 = reinterpret_cast<float2 *>(r32);
     for (long long i = i0; i < n / 2; i += stride) {
       const double2 v = a2[i];
-      const float2 h = make_float2((float)v.x, (float)v.y);
+      float2 h, l;
+      split_one(v.x, h.x, l.x);
+      split_one(v.y, h.y, l.y);
       h2[i] = h;
-      l2[i] = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
+      l2[i] = l;
       if (r32) r2[i] = h;
     }
     if ((n & 1) && i0 == 0) {
-      const double v = a[n - 1];
-      const float h = (float)v;
+      float h, l;
+      split_one(a[n - 1], h, l);
       hi[n - 1] = h;
-      lo[n - 1] = (float)(v - (double)h);
+      lo[n - 1] = l;
       if (r32) r32[n - 1] = h;
     }
   } else {
     for (long long i = i0; i < n; i += stride) {
-      const double v = a[i];
-      const float h = (float)v;
+      float h, l;
+      split_one(a[i], h, l);
       hi[i] = h;
-      lo[i] = (float)(v - (double)h);
+      lo[i] = l;
       if (r32) r32[i] = h;
     }
   }

@@ -1,6 +1,7 @@
 // Scalar, coefficient, coarsest-level, Neumann and layout kernels of the
 // nodal DC engine (the node kernels and their launchers are in
 // dc_kernels.cuh, instantiated by dc_ops_*.cu), plus the launch bookkeeping.
+#include "dc_dfbits.h"
 #include "dc_kernels.cuh"
 
 #include <cstdio>
@@ -495,7 +496,12 @@ __global__ void __launch_bounds__(TT *TR) k_unpack(const T *__restrict__ src, lo
   }
 }
 
-// The same transpose for a double-float (hi, lo) blocked array: dst = hi + lo in fp64.
+// (double)f with the fp64 conversion instruction, in a call of its own (kept out
+// of the common path of k_unpack_df).
+__device__ __noinline__ double widen_fp64(float f) { return (double)f; }
+
+// The same transpose for a double-float (hi, lo) blocked array: dst = hi + lo in fp64
+// (each fp32 widened by bits where that covers it, one fp64 add).
 __global__ void __launch_bounds__(TT *TR) k_unpack_df(const float *__restrict__ hi, const float *__restrict__ lo,
                                                      long long N, int K, int KB, double *__restrict__ dst) {
   __shared__ double tile[TT][TT + 1];
@@ -508,7 +514,10 @@ __global__ void __launch_bounds__(TT *TR) k_unpack_df(const float *__restrict__ 
       const long long n = n0 + j;
       if (r < K && n < N) {
         const long long e = ((long long)b * N + n) * KB + l;
-        tile[threadIdx.x][j] = (double)hi[e] + (double)lo[e];
+        double h, l;
+        if (__builtin_expect(!widen_bits(hi[e], h), 0)) h = widen_fp64(hi[e]);
+        if (__builtin_expect(!widen_bits(lo[e], l), 0)) l = widen_fp64(lo[e]);
+        tile[threadIdx.x][j] = h + l;
       }
     }
   }
