@@ -14,9 +14,12 @@
 // pole solution on those nodes in shared memory (relative to the tile centre,
 // in fp32, so gradients keep fp32 relative accuracy), then streams the data,
 // accumulating W_d^2 J_dc^2 per cell in fp32 per thread (sums of positive
-// terms; the per-thread sums are combined in fp64).  All per-datum arithmetic
-// is fp32: on this part fp64 issues at 1/64 of the fp32 rate.  Cost: nE pole
-// solves plus O(nD * nC) fp32 arithmetic with no J in memory.
+// terms; the per-thread sums are combined in fp64).  The per-datum arithmetic
+// is fp32 (the Robin term of boundary cells aside), and the per-datum currents
+// and weights are converted to fp32 once per call, not once per tile: on this
+// part fp64 arithmetic and the fp64 <-> fp32 conversions issue at 1/64 of the
+// fp32 rate.  Cost: nE pole solves plus O(nD * nC) fp32 arithmetic with no J
+// in memory.
 #include "../../include/dcgpu.h"
 #include "dc_internal.h"
 
@@ -28,11 +31,24 @@ namespace {
 constexpr int JTPB = 512;
 
 struct JtjData {
-  const int *sa, *sb, *rm, *rn;        // electrode indices (-1 = none)
-  const double *ia, *ib, *wm, *wn;     // currents / receiver weights
-  const double *w2;                    // squared data weights
+  const int *sa, *sb, *rm, *rn;  // electrode indices (-1 = none)
+  const float *w;                // fp32 [ia | ib | wm | wn | w2], nD each: currents, receiver weights,
+                                 // squared data weights
   int nD;
 };
+
+// The per-datum currents and weights in fp32, [ia | ib | wm | wn | w2]
+__global__ void k_jtj_weights(int nD, const double *__restrict__ ia, const double *__restrict__ ib,
+                              const double *__restrict__ wm, const double *__restrict__ wn,
+                              const double *__restrict__ w2, float *__restrict__ w) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nD; d += gridDim.x * blockDim.x) {
+    w[d] = (float)ia[d];
+    w[nD + d] = (float)ib[d];
+    w[2 * nD + d] = (float)wm[d];
+    w[3 * nD + d] = (float)wn[d];
+    w[4 * nD + d] = (float)w2[d];
+  }
+}
 
 __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ phi, int nE, long long N,
                                                     int nx, int ny, int nz, const double *__restrict__ h,
@@ -88,8 +104,9 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
   float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int d = threadIdx.x; d < D.nD; d += JTPB) {
     const int sa = D.sa[d], sb = D.sb[d], rm = D.rm[d], rn = D.rn[d];
-    const float ia = (float)D.ia[d], ib = sb >= 0 ? (float)D.ib[d] : 0.f;
-    const float wm = (float)D.wm[d], wn = rn >= 0 ? (float)D.wn[d] : 0.f;
+    const int nD = D.nD;
+    const float ia = D.w[d], ib = sb >= 0 ? D.w[nD + d] : 0.f;
+    const float wm = D.w[2 * nD + d], wn = rn >= 0 ? D.w[3 * nD + d] : 0.f;
     const float *pa = dphi + sa * 27, *pb = dphi + (sb >= 0 ? sb : sa) * 27;
     const float *pm = dphi + rm * 27, *pn = dphi + (rn >= 0 ? rn : rm) * 27;
     float u[27], l[27];
@@ -98,7 +115,7 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
       u[j] = ia * pa[j] + ib * pb[j];
       l[j] = wm * pm[j] + wn * pn[j];
     }
-    const float w2 = (float)D.w2[d];
+    const float w2 = D.w[4 * nD + d];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       if (!have[c]) continue;
@@ -178,11 +195,18 @@ int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD
     last_error() = std::string("dc_jtj_diag: ") + cudaGetErrorString(e);
     return DC_ERR_CUDA;
   }
-  JtjData D{sa, sb, rm, rn, ia, ib, wm, wn, w2, nD};
+  float *w32 = nullptr;
+  if (cudaMallocAsync((void **)&w32, sizeof(float) * 5 * (size_t)(nD > 0 ? nD : 1), stream) != cudaSuccess) {
+    last_error() = "dc_jtj_diag: cannot allocate the fp32 weights";
+    return DC_ERR_NOMEM;
+  }
+  if (nD > 0) k_jtj_weights<<<count_launch(dim3((nD + 255) / 256)), 256, 0, stream>>>(nD, ia, ib, wm, wn, w2, w32);
+  JtjData D{sa, sb, rm, rn, w32, nD};
   const int tiles = ((L.nx + 1) / 2) * ((L.ny + 1) / 2) * ((L.nz + 1) / 2);
   k_jtj_diag<<<count_launch(dim3(tiles)), JTPB, smem, stream>>>(
       phi, nE, L.dims.N, L.nx, L.ny, L.nz, L.d_h, robin ? L.d_bface : nullptr, L.bface_off[0], L.bface_off[1],
       L.bface_off[2], L.bface_off[3], L.bface_off[4], L.bface_off[5], dsig, D, diag);
+  cudaFreeAsync(w32, stream);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
     last_error() = std::string("dc_jtj_diag: ") + cudaGetErrorString(e);
