@@ -95,41 +95,76 @@ class SurveyTables:
     def __init__(self, mesh, source_list, nN):
         self.nN = int(nN)
         self.nSrc = len(source_list)
-        q_idx, q_val = [], []
+        # source term: every electrode of every source in one interpolation
+        locs, curs, sidx = [], [], []
         for s, src in enumerate(source_list):
-            idx, w = interp_weights(mesh, src.location)
+            L = np.atleast_2d(np.asarray(src.location, dtype=np.float64))
             cur = np.asarray(src.electrode_currents() if hasattr(src, "electrode_currents") else src.current,
-                             dtype=np.float64)
-            if cur.size == 1 and idx.shape[0] > 1:
-                cur = np.full(idx.shape[0], cur[0])
-            q_idx.append(idx.ravel() + s * self.nN)
-            q_val.append((cur[:, None] * w).ravel())
-        qi = np.concatenate(q_idx) if q_idx else np.zeros(0, np.int64)
-        qv = np.concatenate(q_val) if q_val else np.zeros(0)
+                             dtype=np.float64).ravel()
+            if cur.size == 1 and L.shape[0] > 1:
+                cur = np.full(L.shape[0], cur[0])
+            locs.append(L)
+            curs.append(cur)
+            sidx.append(np.full(L.shape[0], s, dtype=np.int64))
+        if locs:
+            idx, w = interp_weights(mesh, np.concatenate(locs))
+            qi = (idx + (np.concatenate(sidx) * self.nN)[:, None]).ravel()
+            qv = (np.concatenate(curs)[:, None] * w).ravel()
+        else:
+            qi, qv = np.zeros(0, np.int64), np.zeros(0)
         Q = sp.csr_matrix((qv, (np.zeros_like(qi), qi)), shape=(1, self.nN * max(self.nSrc, 1)))
         Q.sum_duplicates()
         self.q_idx = Q.indices.astype(np.int64)
         self.q_val = Q.data.astype(np.float64)
 
-        rows = []
-        owner = []
+        # receivers: all M electrodes in one interpolation, all N electrodes in another; a datum's
+        # row is interp(M) - interp(N) (duplicates summed), then scaled by 1/geometric factor for
+        # apparent resistivity
+        m_locs, m_rows, m_src, n_locs, n_rows, n_src, fac, owner = [], [], [], [], [], [], [], []
+        d0 = 0
         for s, src in enumerate(source_list):
             for rx in src.receiver_list:
-                P = rx_projection(mesh, rx).tocoo()
-                fac = None
+                dipole = isinstance(rx, Rx.Dipole) or isinstance(getattr(rx, "locations", None), (list, tuple))
+                M = np.atleast_2d(np.asarray(rx.locations[0] if dipole else rx.locations, dtype=np.float64))
+                n = M.shape[0]
+                rows = np.arange(d0, d0 + n, dtype=np.int64)
+                m_locs.append(M)
+                m_rows.append(rows)
+                m_src.append(np.full(n, s, dtype=np.int64))
+                if dipole:
+                    n_locs.append(np.atleast_2d(np.asarray(rx.locations[1], dtype=np.float64)))
+                    n_rows.append(rows)
+                    n_src.append(np.full(n, s, dtype=np.int64))
+                f = np.ones(n)
                 if rx.data_type == "apparent_resistivity":
                     try:
-                        fac = 1.0 / np.asarray(rx.geometric_factor[src], dtype=np.float64)
+                        f = 1.0 / np.asarray(rx.geometric_factor[src], dtype=np.float64)
                     except KeyError:
                         raise KeyError(
                             "Receiver geometric factor has not been set, please execute survey.set_geometric_factor()"
                         )
-                data = P.data * (fac[P.row] if fac is not None else 1.0)
-                rows.append(sp.csr_matrix((data, (P.row, P.col + s * self.nN)), shape=(P.shape[0], self.nN * self.nSrc)))
-                owner.append(np.full(P.shape[0], s, dtype=np.int64))
+                fac.append(f)
+                owner.append(np.full(n, s, dtype=np.int64))
+                d0 += n
         self.owner = np.concatenate(owner) if owner else np.zeros(0, np.int64)
-        self.P = sp.vstack(rows, format="csr") if rows else sp.csr_matrix((0, self.nN * max(self.nSrc, 1)))
-        self.P.sum_duplicates()
+        ncol = self.nN * max(self.nSrc, 1)
+        if d0:
+            parts_r, parts_c, parts_v = [], [], []
+            for locs_, rows_, src_, sign in ((m_locs, m_rows, m_src, 1.0), (n_locs, n_rows, n_src, -1.0)):
+                if not locs_:
+                    continue
+                idx, w = interp_weights(mesh, np.concatenate(locs_))
+                parts_r.append(np.repeat(np.concatenate(rows_), 8))
+                parts_c.append((idx + (np.concatenate(src_) * self.nN)[:, None]).ravel())
+                parts_v.append(sign * w.ravel())
+            P = sp.csr_matrix((np.concatenate(parts_v), (np.concatenate(parts_r), np.concatenate(parts_c))),
+                              shape=(d0, ncol))
+            P.sum_duplicates()
+            P.eliminate_zeros()
+            P.data = P.data * np.concatenate(fac)[np.repeat(np.arange(d0), np.diff(P.indptr))]
+            self.P = P
+        else:
+            self.P = sp.csr_matrix((0, ncol))
         self.nD = self.P.shape[0]
         # transpose restricted to its nonzero rows, built from P's entries (sorted by
         # column, then datum) without materialising the nSrc*nN-row CSR
