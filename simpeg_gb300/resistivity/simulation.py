@@ -432,60 +432,61 @@ class Simulation3DNodal:
 
     def _electrode_tables(self):
         """Unique electrodes and, per datum, its source/receiver electrodes and weights."""
-        locs, rows = [], []
-        for src in self.survey.source_list:
-            L = np.atleast_2d(src.location)
+        src_pts, src_cur, d_src, M_all, N_all, has_n, fac_all = [], [], [], [], [], [], []
+        for s, src in enumerate(self.survey.source_list):
+            L = np.atleast_2d(np.asarray(src.location, dtype=np.float64))
             if L.shape[0] > 2:
                 return None
             cur = np.asarray(src.electrode_currents() if hasattr(src, "electrode_currents") else src.current,
-                             dtype=np.float64)
+                             dtype=np.float64).ravel()
             if cur.size == 1 and L.shape[0] > 1:
                 cur = np.full(L.shape[0], cur[0])
+            src_pts.append(L)
+            src_cur.append(cur)
             for rx in src.receiver_list:
-                fac = np.ones(rx.nD)
+                n = rx.nD
+                fac = np.ones(n)
                 if rx.data_type == "apparent_resistivity":
                     fac = 1.0 / np.asarray(rx.geometric_factor[src], dtype=np.float64)
                 if isinstance(rx.locations, (list, tuple)):
-                    Ms, Ns = np.atleast_2d(rx.locations[0]), np.atleast_2d(rx.locations[1])
+                    M_all.append(np.atleast_2d(np.asarray(rx.locations[0], dtype=np.float64)))
+                    N_all.append(np.atleast_2d(np.asarray(rx.locations[1], dtype=np.float64)))
+                    has_n.append(np.ones(n, dtype=bool))
                 else:
-                    Ms, Ns = np.atleast_2d(rx.locations), None
-                for d in range(rx.nD):
-                    rows.append((L, cur, Ms[d], None if Ns is None else Ns[d], fac[d]))
-        if not rows:
+                    M = np.atleast_2d(np.asarray(rx.locations, dtype=np.float64))
+                    M_all.append(M)
+                    N_all.append(M)  # placeholder rows, not used (has_n False)
+                    has_n.append(np.zeros(n, dtype=bool))
+                fac_all.append(np.broadcast_to(fac, (n,)))
+                d_src.append(np.full(n, s, dtype=np.int64))
+        if not d_src:
             return None
-        for L, cur, M, N, _ in rows:
-            locs.extend(list(L))
-            locs.append(M)
-            if N is not None:
-                locs.append(N)
-        allp = np.asarray(locs, dtype=np.float64)
+        d_src = np.concatenate(d_src)
+        M_all, N_all = np.concatenate(M_all), np.concatenate(N_all)
+        has_n = np.concatenate(has_n)
+        fac = np.concatenate(fac_all)
+        n_e = np.array([L.shape[0] for L in src_pts])
+        first = np.r_[0, np.cumsum(n_e)[:-1]]
+        # one table of all electrode positions: the sources', the M's and the used N's
+        allp = np.concatenate(src_pts + [M_all, N_all[has_n]])
         uniq, inv = np.unique(allp, axis=0, return_inverse=True)
-        inv = np.asarray(inv).ravel()
-        nD = len(rows)
-        sa = np.full(nD, -1, np.int32)
-        sb = np.full(nD, -1, np.int32)
-        rm = np.full(nD, -1, np.int32)
+        inv = np.asarray(inv).ravel().astype(np.int32)
+        n_src_pts, nD = int(n_e.sum()), d_src.size
+        e_src = inv[:n_src_pts]
+        e_m = inv[n_src_pts:n_src_pts + nD]
+        e_n = inv[n_src_pts + nD:]
+        cur_first = np.array([c[0] for c in src_cur])
+        cur_second = np.array([c[1] if c.size > 1 else 0.0 for c in src_cur])
+        two = n_e[d_src] == 2
+        sa = e_src[first[d_src]].astype(np.int32)
+        sb = np.where(two, e_src[np.minimum(first[d_src] + 1, n_src_pts - 1)], -1).astype(np.int32)
+        ia = cur_first[d_src].astype(np.float64)
+        ib = np.where(two, cur_second[d_src], 0.0)
+        rm = e_m.astype(np.int32)
         rn = np.full(nD, -1, np.int32)
-        ia = np.zeros(nD)
-        ib = np.zeros(nD)
-        wm = np.zeros(nD)
-        wn = np.zeros(nD)
-        pos = 0
-        for d, (L, cur, M, N, fac) in enumerate(rows):
-            sa[d] = inv[pos]
-            ia[d] = cur[0]
-            pos += 1
-            if L.shape[0] == 2:
-                sb[d] = inv[pos]
-                ib[d] = cur[1]
-                pos += 1
-            rm[d] = inv[pos]
-            wm[d] = fac
-            pos += 1
-            if N is not None:
-                rn[d] = inv[pos]
-                wn[d] = -fac
-                pos += 1
+        rn[has_n] = e_n
+        wm = fac.astype(np.float64).copy()
+        wn = np.where(has_n, -fac, 0.0)
         return uniq, dict(sa=sa, sb=sb, rm=rm, rn=rn, ia=ia, ib=ib, wm=wm, wn=wn)
 
     def _jtj_diag_reciprocity(self, w):
