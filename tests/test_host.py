@@ -216,3 +216,19 @@ def test_device_map_transforms_match_host():
     for mp in (maps.IdentityMap(nP=50), maps.ExpMap(nP=50), maps.ReciprocalMap(nP=50),
                maps.ExpMap(nP=50) * maps.ReciprocalMap(nP=50)):
         np.testing.assert_allclose(mp.transform_dev(torch.from_numpy(m)).numpy(), mp * m, rtol=1e-15)
+
+
+def test_double_float_bit_routines(tmp_path):
+    """The bit-level double-float split and widening (csrc/dc_dfbits.h), compiled for
+    the host: truncation split exact to 2^-48, widening equal to the fp32 -> fp64
+    conversion, out-of-range values rejected (they take the fp64 instructions)."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "dfbits_check"
+    subprocess.run([cxx, "-O2", "-std=c++17", str(ROOT / "tests" / "dfbits_check.cpp"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
