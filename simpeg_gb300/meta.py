@@ -147,13 +147,14 @@ class MetaSimulation:
         import torch
 
         if self._streams is None:
-            self._streams = [torch.cuda.Stream() for _ in items]
+            # one stream per child, on the child's own device
+            self._streams = [torch.cuda.Stream(device=getattr(sim, "device", None)) for _, _, sim in items]
         caller = torch.cuda.current_stream()
+        caller.synchronize()  # inputs the caller produced on its stream are ready for every child
 
         def run(it):
             s = self._streams[it[0]]
-            s.wait_stream(caller)  # inputs the caller produced on its stream are ready
-            with torch.cuda.stream(s):
+            with torch.cuda.device(s.device), torch.cuda.stream(s):
                 out = fn(*it)
             s.synchronize()  # the child's results are complete when its thread returns
             return out
