@@ -358,6 +358,8 @@ class Simulation3DNodal:
 
         Same operations as :meth:`Jvec` (``simulation.py:156-187``) without host round trips:
         ``-dA/dm v`` by the stencil kernel, one multi-RHS solve, receiver gather."""
+        if self._mini_survey is not None:
+            raise NotImplementedError("device products need miniaturize=False (use Jvec)")
         f = f if f is not None else self._fields_for(self._model, None)
         d = self._sigma_deriv()
         if not isinstance(d, np.ndarray):
@@ -368,6 +370,8 @@ class Simulation3DNodal:
 
     def jtvec_dev(self, w_dev, f=None):
         """J^T w with w a device tensor (nD,) at the current model; returns a device tensor (nP,)."""
+        if self._mini_survey is not None:
+            raise NotImplementedError("device products need miniaturize=False (use Jtvec)")
         f = f if f is not None else self._fields_for(self._model, None)
         t, tq = self._get_tables()
         PTv = torch.zeros(t.nSrc, self.nN, dtype=torch.float64, device=self.device)
