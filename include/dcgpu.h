@@ -62,7 +62,8 @@ int dc_create(int nx, int ny, int nz, const double *hx, const double *hy, const 
 void dc_destroy(dc_handle *h);
 const char *dc_last_error(void);
 
-/* Smoother / hierarchy parameters (before dc_set_model).  Non-positive values keep defaults. */
+/* Smoother / hierarchy parameters (before dc_set_model).  Non-positive values keep defaults:
+ * nu_pre = nu_post = 3, cheb_ratio = 30, coarse_max = 64 nodes (<= 4096), check_every = 1. */
 int dc_set_params(dc_handle *h, int nu_pre, int nu_post, double cheb_ratio, int coarse_max, int check_every);
 
 /* Multigrid coarsening (before the first dc_set_model).  merge = 0: full

@@ -242,7 +242,7 @@ struct dc_handle {
   bool model_set = false;
   int nu_pre = 3, nu_post = 3;
   double cheb_ratio = 30.0;
-  int coarse_max = 200;
+  int coarse_max = 64;  // nodes of the coarsest level (dense Cholesky); 64 halves dc_set_model vs 200 at equal iterations
   double coarsen_merge = 1.0;  // selective coarsening factor (dc_set_coarsening); 0 = full coarsening
   int check_every = 1;
   int mg_storage = DC_MG_FP16;  // mixed solve: storage of the multigrid vectors (dc_set_mg_storage)

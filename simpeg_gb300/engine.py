@@ -63,7 +63,7 @@ class DCEngine:
         0 = halve every axis at every level)
     """
 
-    def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=200, check_every=1,
+    def __init__(self, h, bface=None, nu_pre=3, nu_post=3, cheb_ratio=30.0, coarse_max=64, check_every=1,
                  mg_storage="fp16", smoother=1, coarsening=1.0):
         if not torch.cuda.is_available():
             raise RuntimeError("the DC engine needs a CUDA device")
