@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["BaseSrc", "Pole", "Dipole"]
+__all__ = ["BaseSrc", "Pole", "Multipole", "Dipole"]
 
 
 def _as_locations(loc):
@@ -92,6 +92,23 @@ class Pole(BaseSrc):
 
     def __repr__(self):
         return f"Pole(a: {self.location[0]})"
+
+
+class Multipole(BaseSrc):
+    """Any number of current electrodes, one current each (``sources.py:107-132``)."""
+
+    def __init__(self, receiver_list=None, location=None, current=1.0):
+        if location is None:
+            raise TypeError("Multipole source needs the electrode locations")
+        super().__init__(receiver_list, location, current=current)
+
+    @property
+    def location_a(self):
+        return self.location
+
+    @property
+    def location_b(self):
+        return np.full_like(self.location, np.nan)
 
 
 class Dipole(BaseSrc):

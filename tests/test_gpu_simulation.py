@@ -241,3 +241,19 @@ def test_derived_fields_vs_oracle(cuda, block_case):
     src = survey.source_list[3]
     np.testing.assert_allclose(f[src, "e"], e0[:, 3], rtol=1e-12, atol=1e-12 * np.abs(e0).max())
     assert f._GLoc("e") == "E" and f._GLoc("phi") == "N"
+
+
+def test_multipole_fullspace_fields_gpu(cuda):
+    """tests/em/static/test_DC_FieldsMultipoleFullspace.py:284-305 on the GPU path: a
+    Multipole source in a whole space; f[src_list, "e"] and "j" within 10 % of the analytic
+    field on the region of interest, charge and charge density available."""
+    from test_oracle import _multipole_fullspace
+
+    mesh, sigma, survey, e_ana, roi = _multipole_fullspace()
+    sim = Simulation3DNodal(mesh, survey=survey, sigma=sigma, rtol=1e-10)
+    f = sim.fields()
+    e = f[survey.source_list, "e"].ravel()
+    j = f[survey.source_list, "j"].ravel()
+    assert _rel(e[roi], e_ana[roi]) < 0.1
+    assert _rel(j[roi], 1e-2 * e_ana[roi]) < 0.1
+    assert np.all(np.isfinite(f[:, "charge"])) and np.all(np.isfinite(f[:, "charge_density"]))

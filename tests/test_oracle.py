@@ -275,3 +275,47 @@ def test_derived_fields_of_a_uniform_gradient():
     np.testing.assert_allclose(q3[:, :, 0].sum(), -q3[:, :, -1].sum(), rtol=1e-12)
     rho3 = rho.reshape((nz, ny, nx))
     assert np.all(np.abs(rho3[:, :, 1:-1]) <= 1e-12 * np.abs(rho).max())
+
+
+def _multipole_fullspace():
+    """tests/em/static/test_DC_FieldsMultipoleFullspace.py:185-282: a three-electrode source
+    (+1, +1, -2 A) in a 0.01 S/m whole space on a padded mesh; the analytic electric field is
+    the sum of the point-source fields I (x - x_k) / (4 pi sigma |x - x_k|^3) (the reference
+    writes it as two finite electric dipoles, the same field), compared on the edges outside
+    a 4 m box around the source."""
+    cs = 0.5
+    h = [(cs, 11, -1.5), (cs, 15), (cs, 11, 1.5)]
+    mesh = TensorMesh([h, h, h], origin="CCC")
+    sigma = np.full(mesh.n_cells, 1e-2)
+    locs = np.array([[2.25, 0.0, 0.0], [1.25, 0.0, 0.0], [-0.25, 0.0, 0.0]])
+    currents = np.array([1.0, 1.0, -2.0])
+    src = sources.Multipole([], location=locs, current=currents)
+    grids = [TensorMesh._ndgrid(mesh.cell_centers_x, mesh.nodes_y, mesh.nodes_z),
+             TensorMesh._ndgrid(mesh.nodes_x, mesh.cell_centers_y, mesh.nodes_z),
+             TensorMesh._ndgrid(mesh.nodes_x, mesh.nodes_y, mesh.cell_centers_z)]
+    e_ana = []
+    for axis, g in enumerate(grids):
+        r = g[:, None, :] - locs[None, :, :]
+        dist = np.linalg.norm(r, axis=-1)
+        e_ana.append((currents[None, :] * r[..., axis] / (4 * np.pi * 1e-2 * dist ** 3)).sum(axis=1))
+    e_ana = np.concatenate(e_ana)
+    pts = np.vstack(grids)
+    inside = lambda a: np.all((pts >= -a) & (pts <= a), axis=1)
+    roi = inside(75.0) & ~inside(4.0)
+    return mesh, sigma, Survey([src]), e_ana, roi
+
+
+@pytest.mark.slow
+def test_multipole_fullspace_derived_fields():
+    """The derived fields e and j = sigma e of the oracle within 10 % of the analytic
+    whole-space field (the reference's tolerance), charge and density finite."""
+    from scipy.constants import epsilon_0
+
+    mesh, sigma, survey, e_ana, roi = _multipole_fullspace()
+    o = OracleDC3DNodal(mesh, survey, sigma=sigma)
+    phi = o.fields()[:, 0]
+    e, j, q, rho = o.derived_fields(phi, epsilon_0)
+    err_e = np.linalg.norm(e[roi] - e_ana[roi]) / np.linalg.norm(e_ana[roi])
+    err_j = np.linalg.norm(j[roi] - 1e-2 * e_ana[roi]) / np.linalg.norm(1e-2 * e_ana[roi])
+    assert err_e < 0.1 and err_j < 0.1, (err_e, err_j)
+    assert np.all(np.isfinite(q)) and np.all(np.isfinite(rho))
