@@ -29,6 +29,17 @@ class Survey:
         self.survey_geometry = survey_geometry
 
     @property
+    def survey_type(self):
+        """Removed in the reference (``survey.py:57-72``): sources and receivers carry their type."""
+        raise AttributeError("'survey_type' has been removed.")
+
+    @property
+    def source_locations(self):
+        """[A locations, B locations] of every source, in order (``survey.py:150-166``)."""
+        return [np.vstack([np.atleast_2d(src.location_a) for src in self.source_list]),
+                np.vstack([np.atleast_2d(src.location_b) for src in self.source_list])]
+
+    @property
     def nSrc(self):
         return len(self.source_list)
 

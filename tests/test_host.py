@@ -232,3 +232,24 @@ def test_double_float_bit_routines(tmp_path):
     subprocess.run([cxx, "-O2", "-std=c++17", str(ROOT / "tests" / "dfbits_check.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_survey_source_locations_and_multipole():
+    """Survey.source_locations (survey.py:150-166): A and B rows per source in order, NaN B
+    for poles; Multipole sources keep all electrodes as A (sources.py:107-132)."""
+    from simpeg_gb300.resistivity import receivers, sources
+    from simpeg_gb300.resistivity.survey import Survey
+
+    rx = receivers.Pole(np.zeros((1, 3)))
+    sv = Survey([sources.Pole([rx], np.r_[1.0, 0, 0]), sources.Dipole([rx], np.r_[0.0, 0, 0], np.r_[2.0, 0, 0])])
+    a, b = sv.source_locations
+    np.testing.assert_array_equal(a, [[1.0, 0, 0], [0.0, 0, 0]])
+    assert np.isnan(b[0]).all()
+    np.testing.assert_array_equal(b[1], [2.0, 0, 0])
+    with pytest.raises(AttributeError):
+        sv.survey_type
+    mp = sources.Multipole([rx], location=[[0.0, 0, 0], [1.0, 0, 0], [2.0, 0, 0]], current=[1.0, 1.0, -2.0])
+    assert mp.location_a.shape == (3, 3) and np.isnan(mp.location_b).all()
+    np.testing.assert_array_equal(mp.electrode_currents(), [1.0, 1.0, -2.0])
+    with pytest.raises(ValueError):
+        sources.Multipole([rx], location=[[0.0, 0, 0], [1.0, 0, 0]], current=[1.0, 1.0, -2.0])
