@@ -257,6 +257,60 @@ class Simulation3DNodal:
 
     getSourceTerm = getRHS
 
+    # ------------------------------------------------------------ operator access (host arrays)
+    def _to_dev_cols(self, a):
+        a = np.asarray(a, dtype=np.float64)
+        one = a.ndim == 1
+        t = torch.from_numpy(np.ascontiguousarray((a[:, None] if one else a).T)).to(self.device)
+        return t, one
+
+    def getA(self):
+        """A(sigma) at the current model (``simulation.py:523-555``) as a scipy ``LinearOperator``
+        (nN x nN): ``A @ x`` runs the matrix-free stencil on the GPU, A is never assembled.  With
+        Neumann conditions row 0 is the identity row, as in the reference's pinned matrix."""
+        from scipy.sparse.linalg import LinearOperator
+
+        self._ensure_model()
+        pinned = self.bc_type == "Neumann"
+
+        def sym(X):  # the symmetric operator the stencil applies (no pinned row)
+            T, one = self._to_dev_cols(X)
+            Y = self.engine.apply(T).cpu().numpy().T
+            return Y[:, 0] if one else Y
+
+        def mat(X):
+            Y = sym(X)
+            if pinned:
+                Y[0] = np.asarray(X)[0]
+            return Y
+
+        def rmat(X):
+            X = np.asarray(X, dtype=np.float64)
+            if not pinned:
+                return sym(X)
+            # rows i >= 1 of A are those of the symmetric S, row 0 is e0: A^T x = S x' + e0 x0, x' = x with x0 = 0
+            Xs = X.copy()
+            Xs[0] = 0.0
+            Y = sym(Xs)
+            Y[0] += X[0]
+            return Y
+
+        return LinearOperator((self.nN, self.nN), matvec=mat, matmat=mat, rmatvec=rmat, rmatmat=rmat,
+                              dtype=np.float64)
+
+    def getADeriv(self, u, v, adjoint=False):
+        """dA/dm products (``simulation.py:557-571``) on host arrays.  Forward: u (nN,) or (nN, k),
+        v (nP,) -> (nN,) or (nN, k).  Adjoint: u and v (nN,) or (nN, k) -> (nP,), summed over the k
+        columns.  Stencil kernels on the GPU (``dc_dadm_fwd`` / ``dc_dadm_adj``)."""
+        self._ensure_model()
+        U, one = self._to_dev_cols(u)
+        if not adjoint:
+            R = self.engine.dadm_fwd(U, self._dsig_dev(v), scale=1.0).cpu().numpy().T
+            return R[:, 0] if one else R
+        L, _ = self._to_dev_cols(v)
+        g = self.engine.dadm_adj(U, L, None, scale=1.0).cpu().numpy()
+        return self._map_adjoint(g)
+
     # ------------------------------------------------------------ forward
     def fields(self, m=None, calcJ=True):
         if m is not None:
