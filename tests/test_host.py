@@ -253,3 +253,97 @@ def test_survey_source_locations_and_multipole():
     np.testing.assert_array_equal(mp.electrode_currents(), [1.0, 1.0, -2.0])
     with pytest.raises(ValueError):
         sources.Multipole([rx], location=[[0.0, 0, 0], [1.0, 0, 0]], current=[1.0, 1.0, -2.0])
+
+
+def _mixed_survey(mesh):
+    """Pole, dipole and multipole sources; pole and dipole receivers, volt and apparent
+    resistivity; some electrodes exactly on nodes (interpolation weights of 0 and 1)."""
+    from simpeg_gb300.resistivity import receivers, sources
+    from simpeg_gb300.resistivity.survey import Survey
+
+    xs = np.arange(-40.0, 41.0, 10.0)
+    srcs = []
+    M = np.c_[xs[4:7], np.zeros(3), np.zeros(3)]
+    N = np.c_[xs[5:8], np.zeros(3), np.zeros(3)]
+    srcs.append(sources.Dipole([receivers.Dipole(M, N), receivers.Pole(M, data_type="apparent_resistivity")],
+                               np.r_[-40.0, 0, 0], np.r_[-30.0, 0, 0]))
+    srcs.append(sources.Pole([receivers.Dipole(M + np.r_[3.3, 0, 0], N + np.r_[3.3, 0, 0], data_type="apparent_resistivity")],
+                             np.r_[-25.0, 2.5, 0.0]))
+    srcs.append(sources.Multipole([receivers.Pole(np.c_[xs[:3], np.full(3, 7.5), np.zeros(3)])],
+                                  location=[[-10.0, 0, 0], [0.0, 5.0, 0], [10.0, -5.0, 0]], current=[1.0, 1.0, -2.0]))
+    sv = Survey(srcs)
+    sv.set_geometric_factor()
+    return sv
+
+
+def test_survey_tables_mixed_survey_match_oracle():
+    """The survey tables (one interpolation per electrode kind) reproduce the oracle's
+    source term and per-receiver projections, apparent-resistivity scaling included."""
+    from simpeg_gb300.mesh import TensorMesh
+
+    mesh = TensorMesh([[(10.0, 3, -1.3), (10.0, 10), (10.0, 3, 1.3)], [(10.0, 3, -1.3), (10.0, 6), (10.0, 3, 1.3)],
+                       [(10.0, 3, -1.3), (10.0, 5)]], origin="CCN")
+    survey = _mixed_survey(mesh)
+    t = SurveyTables(mesh, survey.source_list, mesh.n_nodes)
+    o = OracleDC3DNodal(mesh, survey, sigma=np.full(mesh.n_cells, 0.01))
+    q = np.zeros(mesh.n_nodes * survey.nSrc)
+    q[t.q_idx] = t.q_val
+    np.testing.assert_allclose(q.reshape(survey.nSrc, -1).T, o.getRHS(), rtol=1e-15, atol=1e-15)
+    row = 0
+    for s, P, fac in o._projections():
+        blk = t.P[row:row + P.shape[0], s * mesh.n_nodes:(s + 1) * mesh.n_nodes].toarray()
+        ref = P.toarray() * (fac[:, None] if fac is not None else 1.0)
+        np.testing.assert_allclose(blk, ref, rtol=1e-14, atol=1e-14 * np.abs(ref).max())
+        np.testing.assert_array_equal(t.owner[row:row + P.shape[0]], s)
+        row += P.shape[0]
+    assert row == t.nD == survey.nD
+
+
+def test_electrode_tables_mixed_survey():
+    """Per-datum electrode indices and weights of the reciprocity JtJ diagonal, checked
+    against a per-datum restatement: electrode k of datum d is uniq[idx]; currents of the
+    source's A (B) electrode; receiver weights +-1/geometric factor for apparent resistivity."""
+    from simpeg_gb300.mesh import TensorMesh
+    from simpeg_gb300.resistivity.simulation import Simulation3DNodal
+
+    mesh = TensorMesh([[(10.0, 3, -1.3), (10.0, 10), (10.0, 3, 1.3)], [(10.0, 3, -1.3), (10.0, 6), (10.0, 3, 1.3)],
+                       [(10.0, 3, -1.3), (10.0, 5)]], origin="CCN")
+    survey = _mixed_survey(mesh)
+    survey_2 = type(survey)([s for s in survey.source_list if np.atleast_2d(s.location).shape[0] <= 2])
+
+    class Host:
+        pass
+
+    h = Host()
+    h.survey = survey
+    assert Simulation3DNodal._electrode_tables(h) is None  # a three-electrode source: no reciprocity tables
+    h.survey = survey_2
+    uniq, t = Simulation3DNodal._electrode_tables(h)
+    d = 0
+    for src in survey_2.source_list:
+        L = np.atleast_2d(src.location)
+        cur = src.electrode_currents()
+        for rx in src.receiver_list:
+            fac = np.ones(rx.nD)
+            if rx.data_type == "apparent_resistivity":
+                fac = 1.0 / np.asarray(rx.geometric_factor[src])
+            dip = isinstance(rx.locations, (list, tuple))
+            Ms = np.atleast_2d(rx.locations[0] if dip else rx.locations)
+            for i in range(rx.nD):
+                np.testing.assert_array_equal(uniq[t["sa"][d]], L[0])
+                assert t["ia"][d] == cur[0]
+                if L.shape[0] == 2:
+                    np.testing.assert_array_equal(uniq[t["sb"][d]], L[1])
+                    assert t["ib"][d] == cur[1]
+                else:
+                    assert t["sb"][d] == -1 and t["ib"][d] == 0.0
+                np.testing.assert_array_equal(uniq[t["rm"][d]], Ms[i])
+                assert t["wm"][d] == fac[i]
+                if dip:
+                    np.testing.assert_array_equal(uniq[t["rn"][d]], np.atleast_2d(rx.locations[1])[i])
+                    assert t["wn"][d] == -fac[i]
+                else:
+                    assert t["rn"][d] == -1 and t["wn"][d] == 0.0
+                d += 1
+    assert d == t["sa"].size
+    assert len(np.unique(uniq, axis=0)) == len(uniq)
