@@ -16,6 +16,27 @@ from . import receivers, sources
 from .survey import Survey
 
 
+def WennerSrcList(n_electrodes, a_spacing, in2D=False, plotIt=False):
+    """Dipole sources of a Wenner array (``resistivity/utils.py:13-74``): electrodes
+    ``a_spacing`` apart on a line centred on x = 0; for every spacing s = 1, 2, ... and first
+    electrode j with j + 3 s < n_electrodes, source A = e_j, B = e_(j+3s) with one dipole
+    receiver M = e_(j+s), N = e_(j+2s).  Locations are (x, 0, 0), or (x, 0) with ``in2D``."""
+    if plotIt:
+        raise NotImplementedError("plotting is not part of this package")
+    n = int(n_electrodes)
+    x = a_spacing * np.arange(n) - a_spacing * (n - 1) / 2.0
+
+    def loc(i):
+        return np.r_[x[i], 0.0] if in2D else np.r_[x[i], 0.0, 0.0]
+
+    out = []
+    for s in range(1, n):
+        for j in range(n - 3 * s):
+            rx = receivers.Dipole(loc(j + s)[None, :], loc(j + 2 * s)[None, :])
+            out.append(sources.Dipole([rx], loc(j), loc(j + 3 * s)))
+    return out
+
+
 def mini_pole_pole(survey, verbose=False):
     A = survey.locations_a
     B = survey.locations_b

@@ -347,3 +347,20 @@ def test_electrode_tables_mixed_survey():
                 d += 1
     assert d == t["sa"].size
     assert len(np.unique(uniq, axis=0)) == len(uniq)
+
+
+def test_wenner_source_list():
+    """WennerSrcList (resistivity/utils.py:13-74): the 7-electrode, a = 10 array has the
+    spacing-1 quadruples (j, j+1, j+2, j+3), j = 0..3, then the spacing-2 one (0, 2, 4, 6)."""
+    from simpeg_gb300.resistivity.utils import WennerSrcList
+
+    srcs = WennerSrcList(7, 10.0)
+    x = 10.0 * np.arange(7) - 30.0
+    quads = [(0, 1, 2, 3), (1, 2, 3, 4), (2, 3, 4, 5), (3, 4, 5, 6), (0, 2, 4, 6)]
+    assert len(srcs) == len(quads)
+    for src, (a, m, n, b) in zip(srcs, quads):
+        np.testing.assert_array_equal(src.location, [[x[a], 0, 0], [x[b], 0, 0]])
+        (rx,) = src.receiver_list
+        np.testing.assert_array_equal(rx.locations[0], [[x[m], 0, 0]])
+        np.testing.assert_array_equal(rx.locations[1], [[x[n], 0, 0]])
+    assert len(WennerSrcList(5, 2.5)) == 2
