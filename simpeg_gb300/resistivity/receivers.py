@@ -11,6 +11,7 @@ the projection is an electrode gather (see ``electrodes.py``).
 from __future__ import annotations
 
 import numpy as np
+import scipy.sparse as sp
 
 __all__ = ["BaseRx", "Pole", "Dipole"]
 
@@ -53,6 +54,7 @@ class BaseRx:
         self.projField = "phi"
         self.storeProjections = storeProjections
         self._geometric_factor = {}
+        self._Ps = {}
 
     @property
     def data_type(self):
@@ -73,6 +75,56 @@ class BaseRx:
     @property
     def geometric_factor(self):
         return self._geometric_factor
+
+    # ------------------------------------------------------------ host projections
+    def getP(self, mesh, projected_grid="N", transpose=False):
+        """(nD, nN) interpolation of the potential at the receiver electrodes
+        (``receivers.py:379-424,461-498``): the trilinear node weights of M, minus those of
+        N for a dipole.  Only nodal potentials (``projected_grid`` "N") are on this path;
+        the simulation itself uses the same weights as device tables."""
+        if projected_grid not in ("N", "nodes"):
+            raise NotImplementedError("only nodal potentials ('N') are on the GPU path")
+        from .electrodes import rx_projection
+
+        P = self._Ps.get(id(mesh)) if self.storeProjections else None
+        if P is None:
+            P = rx_projection(mesh, self)
+            if self.storeProjections:
+                self._Ps[id(mesh)] = P
+        return P.toarray().T if transpose else P
+
+    def _factor(self, src):
+        if self.data_type != "apparent_resistivity":
+            return None
+        try:
+            return 1.0 / np.asarray(self.geometric_factor[src], dtype=np.float64)
+        except KeyError:
+            raise KeyError(
+                "Receiver geometric factor has not been set, please execute survey.set_geometric_factor()")
+
+    def eval(self, src, mesh, f):
+        """Data of this receiver for source ``src`` from the fields ``f`` (``receivers.py:156-192``):
+        ``P phi``, divided by the geometric factor for apparent resistivity."""
+        v = self.getP(mesh) @ np.asarray(f[src, "phiSolution"])
+        fac = self._factor(src)
+        return v if fac is None else fac * v
+
+    def evalDeriv(self, src, mesh, f, v=None, adjoint=False):
+        """Derivative of ``eval`` with respect to the potential (``receivers.py:194-244``): the
+        (scaled) projection itself when ``v`` is None (its transpose with ``adjoint``), else its
+        product with ``v``."""
+        P = self.getP(mesh)
+        fac = self._factor(src)
+        if v is None:
+            if fac is not None:
+                P = sp.diags(fac) @ P
+            return P.T if adjoint else P
+        if not adjoint:
+            out = P @ v
+            return out if fac is None else fac * out
+        if fac is not None:
+            v = fac * v
+        return P.T @ v
 
 
 class Pole(BaseRx):

@@ -364,3 +364,39 @@ def test_wenner_source_list():
         np.testing.assert_array_equal(rx.locations[0], [[x[m], 0, 0]])
         np.testing.assert_array_equal(rx.locations[1], [[x[n], 0, 0]])
     assert len(WennerSrcList(5, 2.5)) == 2
+
+
+def test_receiver_getP_eval_evalDeriv():
+    """Receiver projections on the host (receivers.py:156-244,379-498): getP equals the
+    oracle's interp(M) - interp(N); eval = P phi (/ geometric factor for apparent
+    resistivity); evalDeriv is P (scaled) and its transpose, consistent with eval."""
+    from oracle.dc3d import _rx_projection
+    from oracle.operators import MeshOps
+    from simpeg_gb300.mesh import TensorMesh
+
+    mesh = TensorMesh([[(10.0, 3, -1.3), (10.0, 10), (10.0, 3, 1.3)], [(10.0, 3, -1.3), (10.0, 6), (10.0, 3, 1.3)],
+                       [(10.0, 3, -1.3), (10.0, 5)]], origin="CCN")
+    survey = _mixed_survey(mesh)
+    ops = MeshOps(mesh.h, mesh.origin)
+    rng = np.random.default_rng(4)
+    phi = {id(s): rng.standard_normal(mesh.n_nodes) for s in survey.source_list}
+
+    class F:
+        def __getitem__(self, key):
+            return phi[id(key[0])]
+
+    for src in survey.source_list:
+        for rx in src.receiver_list:
+            P = rx.getP(mesh)
+            assert (P != _rx_projection(ops, rx)).nnz == 0
+            fac = 1.0 / rx.geometric_factor[src] if rx.data_type == "apparent_resistivity" else 1.0
+            np.testing.assert_allclose(rx.eval(src, mesh, F()), fac * (P @ phi[id(src)]), rtol=1e-14)
+            v = rng.standard_normal(mesh.n_nodes)
+            w = rng.standard_normal(rx.nD)
+            np.testing.assert_allclose(rx.evalDeriv(src, mesh, F(), v=v), fac * (P @ v), rtol=1e-14)
+            np.testing.assert_allclose(w @ rx.evalDeriv(src, mesh, F(), v=v),
+                                       v @ rx.evalDeriv(src, mesh, F(), v=w, adjoint=True), rtol=1e-12)
+            np.testing.assert_allclose(rx.evalDeriv(src, mesh, F()) @ v, fac * (P @ v), rtol=1e-14)
+            assert rx.getP(mesh, transpose=True).shape == (mesh.n_nodes, rx.nD)
+    with pytest.raises(NotImplementedError):
+        survey.source_list[0].receiver_list[0].getP(mesh, "CC")
