@@ -69,6 +69,23 @@ class BaseSrc:
             c = np.full(self.location.shape[0], c[0])
         return c
 
+    def eval(self, sim):
+        """Source term on the mesh nodes (``sources.py:64-88``, nodal formulation):
+        ``q = sum_k I_k interp_N(location_k)`` as a host array (nN,).  The simulation builds
+        the same term on the device from its electrode tables."""
+        if getattr(sim, "_formulation", "EB") != "EB":
+            raise NotImplementedError("only the nodal (EB) formulation is on the GPU path")
+        from .electrodes import interp_weights
+
+        idx, w = interp_weights(sim.mesh, self.location)
+        q = np.zeros(sim.mesh.n_nodes)
+        np.add.at(q, idx.ravel(), (self.electrode_currents()[:, None] * w).ravel())
+        return q
+
+    def evalDeriv(self, sim):
+        """The source term does not depend on the model (``sources.py:90-104``)."""
+        return 0.0
+
 
 class Pole(BaseSrc):
     """Single current electrode A with current ``+I``."""

@@ -400,3 +400,27 @@ def test_receiver_getP_eval_evalDeriv():
             assert rx.getP(mesh, transpose=True).shape == (mesh.n_nodes, rx.nD)
     with pytest.raises(NotImplementedError):
         survey.source_list[0].receiver_list[0].getP(mesh, "CC")
+
+
+def test_source_eval_matches_oracle_rhs():
+    """BaseSrc.eval (sources.py:64-88, nodal formulation) equals the oracle's source term
+    column for pole, dipole and multipole sources; evalDeriv is zero."""
+    from simpeg_gb300.mesh import TensorMesh
+
+    mesh = TensorMesh([[(10.0, 3, -1.3), (10.0, 10), (10.0, 3, 1.3)], [(10.0, 3, -1.3), (10.0, 6), (10.0, 3, 1.3)],
+                       [(10.0, 3, -1.3), (10.0, 5)]], origin="CCN")
+    survey = _mixed_survey(mesh)
+    rhs = OracleDC3DNodal(mesh, survey, sigma=np.full(mesh.n_cells, 0.01)).getRHS()
+
+    class Sim:
+        pass
+
+    sim = Sim()
+    sim.mesh = mesh
+    sim._formulation = "EB"
+    for i, src in enumerate(survey.source_list):
+        np.testing.assert_allclose(src.eval(sim), rhs[:, i], rtol=1e-15, atol=1e-15)
+        assert src.evalDeriv(sim) == 0.0
+    sim._formulation = "HJ"
+    with pytest.raises(NotImplementedError):
+        survey.source_list[0].eval(sim)
