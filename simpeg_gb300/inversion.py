@@ -39,7 +39,47 @@ def _p(t):
 
 
 class L2DataMisfit:
-    def __init__(self, simulation, dobs, W=None):
+    """``phi_d = ||W (d(m) - d_obs)||^2`` with diagonal W (``simpeg/data_misfit.py:238-343``).
+
+    Constructed as the reference constructs it, ``L2DataMisfit(data, simulation)``
+    (``W = diag(1 / data.standard_deviation)``, which must be positive), or as
+    ``L2DataMisfit(simulation, dobs, W=None)`` with the observed data and the weights
+    given directly (W: per-datum weights or a diagonal matrix; default ones).
+    """
+
+    def __init__(self, *args, data=None, simulation=None, dobs=None, W=None):
+        args = list(args)
+        if args and hasattr(args[0], "dobs") and hasattr(args[0], "standard_deviation"):
+            data = args.pop(0)  # the reference's positional order: (data, simulation)
+            if args:
+                simulation = args.pop(0)
+        else:
+            for name in ("simulation", "dobs", "W"):
+                if args:
+                    val = args.pop(0)
+                    if name == "simulation":
+                        simulation = val
+                    elif name == "dobs":
+                        dobs = val
+                    else:
+                        W = val
+        if args:
+            raise TypeError("too many positional arguments")
+        if simulation is None:
+            raise TypeError("L2DataMisfit needs a simulation")
+        self.data = data
+        if data is not None:
+            if dobs is not None:
+                raise TypeError("give the observed data either as data or as dobs")
+            dobs = data.dobs
+            if W is None:
+                std = data.standard_deviation
+                if std is None or np.any(np.asarray(std, dtype=np.float64) <= 0):
+                    raise ValueError("data.standard_deviation must be strictly positive to construct the W matrix: "
+                                     "set data.relative_error and/or data.noise_floor, or pass W")
+                W = 1.0 / np.asarray(std, dtype=np.float64)
+        if dobs is None:
+            raise TypeError("L2DataMisfit needs the observed data (data or dobs)")
         self.simulation = simulation
         dev = simulation.device
         self.dobs = torch.as_tensor(np.asarray(dobs, dtype=np.float64), device=dev)
@@ -68,6 +108,19 @@ class L2DataMisfit:
     def deriv2_dev(self, m, v_dev):
         sim = self.simulation
         return 2.0 * sim.jtvec_dev(self.w * self.w * sim.jvec_dev(v_dev))
+
+    @property
+    def nD(self):
+        return int(self.dobs.numel())
+
+    def deriv(self, m, f=None):
+        """Gradient ``2 J^T W^T W r`` as a host array (``data_misfit.py:280-304``)."""
+        return self.deriv_dev(m).cpu().numpy()
+
+    def deriv2(self, m, v, f=None):
+        """Gauss-Newton Hessian product ``2 J^T W^T W J v`` as a host array (``data_misfit.py:306-343``)."""
+        v_dev = torch.as_tensor(np.asarray(v, dtype=np.float64), device=self.simulation.device)
+        return self.deriv2_dev(m, v_dev).cpu().numpy()
 
 
 class WeightedLeastSquares:

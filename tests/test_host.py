@@ -424,3 +424,58 @@ def test_source_eval_matches_oracle_rhs():
     sim._formulation = "HJ"
     with pytest.raises(NotImplementedError):
         survey.source_list[0].eval(sim)
+
+
+def test_l2_data_misfit_forms_and_host_products():
+    """L2DataMisfit (data_misfit.py:238-343) built the reference's way, (data, simulation)
+    with W = 1 / standard deviation, or from dobs and W; phi_d, deriv and deriv2 against
+    dense algebra with a linear stand-in simulation on host tensors."""
+    import torch
+
+    from simpeg_gb300.data import Data
+    from simpeg_gb300.inversion import L2DataMisfit
+
+    rng = np.random.default_rng(8)
+    nD, nP = 12, 7
+    J = rng.standard_normal((nD, nP))
+    c = rng.standard_normal(nD)
+
+    class Fields:
+        pass
+
+    class LinearSim:
+        device = torch.device("cpu")
+
+        def _fields_for(self, m, f):
+            out = Fields()
+            out.phi_dev = torch.as_tensor(J @ np.asarray(m) + c)
+            return out
+
+        def _gather(self, phi):
+            return phi
+
+        def jvec_dev(self, v):
+            return torch.as_tensor(J) @ v
+
+        def jtvec_dev(self, w):
+            return torch.as_tensor(J.T) @ w
+
+    class Srv:
+        nD = 12
+
+    sim = LinearSim()
+    dobs = rng.standard_normal(nD)
+    data = Data(Srv(), dobs=dobs, relative_error=0.05, noise_floor=1e-3)
+    std = np.sqrt((0.05 * np.abs(dobs)) ** 2 + 1e-6)
+    m = rng.standard_normal(nP)
+    v = rng.standard_normal(nP)
+    for dm in (L2DataMisfit(data, sim), L2DataMisfit(data=data, simulation=sim), L2DataMisfit(sim, dobs, W=1 / std)):
+        w = 1 / std
+        r = J @ m + c - dobs
+        np.testing.assert_allclose(dm(m), np.sum((w * r) ** 2), rtol=1e-12)
+        np.testing.assert_allclose(dm.deriv(m), 2 * J.T @ (w * w * r), rtol=1e-12)
+        np.testing.assert_allclose(dm.deriv2(m, v), 2 * J.T @ (w * w * (J @ v)), rtol=1e-12)
+        assert dm.nD == nD
+    with pytest.raises(ValueError):
+        L2DataMisfit(Data(Srv(), dobs=dobs), sim)  # no uncertainties: no W
+    np.testing.assert_allclose(L2DataMisfit(sim, dobs).W, np.ones(nD))
