@@ -123,12 +123,35 @@ class L2DataMisfit:
         return self.deriv2_dev(m, v_dev).cpu().numpy()
 
 
+class _EngineHolder:
+    """What the regularization needs of a simulation: an engine on the mesh, its device, nC."""
+
+    def __init__(self, mesh):
+        from .engine import DCEngine
+
+        self.engine = DCEngine(mesh.h, None)
+        self.device = torch.device("cuda")
+        self.nC = self.engine.nC
+
+
 class WeightedLeastSquares:
-    def __init__(self, mesh, simulation, alpha_s=1.0, alpha_x=None, alpha_y=None, alpha_z=None,
+    """Smallness + first-order smoothness on an all-active tensor mesh
+    (``simpeg/regularization/base.py``), applied on the device by ``dc_reg_apply``.
+
+    ``WeightedLeastSquares(mesh, simulation, ...)`` uses the simulation's engine; as in
+    the reference, ``WeightedLeastSquares(mesh, ...)`` (or with an ``active_cells`` mask
+    that keeps every cell) gives the regularization an engine of its own."""
+
+    def __init__(self, mesh, simulation=None, alpha_s=1.0, alpha_x=None, alpha_y=None, alpha_z=None,
                  length_scale_x=None, length_scale_y=None, length_scale_z=None, reference_model=None,
-                 reference_model_in_smooth=False):
+                 reference_model_in_smooth=False, active_cells=None):
+        if simulation is not None and not hasattr(simulation, "engine"):
+            active_cells, simulation = simulation, None  # the reference's second positional argument
+        if active_cells is not None and not np.all(np.asarray(active_cells)):
+            raise NotImplementedError("inactive cells are not supported: every cell of the mesh is active")
         self.mesh = mesh
-        self.simulation = simulation
+        self.simulation = simulation if simulation is not None else _EngineHolder(mesh)
+        simulation = self.simulation
         base = min(float(np.min(h)) for h in mesh.h)
         self.base_length = base
 
@@ -167,7 +190,11 @@ class WeightedLeastSquares:
                                  C.c_void_p(0), _p(d), 2.0, _stream()))
         return d
 
+    def _dev(self, m):
+        return m if torch.is_tensor(m) else torch.as_tensor(np.asarray(m, dtype=np.float64), device=self.mref.device)
+
     def __call__(self, m_dev):
+        m_dev = self._dev(m_dev)
         dm = m_dev - self.mref
         ms = dm if self.reference_model_in_smooth else m_dev
         small = self._apply(dm, self.alpha_s, smooth=False)
@@ -181,6 +208,14 @@ class WeightedLeastSquares:
 
     def deriv2_dev(self, v_dev):
         return 2.0 * self.R(v_dev)
+
+    def deriv(self, m):
+        """Gradient as a host array."""
+        return self.deriv_dev(self._dev(m)).cpu().numpy()
+
+    def deriv2(self, m, v):
+        """Second derivative times v as a host array (independent of m)."""
+        return self.deriv2_dev(self._dev(v)).cpu().numpy()
 
 
 def inexact_gauss_newton_direction(dmis, reg, beta, m, cg_maxiter=10, cg_rtol=0.0, precondition=True):

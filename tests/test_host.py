@@ -479,3 +479,32 @@ def test_l2_data_misfit_forms_and_host_products():
     with pytest.raises(ValueError):
         L2DataMisfit(Data(Srv(), dobs=dobs), sim)  # no uncertainties: no W
     np.testing.assert_allclose(L2DataMisfit(sim, dobs).W, np.ones(nD))
+
+
+def test_weighted_least_squares_construction():
+    """WeightedLeastSquares: alphas from length scales (alpha_j = (length_scale_j * smallest
+    cell width)^2, regularization/base.py), reference model on the simulation's device, and
+    the reference's second positional argument (active cells) accepted only when every cell
+    is active."""
+    import torch
+
+    from simpeg_gb300.inversion import WeightedLeastSquares
+    from simpeg_gb300.mesh import TensorMesh
+
+    mesh = TensorMesh([[(5.0, 4)], [(10.0, 3)], [(2.5, 2)]])
+
+    class Sim:
+        engine = None
+        device = torch.device("cpu")
+        nC = 24
+
+    reg = WeightedLeastSquares(mesh, Sim(), length_scale_x=2.0, alpha_y=3.0, reference_model=np.arange(24.0))
+    assert reg.base_length == 2.5
+    assert reg.alpha_x == (2.0 * 2.5) ** 2 and reg.alpha_y == 3.0 and reg.alpha_z == 2.5 ** 2
+    np.testing.assert_array_equal(reg.mref.numpy(), np.arange(24.0))
+    with pytest.raises(ValueError):
+        WeightedLeastSquares(mesh, Sim(), alpha_x=1.0, length_scale_x=1.0)
+    mask = np.ones(24, bool)
+    mask[3] = False
+    with pytest.raises(NotImplementedError):
+        WeightedLeastSquares(mesh, mask)
