@@ -97,7 +97,7 @@ class Simulation3DNodal(_DCSimulation3DNodal):
         """Diagonal of d sigma / d m = -sigma * d eta / d m (``simulation.py:36-38``)."""
         mp = self.etaMap if self.etaMap is not None else IdentityMap()
         s = self.sigma
-        if hasattr(mp, "diag_deriv"):
+        if hasattr(mp, "diag_deriv") and getattr(mp, "is_diagonal", True):
             m = self._model if self._model is not None else np.zeros(self.nC)
             return -s * mp.diag_deriv(m)
         D = mp.deriv(self._model)

@@ -13,7 +13,7 @@ from __future__ import annotations
 import numpy as np
 import scipy.sparse as sp
 
-__all__ = ["IdentityMap", "ExpMap", "ReciprocalMap", "ComboMap"]
+__all__ = ["IdentityMap", "ExpMap", "ReciprocalMap", "ComboMap", "InjectActiveCells"]
 
 
 class IdentityMap:
@@ -131,6 +131,10 @@ class ComboMap(IdentityMap):
         return m
 
     def diag_deriv(self, m):
+        """Diagonal of the derivative when every map in the chain has a diagonal one;
+        NotImplementedError otherwise (the derivative is then ``deriv``)."""
+        if not all(getattr(mp, "is_diagonal", True) for mp in self.maps):
+            raise NotImplementedError("the chain contains a map without a diagonal derivative")
         x = np.asarray(m, dtype=np.float64).ravel()
         d = np.ones_like(x)
         for mp in reversed(self.maps):
@@ -138,6 +142,90 @@ class ComboMap(IdentityMap):
             x = mp._transform(x)
         return d
 
+    def deriv(self, m, v=None):
+        """Chain rule with sparse matrices (any maps)."""
+        if all(getattr(mp, "is_diagonal", True) for mp in self.maps):
+            return super().deriv(m, v)
+        x = np.asarray(m, dtype=np.float64).ravel()
+        D = None
+        for mp in reversed(self.maps):
+            Dm = sp.csr_matrix(mp.deriv(x))
+            D = Dm if D is None else (Dm @ D)
+            x = mp._transform(x)
+        return D @ v if v is not None else D
+
+    @property
+    def is_diagonal(self):
+        return all(getattr(mp, "is_diagonal", True) for mp in self.maps)
+
     @property
     def is_linear(self):
         return all(m.is_linear for m in self.maps)
+
+
+class InjectActiveCells(IdentityMap):
+    """Model on the active cells, a fixed value on the others (``simpeg/maps/_injection.py``):
+    ``out[active] = m``, ``out[~active] = value_inactive``; derivative the (nC, nActive)
+    injection matrix.  Its derivative is not diagonal: a simulation applies it on the host."""
+
+    is_diagonal = False
+
+    def __init__(self, mesh, active_cells=None, value_inactive=0.0, **kwargs):
+        nC = mesh.n_cells if hasattr(mesh, "n_cells") else int(mesh.nC)
+        act = np.ones(nC, dtype=bool) if active_cells is None else np.asarray(active_cells)
+        if act.dtype != bool:
+            idx = act.astype(np.int64)
+            act = np.zeros(nC, dtype=bool)
+            act[idx] = True
+        if act.size != nC:
+            raise ValueError(f"active_cells has {act.size} entries, the mesh {nC} cells")
+        self.active_cells = act
+        self.nC = nC
+        self.value_inactive = value_inactive
+        self._P = sp.csr_matrix((np.ones(int(act.sum())), (np.flatnonzero(act), np.arange(int(act.sum())))),
+                                shape=(nC, int(act.sum())))
+        super().__init__(nP=int(act.sum()))
+
+    @property
+    def value_inactive(self):
+        return self._value_inactive
+
+    @value_inactive.setter
+    def value_inactive(self, value):
+        v = np.asarray(value, dtype=np.float64)
+        n_inact = int((~self.active_cells).sum())
+        if v.size not in (1, n_inact):
+            raise ValueError("value_inactive must be a scalar or one value per inactive cell")
+        self._value_inactive = np.broadcast_to(v.ravel(), (n_inact,)).copy()
+
+    @property
+    def shape(self):
+        return (self.nC, self.nP)
+
+    def _transform(self, m):
+        out = np.empty(self.nC)
+        out[self.active_cells] = np.asarray(m, dtype=np.float64).ravel()
+        out[~self.active_cells] = self._value_inactive
+        return out
+
+    def transform_dev(self, m):
+        import torch
+
+        act = torch.as_tensor(self.active_cells, device=m.device)
+        out = torch.empty(self.nC, dtype=m.dtype, device=m.device)
+        out[act] = m
+        out[~act] = torch.as_tensor(self._value_inactive, dtype=m.dtype, device=m.device)
+        return out
+
+    def diag_deriv(self, m):
+        raise NotImplementedError("InjectActiveCells has no diagonal derivative")
+
+    def deriv(self, m, v=None):
+        return self._P @ v if v is not None else self._P
+
+    def inverse(self, D):
+        return np.asarray(D, dtype=np.float64).ravel()[self.active_cells]
+
+    @property
+    def is_linear(self):
+        return True

@@ -173,7 +173,7 @@ class Simulation3DNodal:
         mp = self.sigmaMap
         if mp is None:
             return None
-        if hasattr(mp, "diag_deriv"):
+        if hasattr(mp, "diag_deriv") and getattr(mp, "is_diagonal", True):
             return mp.diag_deriv(self._model)
         D = mp.deriv(self._model)
         if sp.issparse(D):

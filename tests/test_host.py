@@ -508,3 +508,42 @@ def test_weighted_least_squares_construction():
     mask[3] = False
     with pytest.raises(NotImplementedError):
         WeightedLeastSquares(mesh, mask)
+
+
+def test_inject_active_cells_and_general_combo_derivative():
+    """InjectActiveCells (out[active] = m, out[~active] = value) and the chain rule of
+    ComboMap through it (sparse, not diagonal); diagonal chains keep diag_deriv and agree
+    with the general derivative."""
+    import scipy.sparse as sp_
+
+    from simpeg_gb300.maps import ComboMap, ExpMap, IdentityMap, InjectActiveCells
+    from simpeg_gb300.mesh import TensorMesh
+
+    mesh = TensorMesh([3, 2, 2])
+    act = np.array([True, False, True, True, False, True, True, True, False, True, True, True])
+    inj = InjectActiveCells(mesh, act, value_inactive=1e-8)
+    assert inj.nP == act.sum() and inj.shape == (12, act.sum()) and not inj.is_diagonal
+    rng = np.random.default_rng(2)
+    m = rng.standard_normal(inj.nP)
+    out = inj * m
+    np.testing.assert_array_equal(out[act], m)
+    np.testing.assert_array_equal(out[~act], 1e-8)
+    np.testing.assert_array_equal(inj.inverse(out), m)
+    combo = ComboMap([ExpMap(), inj])
+    assert not combo.is_diagonal
+    with pytest.raises(NotImplementedError):
+        combo.diag_deriv(m)
+    D = combo.deriv(m)
+    assert sp_.issparse(D) and D.shape == (12, inj.nP)
+    v = rng.standard_normal(inj.nP)
+    h = 1e-6
+    fd = (combo * (m + h * v) - combo * (m - h * v)) / (2 * h)
+    np.testing.assert_allclose(D @ v, fd, rtol=1e-6, atol=1e-12)
+    diag_chain = ComboMap([ExpMap(), IdentityMap()])
+    x = rng.standard_normal(12)
+    assert diag_chain.is_diagonal
+    np.testing.assert_allclose(diag_chain.deriv(x).diagonal(), diag_chain.diag_deriv(x))
+    np.testing.assert_array_equal(InjectActiveCells(mesh, np.flatnonzero(act)).active_cells, act)
+    import torch
+
+    np.testing.assert_array_equal(inj.transform_dev(torch.as_tensor(m)).numpy(), out)
