@@ -547,3 +547,45 @@ def test_inject_active_cells_and_general_combo_derivative():
     import torch
 
     np.testing.assert_array_equal(inj.transform_dev(torch.as_tensor(m)).numpy(), out)
+
+
+def test_simulation_sigma_derivative_selection():
+    """The simulation's d sigma / d m: a diagonal array for diagonal maps (the device path),
+    a sparse (nC, nP) matrix through InjectActiveCells (applied on the host); the IP
+    simulation's -sigma * d eta / dm likewise."""
+    import scipy.sparse as sp_
+
+    from simpeg_gb300.induced_polarization.simulation import Simulation3DNodal as IPNodal
+    from simpeg_gb300.maps import ComboMap, ExpMap, IdentityMap, InjectActiveCells
+    from simpeg_gb300.mesh import TensorMesh
+    from simpeg_gb300.resistivity.simulation import Simulation3DNodal
+
+    mesh = TensorMesh([3, 2, 2])
+    act = np.arange(12) % 3 != 1
+    m_act = np.linspace(-1.0, 1.0, act.sum())
+
+    class Stub:
+        pass
+
+    s = Stub()
+    s.sigmaMap = ExpMap(mesh)
+    s._model = np.linspace(-1.0, 1.0, 12)
+    d = Simulation3DNodal._sigma_deriv(s)
+    assert isinstance(d, np.ndarray)
+    np.testing.assert_allclose(d, np.exp(s._model))
+    s.sigmaMap = ComboMap([ExpMap(), InjectActiveCells(mesh, act, value_inactive=-3.0)])
+    s._model = m_act
+    D = Simulation3DNodal._sigma_deriv(s)
+    assert sp_.issparse(D) and D.shape == (12, act.sum())
+    np.testing.assert_allclose(D.toarray()[act], np.diag(np.exp(m_act)))
+
+    ip = Stub()
+    ip.sigma = np.full(12, 0.01)
+    ip.nC = 12
+    ip.etaMap = IdentityMap()
+    ip._model = np.full(12, 0.1)
+    np.testing.assert_allclose(IPNodal._sigma_deriv(ip), -0.01 * np.ones(12))
+    ip.etaMap = InjectActiveCells(mesh, act)
+    ip._model = np.full(act.sum(), 0.1)
+    D = IPNodal._sigma_deriv(ip)
+    assert sp_.issparse(D) and D.shape == (12, act.sum())
