@@ -245,8 +245,9 @@ void dc_csr_destroy(dc_csr *h);
  * exactly what dc_dadm_adj computes.  Scratch: a file-scope device array of
  * 4*DC_NOALLOC_MAX_NODES doubles (36.6 MiB) held by every GPU that loads the
  * library until exit; meshes with more nodes are rejected with DC_ERR_ARG.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * Every call looks up the array's device address on the current device
+ * (cudaGetSymbolAddress; the first call on a device also loads the module,
+ * so it should come before any stream capture).  All
  * calls share the array: calls that overlap on the GPU race.  Calls no
  * cudaMalloc, cudaFree or other allocating routine. */
 #define DC_NOALLOC_MAX_NODES 1200000
@@ -254,8 +255,6 @@ int dc_dadm_adj_noalloc(int nx, int ny, int nz, const double *h_dev, const doubl
                         const double *lam_dev, int k, const double *dsig_dev, double scale, double *g_dev,
                         void *stream);
 
-/* Number of CUDA kernels this library has launched since it was loaded
- * (all handles, all threads).  Instrumentation; no reference counterpart. */
 /* Derived fields of Fields3DNodal (simpeg/electromagnetics/static/resistivity/
  * fields.py:186-257) for k nodal potentials phi (column-major (N, k)), on the
  * edges ordered as discretize orders them (all x-edges, then y-, then z-edges,
@@ -274,6 +273,8 @@ int dc_edge_fields(dc_handle *h, const double *phi, int k, double *e, double *j,
 int dc_node_charge(dc_handle *h, const double *e, int k, double eps0, double *charge, double *charge_density,
                    void *stream);
 
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (all handles, all threads).  Instrumentation; no reference counterpart. */
 long long dc_kernel_launches(void);
 
 /* Event timing of the fine-level fp32 Chebyshev/stencil launches of h.

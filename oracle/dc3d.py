@@ -120,6 +120,21 @@ class OracleDC3DNodal:
     def sigma_deriv_diag(self):
         return self.sigma_map.diag_deriv(self.model)
 
+    def _sigma_deriv(self):
+        """d sigma / d m: its diagonal (array) for elementwise maps, else the map's sparse derivative
+        (``props.py:135-171``: sigmaDeriv = sigmaMap.deriv(model))."""
+        if self.sigma_map is None or getattr(self.sigma_map, "is_diagonal", True):
+            return self.sigma_deriv_diag()
+        return sp.csr_matrix(self.sigma_map.deriv(self.model))
+
+    def _dsig(self, v):
+        d = self._sigma_deriv()
+        return d * v if isinstance(d, np.ndarray) else np.asarray(d @ v).ravel()
+
+    def _dsigT(self, g):
+        d = self._sigma_deriv()
+        return d * g if isinstance(d, np.ndarray) else np.asarray(d.T @ g).ravel()
+
     # ------------------------------------------------------------ operators
     def getA(self, sigma=None):
         s = self.sigma if sigma is None else sigma
@@ -136,28 +151,28 @@ class OracleDC3DNodal:
 
     def getADeriv(self, u, v, adjoint=False):
         """dA/dm products; u, v may be (nN,) or (nN, k) (k sources, adjoint sums over k)."""
-        d = self.sigma_deriv_diag()
         G = self.G
         Gu = G @ u
         if not adjoint:
             # Grad.T @ (Gu * (E sigma' v))  +  u * (AvgBC sigma' v)
-            w = self.E @ (d * v)
+            dv = self._dsig(v)
+            w = self.E @ dv
             out = G.T @ (Gu * (w[:, None] if Gu.ndim == 2 else w))
             if self.bc_type != "Neumann":
-                b = self.AvgBC @ (d * v)
+                b = self.AvgBC @ dv
                 out = out + u * (b[:, None] if np.ndim(u) == 2 else b)
             return out
         Gv = G @ v
         prod = Gu * Gv
         if prod.ndim == 2:
             prod = prod.sum(axis=1)
-        out = d * (self.E.T @ prod)
+        out = self.E.T @ prod
         if self.bc_type != "Neumann":
             uv = u * v
             if uv.ndim == 2:
                 uv = uv.sum(axis=1)
-            out = out + d * (self.AvgBC.T @ uv)
-        return out
+            out = out + self.AvgBC.T @ uv
+        return self._dsigT(out)
 
     def getRHS(self):
         cols = []
@@ -269,9 +284,8 @@ class OracleDC3DNodal:
         PT = np.hstack(cols)
         lam = self._solve(PT)
         owner = np.array(owner)
-        J = np.zeros((PT.shape[1], self.ops.nC))
-        for dcol in range(PT.shape[1]):
-            J[dcol] = -self.getADeriv(f[:, owner[dcol]], lam[:, dcol], adjoint=True)
+        rows = [-self.getADeriv(f[:, owner[dcol]], lam[:, dcol], adjoint=True) for dcol in range(PT.shape[1])]
+        J = np.array(rows).reshape(PT.shape[1], -1)  # (nD, nP): nP = the model's size under any map
         return J
 
     def getJtJdiag(self, m, W=None, f=None):

@@ -9,6 +9,10 @@ diagonal derivative (ExpMap: ``sigma' = sigma``).  This is the reference's
 driven by autograd, so a misfit written in torch gets its gradient without
 forming J.
 
+A model on a CUDA device stays there: an elementwise map (ExpMap, Identity,
+Reciprocal and chains of them) is applied on the device and its diagonal
+derivative too, so the training loop copies no model to the host.
+
 ``recompute=True`` drops the forward fields after the forward pass and solves
 them again in backward (for meshes whose fields do not fit next to the
 adjoint workspace); ``False`` keeps them on the device between the passes.
@@ -27,41 +31,49 @@ __all__ = ["DCPredict", "dpred"]
 class DCPredict(torch.autograd.Function):
     @staticmethod
     def forward(ctx, m, sim, recompute):
-        m_np = m.detach().cpu().numpy().astype(np.float64)
-        f = sim.fields(m_np)
-        d = sim._gather(f.phi_dev)
+        # a CUDA model stays on the device when the map is elementwise (no host round trip)
+        on_dev = m.is_cuda and sim._device_model_ok()
+        if on_dev:
+            m_dev = m.detach().to(sim.device, torch.float64)
+            f = sim.fields_dev(m_dev)
+            ctx.m_dev, ctx.m_np = m_dev, None
+        else:
+            m_np = m.detach().cpu().numpy().astype(np.float64)
+            f = sim.fields(m_np)
+            ctx.m_dev, ctx.m_np = None, m_np
+        d = sim._mini_survey_data_dev(sim._gather(f.phi_dev))
         ctx.sim = sim
         ctx.recompute = bool(recompute)
-        ctx.m_np = m_np
         ctx.fields = None if recompute else f
         if recompute:
             sim._f_cache = None
             del f
         ctx.out_device = m.device
-        if sim._mini_survey is not None:
-            d = torch.from_numpy(sim._mini_survey_data(d.cpu().numpy()))
         return d.to(m.device)
 
     @staticmethod
     def backward(ctx, grad_d):
         sim = ctx.sim
-        m_np = ctx.m_np
-        sim.model = m_np
-        f = ctx.fields if ctx.fields is not None else sim.fields(m_np)
-        t, tq = sim._get_tables()
-        g = grad_d.detach().to(sim.device, torch.float64).contiguous()
-        if sim._mini_survey is not None:
-            g = torch.from_numpy(sim._mini_survey_dataT(g.cpu().numpy())).to(sim.device)
-        PTv = torch.zeros(t.nSrc, sim.nN, dtype=torch.float64, device=sim.device)
-        csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], g, PTv.view(-1), out_idx=tq["PT_out"])
-        Lam = sim._solve(PTv)
-        d = sim._sigma_deriv()
-        if isinstance(d, np.ndarray):
-            dsig = torch.from_numpy(np.ascontiguousarray(d)).to(sim.device)
-            gm = sim.engine.dadm_adj(f.phi_dev, Lam, dsig, scale=-1.0)
+        if ctx.m_dev is not None:
+            f = ctx.fields if ctx.fields is not None else sim.fields_dev(ctx.m_dev)
         else:
-            gs = sim.engine.dadm_adj(f.phi_dev, Lam, None, scale=-1.0).cpu().numpy()
-            gm = torch.from_numpy(np.asarray(d.T @ gs).ravel()).to(sim.device)
+            sim.model = ctx.m_np
+            f = ctx.fields if ctx.fields is not None else sim.fields(ctx.m_np)
+        t, tq = sim._get_tables()
+        g = sim._mini_survey_dataT_dev(grad_d.detach().to(sim.device, torch.float64).contiguous())
+        PTv = torch.zeros(t.nSrc, sim.nN, dtype=torch.float64, device=sim.device)
+        csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], g.contiguous(), PTv.view(-1), out_idx=tq["PT_out"])
+        Lam = sim._solve(PTv)
+        if ctx.m_dev is not None:
+            gm = sim.engine.dadm_adj(f.phi_dev, Lam, sim._dsig_diag_dev(), scale=-1.0)
+        else:
+            d = sim._sigma_deriv()
+            if isinstance(d, np.ndarray):
+                dsig = torch.from_numpy(np.ascontiguousarray(d)).to(sim.device)
+                gm = sim.engine.dadm_adj(f.phi_dev, Lam, dsig, scale=-1.0)
+            else:
+                gs = sim.engine.dadm_adj(f.phi_dev, Lam, None, scale=-1.0).cpu().numpy()
+                gm = torch.from_numpy(np.asarray(d.T @ gs).ravel()).to(sim.device)
         if ctx.recompute:
             del f
             sim._f_cache = None

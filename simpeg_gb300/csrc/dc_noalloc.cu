@@ -20,7 +20,6 @@
 #include "dc_internal.h"
 
 #include <cstdio>
-#include <mutex>
 
 namespace dc {
 namespace {
@@ -30,35 +29,20 @@ constexpr long long kMaxNodes = DC_NOALLOC_MAX_NODES;
 // Edge products P (3 per node) and boundary products Q (1 per node).
 static __device__ __align__(256) double g_noalloc_scratch[4 * kMaxNodes];
 
-// Device address of g_noalloc_scratch per device.  In host code the symbol is
-// only a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress once per device (with that device current).
-constexpr int kMaxDevices = 64;
-void *g_scratch_addr[kMaxDevices] = {nullptr};
-std::mutex g_scratch_mu;
-
+// Device address of g_noalloc_scratch on the current device.  In host code the
+// symbol is only a host-side stand-in, so the address is looked up with
+// cudaGetSymbolAddress, with the calling thread's device current.  It is looked
+// up on every call (a table lookup in the runtime, no allocation): a cached
+// address would go stale if the caller tore the context down
+// (cudaDeviceReset) and the module were loaded again at another address.
 int scratch_for_current_device(double **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    last_error() = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    last_error() = std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e);
     return DC_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    last_error() = "device index out of range for the no-allocation scratch table";
-    return DC_ERR_ARG;
-  }
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      last_error() = std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e);
-      return DC_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = p;
-  }
-  *out = static_cast<double *>(g_scratch_addr[dev]);
+  *out = static_cast<double *>(p);
   return DC_OK;
 }
 

@@ -105,9 +105,10 @@ class L2DataMisfit:
         r = self.residual_dev(m)
         return 2.0 * self.simulation.jtvec_dev(self.w * self.w * r)
 
-    def deriv2_dev(self, m, v_dev):
+    def deriv2_dev(self, m, v_dev, f=None):
         sim = self.simulation
-        return 2.0 * sim.jtvec_dev(self.w * self.w * sim.jvec_dev(v_dev))
+        f = sim._fields_for(m, f)  # the products run at m, whatever model was evaluated last
+        return 2.0 * sim.jtvec_dev(self.w * self.w * sim.jvec_dev(v_dev, f=f), f=f)
 
     @property
     def nD(self):
@@ -120,7 +121,7 @@ class L2DataMisfit:
     def deriv2(self, m, v, f=None):
         """Gauss-Newton Hessian product ``2 J^T W^T W J v`` as a host array (``data_misfit.py:306-343``)."""
         v_dev = torch.as_tensor(np.asarray(v, dtype=np.float64), device=self.simulation.device)
-        return self.deriv2_dev(m, v_dev).cpu().numpy()
+        return self.deriv2_dev(m, v_dev, f=f).cpu().numpy()
 
 
 class _EngineHolder:

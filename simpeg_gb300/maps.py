@@ -41,6 +41,10 @@ class IdentityMap:
         """Diagonal of d(map(m))/dm."""
         return np.ones(np.asarray(m).size)
 
+    def diag_deriv_dev(self, m):
+        """Diagonal of d(map(m))/dm for a device (torch) model vector."""
+        return m.new_ones(m.shape)
+
     def deriv(self, m, v=None):
         d = sp.diags(self.diag_deriv(m))
         return d @ v if v is not None else d
@@ -79,6 +83,9 @@ class ExpMap(IdentityMap):
     def diag_deriv(self, m):
         return np.exp(np.asarray(m, dtype=np.float64).ravel())
 
+    def diag_deriv_dev(self, m):
+        return m.exp()
+
     def inverse(self, D):
         return np.log(np.asarray(D, dtype=np.float64).ravel())
 
@@ -99,6 +106,9 @@ class ReciprocalMap(IdentityMap):
     def diag_deriv(self, m):
         m = np.asarray(m, dtype=np.float64).ravel()
         return -1.0 / m**2
+
+    def diag_deriv_dev(self, m):
+        return -1.0 / (m * m)
 
     def inverse(self, D):
         return 1.0 / np.asarray(D, dtype=np.float64).ravel()
@@ -140,6 +150,16 @@ class ComboMap(IdentityMap):
         for mp in reversed(self.maps):
             d = mp.diag_deriv(x) * d
             x = mp._transform(x)
+        return d
+
+    def diag_deriv_dev(self, m):
+        """:meth:`diag_deriv` for a device model vector (chains of diagonal maps)."""
+        if not self.is_diagonal:
+            raise NotImplementedError("the chain contains a map without a diagonal derivative")
+        d = m.new_ones(m.shape)
+        for mp in reversed(self.maps):
+            d = mp.diag_deriv_dev(m) * d
+            m = mp.transform_dev(m)
         return d
 
     def deriv(self, m, v=None):

@@ -12,6 +12,8 @@ is a stencil (forward) or an edge-product reduction (adjoint) kernel.
 
 from __future__ import annotations
 
+import warnings
+
 import numpy as np
 import scipy.sparse as sp
 import torch
@@ -58,6 +60,12 @@ class Simulation3DNodal:
         self.storeJ = bool(storeJ)
         self.verbose = verbose
         self.counter = counter
+        if solver is not None:
+            warnings.warn(
+                f"solver={getattr(solver, '__name__', solver)!r} is not used: Simulation3DNodal solves with its "
+                "matrix-free multigrid-PCG engine on the GPU (precision, rtol and maxit select it); pass the "
+                "solver class to a simulation that assembles A (e.g. GPUSolver for a CSR matrix)",
+                UserWarning, stacklevel=2)
         self.solver = solver
         self.solver_opts = {} if solver_opts is None else dict(solver_opts)
         if bc_type == "Mixed":
@@ -80,6 +88,7 @@ class Simulation3DNodal:
         self.sigmaMap = sigmaMap
         self.rhoMap = rhoMap
         self._model = None
+        self._model_dev = None  # a model given as a device tensor (fields_dev); host copy made on request
         self._miniaturize = bool(miniaturize)
         self._mini_survey = None
         if self._miniaturize:
@@ -128,10 +137,13 @@ class Simulation3DNodal:
 
     @property
     def model(self):
+        if self._model is None and self._model_dev is not None:
+            self._model = self._model_dev.detach().cpu().numpy().astype(np.float64).ravel()
         return self._model
 
     @model.setter
     def model(self, m):
+        self._model_dev = None
         if m is None:
             self._model = None
             self._clear()
@@ -160,9 +172,9 @@ class Simulation3DNodal:
             return 1.0 / self._rho
         if self.sigmaMap is None:
             raise AttributeError("Neither a value nor mapping for sigma/rho has been set")
-        if self._model is None:
+        if self.model is None:
             raise AttributeError("A `model` is required for physical property sigma")
-        return self.sigmaMap * self._model
+        return self.sigmaMap * self.model
 
     @property
     def rho(self):
@@ -174,8 +186,8 @@ class Simulation3DNodal:
         if mp is None:
             return None
         if hasattr(mp, "diag_deriv") and getattr(mp, "is_diagonal", True):
-            return mp.diag_deriv(self._model)
-        D = mp.deriv(self._model)
+            return mp.diag_deriv(self.model)
+        D = mp.deriv(self.model)
         if sp.issparse(D):
             D = D.tocsr()
             if D.shape[0] == D.shape[1] and D.nnz == np.count_nonzero(D.diagonal()):
@@ -210,7 +222,7 @@ class Simulation3DNodal:
     def _ensure_model(self):
         if self._sigma_dev is None:
             mp = self.sigmaMap
-            if (self._sigma is None and self._rho is None and self._model is not None and mp is not None
+            if (self._sigma is None and self._rho is None and self.model is not None and mp is not None
                     and hasattr(mp, "transform_dev") and np.size(self._model) == self.nC):
                 # the model goes to the device once and is mapped there (elementwise maps)
                 m = torch.from_numpy(np.ascontiguousarray(self._model, dtype=np.float64).ravel()).to(self.device)
@@ -312,6 +324,33 @@ class Simulation3DNodal:
         return self._map_adjoint(g)
 
     # ------------------------------------------------------------ forward
+    def _device_model_ok(self):
+        """True when a device model can be mapped on the device (an elementwise map, no fixed sigma/rho)."""
+        mp = self.sigmaMap
+        return (self._sigma is None and self._rho is None and mp is not None and hasattr(mp, "transform_dev")
+                and getattr(mp, "is_diagonal", True))
+
+    def fields_dev(self, m_dev):
+        """Fields at a model given as a device tensor (nP,): the map runs on the device and the model is
+        not copied to the host (a host copy is made only if a host-side method asks for ``model``)."""
+        if not self._device_model_ok():
+            raise NotImplementedError("device models need an elementwise sigmaMap with a diagonal derivative")
+        m_dev = m_dev.detach().to(self.device, torch.float64).reshape(-1)
+        nP = getattr(self.sigmaMap, "nP", "*")
+        if isinstance(nP, (int, np.integer)) and m_dev.numel() != nP:
+            raise ValueError(f"model must have {nP} parameters, got {m_dev.numel()}")
+        self._model = None
+        self._clear()
+        self._model_dev = m_dev
+        s = self.sigmaMap.transform_dev(m_dev)
+        if not bool(((s > 0) & torch.isfinite(s)).all()):
+            raise ValueError("conductivity must be positive and finite")
+        self._sigma_dev = s.contiguous()
+        self.engine.set_model(self._sigma_dev)
+        f = Fields3DNodal(self, self._solve(self.getRHS()))
+        self._f_cache = f
+        return f
+
     def fields(self, m=None, calcJ=True):
         if m is not None:
             self.model = m
@@ -354,9 +393,9 @@ class Simulation3DNodal:
     # ------------------------------------------------------------ sensitivities
     def _fields_for(self, m, f):
         if f is None:
-            if self._f_cache is not None and m is not None and self._model is not None and \
-                    np.array_equal(np.asarray(m, dtype=np.float64).ravel(), self._model):
-                return self._f_cache
+            if self._f_cache is not None and (m is None or (self._model is not None and np.array_equal(
+                    np.asarray(m, dtype=np.float64).ravel(), self._model))):
+                return self._f_cache  # m None: the fields of the current model
             return self.fields(m)
         return f
 
@@ -386,6 +425,13 @@ class Simulation3DNodal:
         csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], vd, PTv.view(-1), out_idx=tq["PT_out"])
         return PTv
 
+    def _n_params(self):
+        """Number of model parameters: the map's nP, else the model's size."""
+        nP = getattr(self.sigmaMap, "nP", None) if self.sigmaMap is not None else None
+        if isinstance(nP, (int, np.integer)):
+            return int(nP)
+        return int(np.size(self._model)) if self._model is not None else self.nC
+
     def _map_adjoint(self, g_sigma):
         d = self._sigma_deriv()
         if isinstance(d, np.ndarray):
@@ -414,11 +460,12 @@ class Simulation3DNodal:
         ``-dA/dm v`` by the stencil kernel, one multi-RHS solve, receiver gather."""
         if self._mini_survey is not None:
             raise NotImplementedError("device products need miniaturize=False (use Jvec)")
-        f = f if f is not None else self._fields_for(self._model, None)
+        f = f if f is not None else self._fields_for(None, None)
         d = self._sigma_deriv()
-        if not isinstance(d, np.ndarray):
-            raise NotImplementedError("device products need a map with a diagonal derivative")
-        dsig = self._dsig_diag_dev() * v_dev
+        if isinstance(d, np.ndarray):
+            dsig = self._dsig_diag_dev() * v_dev
+        else:  # sparse d sigma / d m (e.g. through InjectActiveCells): applied on the host
+            dsig = self._dsig_dev(v_dev.detach().cpu().numpy())
         R = self.engine.dadm_fwd(f.phi_dev, dsig.contiguous(), scale=-1.0)
         return self._gather(self._solve(R))
 
@@ -426,17 +473,31 @@ class Simulation3DNodal:
         """J^T w with w a device tensor (nD,) at the current model; returns a device tensor (nP,)."""
         if self._mini_survey is not None:
             raise NotImplementedError("device products need miniaturize=False (use Jtvec)")
-        f = f if f is not None else self._fields_for(self._model, None)
+        f = f if f is not None else self._fields_for(None, None)
         t, tq = self._get_tables()
         PTv = torch.zeros(t.nSrc, self.nN, dtype=torch.float64, device=self.device)
         csr_spmv(tq["PT_ptr"], tq["PT_idx"], tq["PT_w"], w_dev.contiguous(), PTv.view(-1), out_idx=tq["PT_out"])
         Lam = self._solve(PTv)
-        return self.engine.dadm_adj(f.phi_dev, Lam, self._dsig_diag_dev(), scale=-1.0)
+        d = self._sigma_deriv()
+        if isinstance(d, np.ndarray):
+            return self.engine.dadm_adj(f.phi_dev, Lam, self._dsig_diag_dev(), scale=-1.0)
+        # sparse d sigma / d m: the cell gradient is mapped back on the host
+        g = self.engine.dadm_adj(f.phi_dev, Lam, None, scale=-1.0).cpu().numpy()
+        return torch.from_numpy(self._map_adjoint(g)).to(self.device)
 
     def _dsig_diag_dev(self):
-        if getattr(self, "_dsig_cache", None) is None or self._dsig_cache[0] is not self._model:
-            d = self._sigma_deriv()
-            self._dsig_cache = (self._model, torch.from_numpy(np.ascontiguousarray(d)).to(self.device))
+        """Diagonal of d sigma / d m on the device (maps with a diagonal derivative only)."""
+        key = self._model_dev if self._model_dev is not None else self._model
+        if getattr(self, "_dsig_cache", None) is None or self._dsig_cache[0] is not key:
+            mp = self.sigmaMap
+            if self._model_dev is not None and hasattr(mp, "diag_deriv_dev") and getattr(mp, "is_diagonal", True):
+                dd = mp.diag_deriv_dev(self._model_dev).contiguous()
+            else:
+                d = self._sigma_deriv()
+                if not isinstance(d, np.ndarray):
+                    raise NotImplementedError("the map's derivative is not diagonal: no device diagonal exists")
+                dd = torch.from_numpy(np.ascontiguousarray(d)).to(self.device)
+            self._dsig_cache = (key, dd)
         return self._dsig_cache[1]
 
     def getJ(self, m, f=None):
@@ -448,7 +509,7 @@ class Simulation3DNodal:
         self._ensure_model()
         t, tq = self._get_tables()
         nD = t.nD
-        J = np.zeros((nD, self.nC))
+        J = np.zeros((nD, self._n_params()))
         PT = t.P.T.tocsc()
         owner = t.owner
         chunk = max(1, min(nD, 256))
@@ -601,6 +662,36 @@ class Simulation3DNodal:
         np.subtract.at(out, self._invs[1], v[self._dipoles[0]])
         np.subtract.at(out, self._invs[2], v[self._dipoles[1]])
         np.add.at(out, self._invs[3], v[self._dipoles[0] & self._dipoles[1]])
+        return out
+
+    def _mini_survey_data_dev(self, d_mini):
+        """:meth:`_mini_survey_data` on a device tensor (same integer maps, gathered on the device)."""
+        if self._mini_survey is None:
+            return d_mini
+        dev = d_mini.device
+        if getattr(self, "_mini_dev", None) is None or self._mini_dev[0] != dev:
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+            self._mini_dev = (dev, [t(x.astype(np.int64)) for x in self._invs],
+                              [t(x) for x in (self._dipoles[0], self._dipoles[1],
+                                              self._dipoles[0] & self._dipoles[1])])
+        _, inv, dip = self._mini_dev
+        out = d_mini[inv[0]].clone()
+        out[dip[0]] -= d_mini[inv[1]]
+        out[dip[1]] -= d_mini[inv[2]]
+        out[dip[2]] += d_mini[inv[3]]
+        return out
+
+    def _mini_survey_dataT_dev(self, v):
+        """:meth:`_mini_survey_dataT` on a device tensor (index_add in place of np.add.at)."""
+        if self._mini_survey is None:
+            return v
+        self._mini_survey_data_dev(torch.zeros(self._mini_survey.nD, dtype=v.dtype, device=v.device))
+        _, inv, dip = self._mini_dev
+        out = torch.zeros(self._mini_survey.nD, dtype=v.dtype, device=v.device)
+        out.index_add_(0, inv[0], v)
+        out.index_add_(0, inv[1], -v[dip[0]])
+        out.index_add_(0, inv[2], -v[dip[1]])
+        out.index_add_(0, inv[3], v[dip[2]])
         return out
 
     def _mini_J(self, J):

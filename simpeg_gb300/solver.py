@@ -11,8 +11,13 @@ multi-RHS fp64 CG solve there (``dc_csr_solve`` in ``include/dcgpu.h``).
 When pymatsolver is importable the class derives from its ``solvers.Base`` so
 simpeg's ``issubclass`` check passes; otherwise a minimal base with the same
 constructor arguments and calls (``solve``, ``*``, ``@``, ``.T``, ``clean``) is
-used.  Only symmetric positive-definite matrices are accepted (simpeg's Robin
-nodal and cell-centred DC matrices are); a non-symmetric matrix raises.
+used.  Symmetric positive-definite matrices are accepted (simpeg's Robin
+nodal and cell-centred DC matrices are), and so are matrices that are
+symmetric apart from pinned rows -- rows whose only entry is the diagonal, as
+the reference's Neumann ``getA`` pins row 0 (``resistivity/simulation.py:535-540``).
+A pinned unknown is known from its row (``x_p = b_p / A_pp``); its column is
+moved to the right-hand side, which leaves a symmetric system for CG.  Any
+other non-symmetric matrix raises.
 """
 
 from __future__ import annotations
@@ -111,14 +116,42 @@ class GPUSolver(_Base):
         A.sort_indices()
         if A.shape[0] != A.shape[1]:
             raise ValueError("matrix must be square")
+        A, self._pin = self._unpin(A)
         diff = abs(A - A.T)
         if diff.nnz and diff.max() > 1e-12 * abs(A).max():
-            raise NotImplementedError("GPUSolver needs a symmetric positive-definite matrix (CG)")
+            raise NotImplementedError("GPUSolver needs a symmetric positive-definite matrix (CG), or one that is "
+                                      "symmetric apart from rows holding only their diagonal")
         self._csr = A
         self.rtol = float(rtol)
         self.maxiter = int(maxiter)
         self._h = None
         self._upload()
+
+    @staticmethod
+    def _unpin(A):
+        """Split off pinned rows (only a diagonal entry) whose columns break the symmetry.
+
+        Returns the matrix with those columns' off-diagonal entries removed and, per pinned row p,
+        what the solve needs: the rows p, their diagonals and the removed column entries (a sparse
+        (n, n_pinned) matrix), or None when nothing is pinned."""
+        nnz_row = np.diff(A.indptr)
+        cand = np.flatnonzero(nnz_row == 1)
+        if cand.size:
+            cand = cand[A.indices[A.indptr[cand]] == cand]
+        if cand.size == 0:
+            return A, None
+        colmask = np.zeros(A.shape[0], dtype=bool)
+        colmask[cand] = True
+        coo = A.tocoo()
+        off = colmask[coo.col] & (coo.row != coo.col)
+        if not off.any():
+            return A, None
+        C_ = sp.csr_matrix((coo.data[off], (coo.row[off], np.searchsorted(cand, coo.col[off]))),
+                           shape=(A.shape[0], cand.size))
+        keep = ~off
+        A2 = sp.csr_matrix((coo.data[keep], (coo.row[keep], coo.col[keep])), shape=A.shape)
+        A2.sort_indices()
+        return A2, (cand, np.asarray(A.diagonal()[cand], dtype=np.float64), C_)
 
     def _upload(self):
         import torch
@@ -142,6 +175,10 @@ class GPUSolver(_Base):
             self._upload()
         rhs = np.asarray(rhs, dtype=np.float64)
         n, k = rhs.shape
+        if self._pin is not None:  # pinned unknowns to the right-hand side: b - A[:, P] x_P
+            rows, diag, C_ = self._pin
+            xp = rhs[rows] / diag[:, None]
+            rhs = rhs - C_ @ xp
         b = torch.from_numpy(np.ascontiguousarray(rhs.T)).cuda()
         x = torch.empty_like(b)
         st = _lib.dc_stats()

@@ -6,6 +6,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import scipy.sparse as sp
 import pytest
 
 from oracle.dc3d import OracleDC3DNodal
@@ -454,10 +455,10 @@ def test_l2_data_misfit_forms_and_host_products():
         def _gather(self, phi):
             return phi
 
-        def jvec_dev(self, v):
+        def jvec_dev(self, v, f=None):
             return torch.as_tensor(J) @ v
 
-        def jtvec_dev(self, w):
+        def jtvec_dev(self, w, f=None):
             return torch.as_tensor(J.T) @ w
 
     class Srv:
@@ -565,7 +566,9 @@ def test_simulation_sigma_derivative_selection():
     m_act = np.linspace(-1.0, 1.0, act.sum())
 
     class Stub:
-        pass
+        @property
+        def model(self):
+            return self._model
 
     s = Stub()
     s.sigmaMap = ExpMap(mesh)
@@ -589,3 +592,53 @@ def test_simulation_sigma_derivative_selection():
     ip._model = np.full(act.sum(), 0.1)
     D = IPNodal._sigma_deriv(ip)
     assert sp_.issparse(D) and D.shape == (12, act.sum())
+
+
+def test_gpu_solver_unpins_neumann_rows():
+    """The Solver plug-in's host transform of a pinned-row matrix (the reference's Neumann getA,
+    row 0 = e0): the unpinned matrix is symmetric, and solving it with the pinned column moved to
+    the right-hand side gives the pinned matrix's solution (checked with SuperLU on the CPU)."""
+    import scipy.sparse.linalg as spla
+
+    from oracle.dc3d import OracleDC3DNodal
+    from simpeg_gb300.mesh import TensorMesh
+    from simpeg_gb300.resistivity.survey import Survey
+    from simpeg_gb300.solver import GPUSolver
+
+    mesh = TensorMesh([[(10.0, 6)], [(10.0, 5)], [(10.0, 4)]], origin="CCN")
+    rng = np.random.default_rng(2)
+    orc = OracleDC3DNodal(mesh, Survey([]), sigma=10 ** rng.uniform(-2.5, -1.5, mesh.n_cells), bc_type="Neumann")
+    A = orc.getA().tocsr()
+    A2, pin = GPUSolver._unpin(A)
+    assert pin is not None and list(pin[0]) == [0]
+    assert abs(A2 - A2.T).max() == 0
+    b = rng.standard_normal(A.shape[0])
+    rows, diag, C_ = pin
+    xp = b[rows] / diag
+    x = spla.spsolve(A2.tocsc(), b - C_ @ xp)
+    x0 = spla.spsolve(A.tocsc(), b)
+    np.testing.assert_allclose(x, x0, rtol=1e-10, atol=1e-12 * np.abs(x0).max())
+    # a symmetric matrix passes through unchanged
+    S = (A2 + sp.eye(A2.shape[0])).tocsr()
+    assert GPUSolver._unpin(S)[1] is None
+
+
+def test_solver_argument_warns():
+    """Simulation3DNodal solves on its own engine: a solver class passed to it is reported as unused."""
+    import warnings
+
+    from simpeg_gb300.mesh import TensorMesh
+    from simpeg_gb300.resistivity import Simulation3DNodal
+
+    mesh = TensorMesh([[(10.0, 4)], [(10.0, 4)], [(10.0, 4)]], origin="CCN")
+
+    class SolverLU:
+        pass
+
+    with warnings.catch_warnings(record=True) as rec:
+        warnings.simplefilter("always")
+        try:
+            Simulation3DNodal(mesh, solver=SolverLU)
+        except Exception:
+            pass  # no CUDA here: the engine may fail to build after the warning
+    assert any("SolverLU" in str(w.message) and "not used" in str(w.message) for w in rec)
