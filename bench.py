@@ -32,11 +32,29 @@ import sys
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "source-solves/s + Jtvec/s, 1M-cell DC3D: mixed vs FP64 plain on GB300 @<=1e-6 err"
 RTOL = 1e-9
+
+# SciPy SuperLU (what the reference's default SolverLU runs) on nodal 7-point matrices, measured
+# on one core (Xeon 2.7 GHz): nodes -> (factor s, nnz(L+U), solve s per right-hand side).
+SUPERLU_PROBES = {18513: (1.25, 12.2e6, 6.3e-3), 60025: (21.2, 85.3e6, 40.7e-3), 139425: (136.9, 321e6, 154e-3)}
+
+
+def _superlu_extrapolated(n_nodes=1081665, n_rhs=256):
+    """Power laws through the two largest probes, taken to n_nodes (not run: the fill does not fit)."""
+    (n1, a), (n2, b) = sorted(SUPERLU_PROBES.items())[1:]
+    r = n_nodes / n2
+    ex = [float(np.log(b[i] / a[i]) / np.log(n2 / n1)) for i in range(3)]
+    fac, nnz, sol = (b[i] * r ** ex[i] for i in range(3))
+    return {"nodes": n_nodes, "factor_s": fac, "nnz_LU": nnz, "memory_GB": nnz * 12 / 1e9, "solve_s_per_rhs": sol,
+            f"source_solves_per_s_{n_rhs}": n_rhs / (fac + n_rhs * sol),
+            "exponents": {"factor": ex[0], "fill": ex[1], "solve": ex[2]},
+            "basis": "SciPy SuperLU probes at 60k and 139k nodes (one core), power laws extrapolated; not run"}
 
 
 def _args():
@@ -46,9 +64,11 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the oracle spot checks at full size")
     ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
     ap.add_argument("--sources", type=int, default=0, help="use only the first N sources (profiling runs)")
-    ap.add_argument("--workload", default="forward", choices=["forward", "differentiation", "gauss_newton", "batched"],
+    ap.add_argument("--workload", default="forward",
+                    choices=["forward", "block", "differentiation", "gauss_newton", "batched"],
                     help="forward: the headline 1M-cell line; differentiation: the 96x96x48 gradient checks")
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--profile-solve", action="store_true",
@@ -166,6 +186,79 @@ def _cpu_baseline(mesh, sigma, survey):
     }
 
 
+ORACLE_RTOL = 1e-12
+
+
+def _oracle_spot_worker(mesh, m, src, v_s, rtol):
+    """One source of the oracle (the CPU restatement of the reference path, fp64 SciPy CG + Jacobi
+    to ``rtol``): the source's data and ``J^T v_s`` with respect to m = ln sigma.  Runs in a spawned
+    process (never the product path)."""
+    from oracle.dc3d import OracleDC3DNodal
+    from simpeg_gb300 import maps
+    from simpeg_gb300.resistivity.survey import Survey
+
+    t0 = time.perf_counter()
+    o = OracleDC3DNodal(mesh, Survey([src]), sigma_map=maps.ExpMap(mesh), solver="cg", cg_rtol=rtol)
+    o.set_model(m)
+    f = o.fields()
+    d = o.dpred(f=f)
+    g = o.Jtvec(m, v_s, f=f) if v_s is not None else None
+    return d, g, time.perf_counter() - t0
+
+
+class OracleSpots:
+    """Independent at-scale parity: a few sources of the workload solved by the oracle on the host
+    (spawned processes, one per source, overlapping the GPU work), compared with the GPU path."""
+
+    def __init__(self, mesh, m, survey, idx, v, rtol=ORACLE_RTOL):
+        import multiprocessing as mp
+
+        self.idx = list(idx)
+        self.rtol = rtol
+        ctx = mp.get_context("spawn")
+        env_old = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")}
+        os.environ.update(OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+        self.pool = ctx.Pool(len(self.idx))
+        for k, val in env_old.items():
+            if val is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = val
+        sl = survey.get_all_slices() if hasattr(survey, "get_all_slices") else None
+        self.slices = []
+        self.jobs = []
+        for i in self.idx:
+            src = survey.source_list[i]
+            rx = src.receiver_list[0]
+            s_ = sl[src, rx] if sl is not None else None
+            self.slices.append(s_)
+            vs = None if v is None else np.ascontiguousarray(v[s_])
+            self.jobs.append(self.pool.apply_async(_oracle_spot_worker, (mesh, m, src, vs, rtol)))
+
+    def compare(self, d_gpu, jtvec_gpu_fn, timeout=1800):
+        """d_gpu: the GPU data of the whole survey; jtvec_gpu_fn(i, v_s): the GPU J^T v_s of source i
+        alone.  Returns the worst relative errors over the sources."""
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        ed, eg, secs = [], [], []
+        try:
+            for i, s_, job in zip(self.idx, self.slices, self.jobs):
+                d, g, t = job.get(timeout=timeout)
+                secs.append(t)
+                ed.append(rel(d_gpu[s_], d))
+                if g is not None:
+                    eg.append(rel(jtvec_gpu_fn(i, s_), g))
+        finally:
+            self.pool.close()
+            self.pool.terminate()
+        out = {"sources": self.idx, "dpred": max(ed)}
+        if eg:
+            out["jtvec_m"] = max(eg)
+        out["oracle"] = (f"CPU restatement of the reference path (oracle/), fp64 SciPy CG + Jacobi to rtol "
+                         f"{self.rtol:g}, one process per source")
+        out["oracle_seconds_per_source"] = secs
+        return out
+
+
 def _cpu_worker(mesh, sigma, survey, i, barrier, out):
     """One source of the CPU path in its own process: assembly, then (after every
     worker has assembled) SciPy CG + Jacobi to rtol."""
@@ -248,19 +341,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _traffic_per_unit():
-    """DRAM bytes per (node x RHS) of the fine-level Chebyshev step (fp16 multigrid storage) from the
-    committed ncu summary."""
+def _traffic_by_kind():
+    """DRAM bytes per (node x RHS) of each kind of fine-level Chebyshev step (fp16 multigrid storage),
+    from the committed ncu summary (lines ``dram_bytes_per_node_rhs[<kind>]: <value>``)."""
+    import re
+
     p = ROOT / "profiles" / "cheb_step_fp16_dc3d.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("dram_bytes_per_node_rhs:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            mt = re.match(r"\s*dram_bytes_per_node_rhs\[(\w+)\]:\s*([0-9.eE+-]+)", line)
+            if mt:
+                out[mt.group(1)] = float(mt.group(2))
+    return out
 
 
 def run_gb300(args):
@@ -279,6 +372,13 @@ def run_gb300(args):
     mesh, sigma, survey = _workload(args.n_side, args.sources)
     m = np.log(sigma)
     K = survey.nSrc
+    rng = np.random.default_rng(5)
+    v_host = rng.standard_normal(survey.nD)
+    # independent parity at full size: the first and last source solved by the oracle on the host,
+    # in spawned processes that overlap the GPU work below
+    spots = None
+    if rank == 0 and not args.no_oracle:
+        spots = OracleSpots(mesh, m, survey, sorted({0, K - 1}), v_host)
     sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
     sim.model = m
     sim._ensure_model()
@@ -297,8 +397,6 @@ def run_gb300(args):
         csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U.view(-1), d_out)
         return U, info
 
-    rng = np.random.default_rng(5)
-    v_host = rng.standard_normal(t.nD)
     v_dev = torch.from_numpy(v_host).to(dev)
 
     def jtvec(mode, U):
@@ -335,6 +433,7 @@ def run_gb300(args):
     with Clocks(local) as clk:
         ms_mixed, (U_mixed, info_mixed) = timed(lambda: fwd("mixed"), args.steps)
     st_ms, st_n, st_bytes = eng.stencil_timing(False)
+    kinds = eng.stencil_timing_kinds()
     launches = kernel_launches() - n0
     clocks = clk.summary()
     d_mixed = d_out.cpu().numpy()
@@ -381,14 +480,18 @@ def run_gb300(args):
     d2h = int(t.nD * 8)
 
     value = world * K * args.steps / (ms_mixed / 1e3)
-    peaks = {}
-    pk = ROOT / "MEASURED_PEAKS.json"
-    if pk.exists():
-        peaks = json.loads(pk.read_text())
-    peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = (st_bytes / st_n) / (st_ms / st_n * 1e-3) / 1e9 if st_n else None
-    tpu = _traffic_per_unit()
-    traffic = tpu * mesh.n_nodes * padded_rhs(K) if tpu is not None else None
+    roof = _stencil_roofline(st_ms, st_n, st_bytes, kinds)
+    # DRAM traffic per launch: the ncu bytes of each kind of step, weighted by this run's launch mix
+    tbk = _traffic_by_kind()
+    if roof is not None and kinds and all(k in tbk for k in kinds):
+        units = mesh.n_nodes * padded_rhs(K)
+        roof["traffic"] = sum(c * tbk[k] * units for k, (c, _, _) in kinds.items()) / st_n
+        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per kind of step "
+                                  "(profiles/cheb_step_fp16_dc3d.md), weighted by the launches timed here")
+        for k, v in roof["by_kind"].items():
+            v["traffic_per_launch"] = tbk[k] * units
+    elif roof is not None:
+        roof["traffic_source"] = "no ncu figure for every kind of step timed: not reported"
     line = {
         "metric": METRIC,
         "value": value,
@@ -417,24 +520,25 @@ def run_gb300(args):
         "e2e": {"value": world * K * e2e_steps / e2e_s, "unit": "source-solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "Simulation3DNodal.dpred(m): host model -> H2D -> exp map on device -> set_model -> solve -> gather -> D2H"},
-        "roofline": {
-            "kernel": "k_cheb_step<float,__half,*,32> (fine-level Chebyshev stencil step, fp16 multigrid storage)",
-            "bound": "hbm",
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None,
-            "traffic": traffic,
-            "launches_timed": st_n,
-            "alg_bytes_per_launch": (st_bytes / st_n) if st_n else None,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if pk.exists() else "fallback",
-        },
+        "roofline": roof,
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if spots is not None:
+        from simpeg_gb300.resistivity.survey import Survey
+
+        def jt_one(i, s_):
+            one = Simulation3DNodal(mesh, survey=Survey([survey.source_list[i]]), sigmaMap=maps.ExpMap(mesh),
+                                    precision="mixed", rtol=RTOL)
+            return one.Jtvec(m, v_host[s_])
+
+        line["rel_err_vs_oracle_cg"] = spots.compare(d_mixed, jt_one)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = _cpu_baseline(mesh, sigma, survey)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"]["solver"] = ("SciPy CG + Jacobi (an iterative plug-in): the reference's default "
+                                          "direct solver (SuperLU) does not fit at this size")
+        line["superlu_extrapolated"] = _superlu_extrapolated(mesh.n_nodes, K)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -442,61 +546,147 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def _peak_hbm():
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        return json.loads(pk.read_text()).get("hbm_gbs", 6800.0), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    return 6800.0, "fallback"
+
+
+def _stencil_roofline(ms, n, alg_bytes, kinds=None, what="fine-level Chebyshev steps"):
+    """Roofline of the fine-level Chebyshev steps timed with CUDA events inside a timed region."""
+    if not n:
+        return None
+    peak, src = _peak_hbm()
+    ach = alg_bytes / (ms * 1e-3) / 1e9
+    out = {"kernel": f"k_cheb_step<float,__half,*,*> ({what}, fp16 multigrid storage)", "bound": "hbm",
+           "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+           "launches_timed": n, "alg_bytes_per_launch": alg_bytes / n, "peak_source": src}
+    if kinds:
+        out["by_kind"] = {k: {"launches": c, "us_per_launch": t / c * 1e3, "achieved": b / (t * 1e-3) / 1e9,
+                              "frac": b / (t * 1e-3) / 1e9 / peak} for k, (c, t, b) in kinds.items()}
+    return out
+
+
 def run_differentiation(args):
     """96x96x48 cells, m = ln sigma (ExpMap), 128 dipole sources x 30 receivers.
 
     Gradient of the L2 data misfit by the autograd backward (adjoint solve +
     dA/dsigma kernel), checked against central finite differences (step 1e-4)
-    on random unit directions, and against an fp64 Jtvec at rtol 5e-13 (the
-    oracle at this size); run in fp64 and in mixed precision with forward
-    recomputation.  Prints one JSON line.
+    on random unit directions, against an fp64 Jtvec at rtol 5e-13, and for two
+    sources against the oracle (CPU restatement, SciPy CG to 1e-12); run in
+    fp64 and in mixed precision with forward recomputation.  ``value``: mixed
+    gradients per second with model, data and gradient on the device; ``e2e``:
+    the same from a host model to a host gradient.  Prints one JSON line.
     """
-    import numpy as np
     import torch
 
     from simpeg_gb300 import maps, workloads
     from simpeg_gb300.autograd import dpred
+    from simpeg_gb300.engine import kernel_launches
     from simpeg_gb300.resistivity import Simulation3DNodal
+    from simpeg_gb300.resistivity.survey import Survey
 
-    torch.cuda.set_device(0)
     mesh, m, survey = workloads.differentiation(seed=2)
     rng = np.random.default_rng(11)
+    m0 = m + 0.1 * rng.standard_normal(m.size)
+    v_spot = np.random.default_rng(12).standard_normal(survey.nD)
+    spots = None if args.no_oracle else OracleSpots(mesh, m0, survey, [0, survey.nSrc - 1], v_spot)
+    torch.cuda.set_device(0)
     # fp64 reference at 5e-13 (a 1e-13 target sits at the fp64 residual's rounding floor on this mesh)
     ref = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="fp64", rtol=5e-13)
     d_true = ref.dpred(m)
     dobs = torch.from_numpy(d_true * (1 + 0.03 * rng.standard_normal(d_true.size)))
-    m0 = m + 0.1 * rng.standard_normal(m.size)
     r0 = ref.dpred(m0) - dobs.numpy()
     g_ref = ref.Jtvec(m0, r0)
-    out = {"metric": "misfit gradient: autograd vs central FD and fp64 Jtvec", "workload": "dc3d_differentiation",
-           "config": {"mesh_cells": list(mesh.shape_cells), "nodes": int(mesh.n_nodes), "sources": survey.nSrc,
-                      "data": survey.nD, "fd_step": 1e-4, "directions": args.fd_directions}}
+    del ref
+    torch.cuda.empty_cache()
+    cfg = {"workload": "dc3d_differentiation_96x96x48", "mesh_cells": list(mesh.shape_cells),
+           "nodes": int(mesh.n_nodes), "sources": survey.nSrc, "data": survey.nD, "fd_step": 1e-4,
+           "directions": args.fd_directions, "l2": "inputs larger than L2 (fields 0.47 GB fp64)"}
+    out = {"metric": "misfit gradients/s by autograd (adjoint solve + dA/dsigma kernel), 96x96x48 DC3D: "
+                     "mixed+recompute vs fp64", "unit": "gradients/s", "higher_is_better": True, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 inner / f64 refinement", "data": "synthetic (seeded Gaussian random field)", "config": cfg}
     dirs = [v / np.linalg.norm(v) for v in rng.standard_normal((args.fd_directions, m.size))]
     for label, precision, recompute in (("fp64", "fp64", False), ("mixed_recompute", "mixed", True)):
         sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=precision, rtol=1e-11)
 
-        def phi(mm):
-            r = dpred(sim, mm, recompute=recompute) - dobs
+        def phi(mm, dd):
+            r = dpred(sim, mm, recompute=recompute) - dd
             return 0.5 * (r * r).sum()
 
-        mt = torch.tensor(m0, requires_grad=True)
+        def grad(mm, dd):
+            mt = mm.detach().clone().requires_grad_(True)
+            phi(mt, dd).backward()
+            return mt.grad
+
+        m_dev, d_dev = torch.from_numpy(m0).cuda(), dobs.cuda()
+        for _ in range(args.warmup):
+            grad(m_dev, d_dev)
+            grad(torch.from_numpy(m0), dobs)
         torch.cuda.synchronize()
+        # device resident: model, data and gradient stay on the GPU
+        n0 = kernel_launches()
+        sim.engine.stencil_timing(True)
+        with Clocks(0) as clk:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                g_dev = grad(m_dev, d_dev)
+            e1.record()
+            torch.cuda.synchronize()
+        st = sim.engine.stencil_timing(False)
+        kinds = sim.engine.stencil_timing_kinds()
+        launches = kernel_launches() - n0
+        t_dev = e0.elapsed_time(e1) / 1e3 / args.steps
+        # end to end: host model and data in, host gradient out
         t0 = time.perf_counter()
-        f = phi(mt)
-        f.backward()
-        torch.cuda.synchronize()
-        t_grad = time.perf_counter() - t0
-        g = mt.grad.numpy()
+        for _ in range(args.steps):
+            g = grad(torch.from_numpy(m0), dobs)
+        t_e2e = (time.perf_counter() - t0) / args.steps
+        g = g.numpy()
         errs = []
         for v in dirs:
             with torch.no_grad():
-                fp = phi(torch.from_numpy(m0 + 1e-4 * v)).item()
-                fm = phi(torch.from_numpy(m0 - 1e-4 * v)).item()
+                fp = phi(torch.from_numpy(m0 + 1e-4 * v), dobs).item()
+                fm = phi(torch.from_numpy(m0 - 1e-4 * v), dobs).item()
             fd = (fp - fm) / 2e-4
             errs.append(abs(fd - g @ v) / max(abs(fd), 1e-300))
-        out[label] = {"grad_seconds": t_grad, "fd_max_rel_err": float(max(errs)),
+        out[label] = {"grad_seconds": t_dev, "grad_seconds_e2e": t_e2e, "fd_max_rel_err": float(max(errs)),
                       "fd_median_rel_err": float(np.median(errs)),
-                      "rel_err_vs_fp64_jtvec": float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))}
+                      "rel_err_vs_fp64_jtvec": float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)),
+                      "device_vs_host_model": float(np.linalg.norm(g_dev.cpu().numpy() - g) / np.linalg.norm(g))}
+        if label == "mixed_recompute":
+            out["value"] = 1.0 / t_dev
+            out["ms_per_step"] = t_dev * 1e3
+            out["clocks"] = clk.summary()
+            out["gpu_launches"] = launches
+            out["roofline"] = _stencil_roofline(*st, kinds)
+            out["e2e"] = {"value": 1.0 / t_e2e, "unit": "gradients/s",
+                          "h2d_bytes_per_step": int(m.size * 8 + 2 * survey.nD * 8),
+                          "d2h_bytes_per_step": int(m.size * 8 + survey.nD * 8),
+                          "path": "dpred autograd Function from a host model tensor: m, dobs and dL/dd up, d and "
+                                  "dL/dm down"}
+        del sim
+        torch.cuda.empty_cache()
+    out["speedup_vs_fp64"] = out["fp64"]["grad_seconds"] / out["mixed_recompute"]["grad_seconds"]
+    if spots is not None:
+        sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=1e-11)
+        d_gpu = sim.dpred(m0)
+
+        def jt_one(i, s_):
+            one = Simulation3DNodal(mesh, survey=Survey([survey.source_list[i]]), sigmaMap=maps.ExpMap(mesh),
+                                    precision="mixed", rtol=1e-11)
+            return one.Jtvec(m0, v_spot[s_])
+
+        out["rel_err_vs_oracle_cg"] = spots.compare(d_gpu, jt_one)
+        t_one = float(np.mean(out["rel_err_vs_oracle_cg"]["oracle_seconds_per_source"]))
+        out["cpu_baseline"] = {"value": 1.0 / (t_one * survey.nSrc), "unit": "gradients/s", "cores": 1,
+                               "kind": "port",
+                               "sample": (f"1 of {survey.nSrc} sources timed (forward + adjoint SciPy CG solves to "
+                                          f"1e-12 and the adjoint product on the oracle, {t_one:.0f} s), times "
+                                          f"{survey.nSrc}")}
     print(json.dumps(out), flush=True)
 
 
@@ -508,17 +698,21 @@ def run_gauss_newton(args):
     (electrode reciprocity) for the Jacobi preconditioner, and 10 CG iterations
     on 2 J^T W^2 J + 2 beta R, each one batched Jvec and one batched Jtvec.
     Run in mixed precision and in plain fp64 on the same GPU; prints times and
-    the relative differences of g, diag(J^T J) and the search direction.
+    the relative differences of g, diag(J^T J) and the search direction, and
+    for two sources the data and J^T v against the oracle (SciPy CG to 1e-12).
     """
-    import numpy as np
     import torch
 
     from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.engine import kernel_launches
     from simpeg_gb300.inversion import L2DataMisfit, WeightedLeastSquares, inexact_gauss_newton_direction
     from simpeg_gb300.resistivity import Simulation3DNodal
+    from simpeg_gb300.resistivity.survey import Survey
 
-    torch.cuda.set_device(0)
     mesh, m_true, m0, survey = workloads.gauss_newton(seed=4)
+    v_spot = np.random.default_rng(13).standard_normal(survey.nD)
+    spots = None if args.no_oracle else OracleSpots(mesh, m0, survey, [0, survey.nSrc - 1], v_spot)
+    torch.cuda.set_device(0)
     truth = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=1e-10)
     rng = np.random.default_rng(9)
     d = truth.dpred(m_true)
@@ -539,23 +733,45 @@ def run_gauss_newton(args):
                                        beta, wm0, cg_maxiter=2)
         del wsim
     torch.cuda.synchronize()
-    out = {"metric": "Gauss-Newton step (getJtJdiag + gradient + 10 CG iterations): mixed vs fp64",
-           "workload": "dc3d_gauss_newton",
-           "config": {"mesh_cells": list(mesh.shape_cells), "nodes": int(mesh.n_nodes), "sources": survey.nSrc,
-                      "data": survey.nD, "beta": beta, "cg_iterations": 10, "rtol": RTOL}}
+    out = {"metric": "Gauss-Newton steps/s (getJtJdiag + gradient + 10 CG iterations on J^T J + beta R), "
+                     "2.05M-cell DC3D, 512 sources: mixed vs fp64",
+           "unit": "Gauss-Newton steps/s", "higher_is_better": True, "n_gpus": 1, "steps": 1, "warmup": 1,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement",
+           "data": "synthetic (seeded Gaussian random field; data from the true model + 2 % noise)",
+           "config": {"workload": "dc3d_gauss_newton_160x160x80", "mesh_cells": list(mesh.shape_cells),
+                      "nodes": int(mesh.n_nodes), "sources": survey.nSrc, "data": survey.nD, "beta": beta,
+                      "cg_iterations": 10, "rtol": RTOL, "l2": "inputs larger than L2 (fields 8.6 GB fp64)"}}
     res = {}
     for precision in ("mixed", "fp64"):
         sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=precision, rtol=RTOL)
         dmis = L2DataMisfit(sim, dobs, W=W)
         reg = WeightedLeastSquares(mesh, sim)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        p, info = inexact_gauss_newton_direction(dmis, reg, beta, m0, cg_maxiter=10)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        res[precision] = (p.cpu().numpy(), info["g"].cpu().numpy(), info["jtj_diag"].cpu().numpy())
+        n0 = kernel_launches()
+        sim.engine.stencil_timing(True)
+        with Clocks(0) as clk:
+            t0 = time.perf_counter()
+            p, info = inexact_gauss_newton_direction(dmis, reg, beta, m0, cg_maxiter=10)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            p_host = p.cpu().numpy()  # the step's result on the host (end to end)
+            dt_e2e = time.perf_counter() - t0
+        st = sim.engine.stencil_timing(False)
+        kinds = sim.engine.stencil_timing_kinds()
+        launches = kernel_launches() - n0
+        res[precision] = (p_host, info["g"].cpu().numpy(), info["jtj_diag"].cpu().numpy())
         out[precision] = {"seconds": dt, "cg_rel_res": info["cg_rel_res"][-1],
                           "phases_seconds": {k: round(v, 3) for k, v in info["seconds"].items()}}
+        if precision == "mixed":
+            out["value"] = 1.0 / dt
+            out["ms_per_step"] = dt * 1e3
+            out["clocks"] = clk.summary()
+            out["gpu_launches"] = launches
+            out["roofline"] = _stencil_roofline(*st, kinds)
+            out["e2e"] = {"value": 1.0 / dt_e2e, "unit": "Gauss-Newton steps/s",
+                          "h2d_bytes_per_step": int(m0.size * 8), "d2h_bytes_per_step": int(m0.size * 8),
+                          "path": "inexact_gauss_newton_direction(dmis, reg, beta, m) from a host model; the "
+                                  "search direction copied to the host"}
         del sim, dmis, reg, p, info
         torch.cuda.empty_cache()
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
@@ -563,6 +779,25 @@ def run_gauss_newton(args):
     out["rel_err_mixed_vs_fp64"] = {"direction": rel(res["mixed"][0], res["fp64"][0]),
                                     "gradient": rel(res["mixed"][1], res["fp64"][1]),
                                     "jtj_diag": rel(res["mixed"][2], res["fp64"][2])}
+    if spots is not None:
+        sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+        d_gpu = sim.dpred(m0)
+        del sim
+
+        def jt_one(i, s_):
+            one = Simulation3DNodal(mesh, survey=Survey([survey.source_list[i]]), sigmaMap=maps.ExpMap(mesh),
+                                    precision="mixed", rtol=RTOL)
+            return one.Jtvec(m0, v_spot[s_])
+
+        out["rel_err_vs_oracle_cg"] = spots.compare(d_gpu, jt_one)
+        t_one = float(np.mean(out["rel_err_vs_oracle_cg"]["oracle_seconds_per_source"]))
+        n_solves = 2 * survey.nSrc + 2 * 10 * survey.nSrc
+        out["cpu_baseline"] = {"value": 1.0 / (t_one / 2 * n_solves), "unit": "Gauss-Newton steps/s", "cores": 1,
+                               "kind": "port",
+                               "sample": (f"one source's forward + adjoint SciPy CG solves (1e-12) on the oracle "
+                                          f"timed ({t_one:.0f} s), scaled to the step's {n_solves} source solves "
+                                          "(fields, gradient, 10 x (Jvec + Jtvec)); getJtJdiag's pole solves not "
+                                          "counted")}
     print(json.dumps(out), flush=True)
 
 
@@ -572,32 +807,57 @@ def run_batched(args):
     conductivity.  After the autotuner picks RHS-block width and smoother per
     problem, all 64 adaptive solves are recorded into one CUDA graph whose
     solver loops run on the device; the timed step is one launch of that graph
-    (inputs resident).  Compared with solving the same problems one after the
-    other with the host-driven adaptive solver (identical results)."""
-    import numpy as np
+    (inputs resident).  ``e2e``: the source terms copied up from pinned host
+    memory, one launch, the convergence check and every problem's data copied
+    back (``BatchedForward.run``).  Compared with solving the same problems one
+    after the other with the host-driven adaptive solver (identical results),
+    and for two problems with the oracle (SciPy CG to 1e-12)."""
     import torch
 
     from simpeg_gb300 import workloads
     from simpeg_gb300.batch import BatchedForward
+    from simpeg_gb300.engine import kernel_launches
 
-    torch.cuda.set_device(0)
     probs = workloads.batched_problems(seed=5, n=64)
     nsrc = sum(sv.nSrc for _, _, sv in probs)
+    spot_p = [0, len(probs) - 1]
+    spots = None
+    if not args.no_oracle:
+        from simpeg_gb300.resistivity.survey import Survey
+
+        spots = [OracleSpots(probs[i][0], np.log(probs[i][1]), Survey(probs[i][2].source_list[:1]), [0], None)
+                 for i in spot_p]
+    torch.cuda.set_device(0)
     t0 = time.perf_counter()
     bf = BatchedForward(probs, precision="mixed", rtol=RTOL, tune=True)
     t_setup = time.perf_counter() - t0
     for _ in range(args.warmup):
         bf.launch()
     torch.cuda.synchronize()
+    n0 = kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        bf.launch()
-    e1.record()
-    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            bf.launch()
+        e1.record()
+        torch.cuda.synchronize()
+    launches = kernel_launches() - n0
     ms = e0.elapsed_time(e1) / args.steps
     conv = bf.convergence()
-    # the same problems one by one, adaptive solver, same engines and workspaces
+    data = bf.data()
+    # end to end: source terms up from pinned host memory, launch, check, data down
+    q_host = [p.Q.cpu().pin_memory() for p in bf.problems]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for p, qh in zip(bf.problems, q_host):
+            p.Q.copy_(qh, non_blocking=True)
+        bf.run()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    # the same problems one by one, adaptive solver, same engines and workspaces; fine-level steps timed
+    for p in bf.problems:
+        p.engine.stencil_timing(True)
     torch.cuda.synchronize()
     e0.record()
     for p in bf.problems:
@@ -605,20 +865,169 @@ def run_batched(args):
     e1.record()
     torch.cuda.synchronize()
     ms_seq = e0.elapsed_time(e1)
+    tot = [0.0, 0, 0.0]
+    for p in bf.problems:
+        st = p.engine.stencil_timing(False)
+        tot = [tot[0] + st[0], tot[1] + st[1], tot[2] + st[2]]
     tunes = [getattr(p, "tuning", None) for p in bf.problems]
+    h2d = sum(int(p.Q.numel() * 8) for p in bf.problems)
+    d2h = sum(int(p.tables.nD * 8) for p in bf.problems)
     out = {"metric": "batched uneven problems: source-solves/s, one CUDA-graph launch vs sequential",
            "workload": "dc3d_batched_64", "value": nsrc / (ms / 1e3), "unit": "source-solves/s",
-           "ms_per_launch": ms, "steps": args.steps,
+           "higher_is_better": True, "n_gpus": 1, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 inner / f64 refinement", "data": "synthetic (seeded block + random field per problem)",
+           "ms_per_step": ms, "ms_per_launch": ms, "steps": args.steps, "warmup": args.warmup,
            "sequential": {"ms": ms_seq, "source_solves_per_s": nsrc / (ms_seq / 1e3)},
            "speedup_vs_sequential": ms_seq / ms,
            "converged": all(c[1] == 0 for c in conv), "max_rel_res": max(c[0] for c in conv),
            "inner_iterations": [min(c[2] for c in conv), max(c[2] for c in conv)],
            "setup_seconds": t_setup,
-           "config": {"problems": len(probs), "sources": nsrc,
+           "config": {"workload": "dc3d_batched_64", "problems": len(probs), "sources": nsrc,
                       "nodes_range": [min(p[0].n_nodes for p in probs), max(p[0].n_nodes for p in probs)],
-                      "rtol": RTOL},
-           "autotune": {"kb": sorted({t["kb"] for t in tunes if t}), "nu": sorted({t["nu"] for t in tunes if t})}}
+                      "rtol": RTOL, "l2": "inputs larger than L2 (all problems' vectors, ~2 GB)"},
+           "autotune": {"kb": sorted({t["kb"] for t in tunes if t}), "nu": sorted({t["nu"] for t in tunes if t})},
+           "clocks": clk.summary(), "gpu_launches": launches,
+           "roofline": _stencil_roofline(*tot, what="fine-level Chebyshev steps of every problem, timed in the "
+                                                    "sequential pass (events cannot bracket single kernels inside "
+                                                    "the graph)"),
+           "e2e": {"value": nsrc / t_e2e, "unit": "source-solves/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h, "path": "source terms from pinned host memory -> BatchedForward.run() "
+                                                      "(launch, convergence check, data to the host)"}}
+    if spots is not None:
+        errs, secs = [], []
+        for i, sp_ in zip(spot_p, spots):
+            nd0 = probs[i][2].source_list[0].receiver_list[0].nD
+            r = sp_.compare(data[i][:nd0], None)
+            errs.append(r["dpred"])
+            secs.append(r["oracle_seconds_per_source"][0])
+        out["rel_err_vs_oracle_cg"] = {"problems": spot_p, "sources": [0], "dpred": max(errs),
+                                       "oracle": "CPU restatement of the reference path, fp64 SciPy CG + Jacobi to "
+                                                 f"rtol {ORACLE_RTOL:g}"}
+        t_src = secs[-1]
+        out["cpu_baseline"] = {"value": 1.0 / t_src, "unit": "source-solves/s", "cores": 1, "kind": "port",
+                               "sample": (f"source 0 of problem {spot_p[-1]} ({probs[spot_p[-1]][0].n_nodes} nodes) "
+                                          f"solved by the oracle (SciPy CG + Jacobi to 1e-12), {t_src:.1f} s")}
     print(json.dumps(out), flush=True)
+
+
+def _superlu_step(mesh, sigma, survey):
+    """The reference's default forward path on the host: assembly of A (oracle restatement), SuperLU
+    factorisation (SciPy splu, what pymatsolver.SolverLU wraps), one solve of all sources, dpred."""
+    import scipy.sparse.linalg as spla
+
+    from oracle.dc3d import OracleDC3DNodal
+
+    t0 = time.perf_counter()
+    o = OracleDC3DNodal(mesh, survey, sigma=sigma)
+    A = o.getA().tocsc()
+    q = o.getRHS()
+    t1 = time.perf_counter()
+    lu = spla.splu(A)
+    t2 = time.perf_counter()
+    f = lu.solve(q)
+    t3 = time.perf_counter()
+    d = o.dpred(f=f)
+    t4 = time.perf_counter()
+    return d, {"assembly_s": t1 - t0, "factor_s": t2 - t1, "solve_s": t3 - t2, "dpred_s": t4 - t3, "total_s": t4 - t0}
+
+
+def run_block(args):
+    """32x32x16 cells of 10 m (18,513 nodes), 0.01 S/m with a 0.1 and a 0.001 S/m block, dipole-dipole
+    line of 20 sources x 15 receivers (300 data): the size where the reference's default direct solver
+    fits.  One step = dpred of all 20 sources.  ``value``: GPU mixed precision with the model resident;
+    ``e2e``: ``Simulation3DNodal.dpred(m)`` from a host model to host data; ``cpu_baseline`` /
+    ``--impl reference``: assembly + SuperLU factorisation + solve + dpred on the host, the reference's
+    ``fields`` with ``SolverLU`` (``resistivity/simulation.py:100-113``)."""
+    import torch
+
+    from simpeg_gb300 import maps
+    from simpeg_gb300.engine import csr_spmv, kernel_launches
+    from simpeg_gb300.resistivity import Simulation3DNodal
+    from simpeg_gb300.workloads import block_model_survey
+
+    mesh, sigma, survey, _ = block_model_survey(seed=0)
+    m = np.log(sigma)
+    cfg = {"workload": "dc3d_nodal_block_32x32x16", "mesh_cells": list(mesh.shape_cells), "nodes": int(mesh.n_nodes),
+           "sources": survey.nSrc, "data": survey.nD, "rtol": RTOL,
+           "l2": "working set fits in L2 (18.5k nodes); timed back to back"}
+    metric = "source-solves/s, 32x32x16 block model (300 data): GPU vs the reference's SuperLU path"
+    if args.impl == "reference":
+        for _ in range(args.warmup):
+            _superlu_step(mesh, sigma, survey)
+        ts = [_superlu_step(mesh, sigma, survey)[1] for _ in range(args.steps)]
+        v = survey.nSrc / statistics.median(t["total_s"] for t in ts)
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "source-solves/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": survey.nSrc / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded block model)", "config": cfg, "phases_s": ts[-1],
+                "cpu_baseline": {"value": v, "unit": "source-solves/s", "cores": 1, "kind": "port",
+                                 "sample": "the whole step: oracle assembly + SciPy SuperLU factor + solve + dpred"},
+                "e2e": {"value": v, "unit": "source-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    torch.cuda.set_device(0)
+    res = {}
+    for precision in ("mixed", "fp64"):
+        sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=precision, rtol=RTOL)
+        sim.model = m
+        sim._ensure_model()
+        t, tq = sim._get_tables()
+        Q = sim.getRHS()
+        d_out = torch.empty(t.nD, dtype=torch.float64, device="cuda")
+
+        def step():
+            U, _ = sim.engine.solve(Q, mode=precision, rtol=RTOL)
+            csr_spmv(tq["P_ptr"], tq["P_idx"], tq["P_w"], U.view(-1), d_out)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        n0 = kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(0) as clk:
+            e0.record()
+            for _ in range(args.steps):
+                step()
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        launches = kernel_launches() - n0
+        d_dev = d_out.cpu().numpy()
+        m2 = m + 1e-3
+        sim.dpred(m2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            sim.dpred(m if i % 2 == 0 else m2)
+        e2e = (time.perf_counter() - t0) / args.steps
+        res[precision] = dict(ms=ms, d=d_dev, e2e_s=e2e, clocks=clk.summary(), launches=launches,
+                              iters=sim.last_solve_info.iterations if hasattr(sim, "last_solve_info") else None)
+        del sim
+    d_lu, ph = _superlu_step(mesh, sigma, survey)
+    ph_all = [_superlu_step(mesh, sigma, survey)[1] for _ in range(max(1, min(3, args.steps)))]
+    t_lu = statistics.median(p["total_s"] for p in ph_all)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    K = survey.nSrc
+    line = {
+        "metric": metric, "value": K / (res["mixed"]["ms"] / 1e3), "unit": "source-solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement",
+        "data": "synthetic (seeded block model)", "config": cfg,
+        "fp64_plain": {"source_solves_per_s": K / (res["fp64"]["ms"] / 1e3), "ms_per_step": res["fp64"]["ms"]},
+        "rel_err_vs_superlu": {"dpred_mixed": rel(res["mixed"]["d"], d_lu), "dpred_fp64": rel(res["fp64"]["d"], d_lu)},
+        "superlu": {"phases_s": ph_all[-1], "source_solves_per_s": K / t_lu,
+                    "solve_only_source_solves_per_s": K / statistics.median(p["solve_s"] for p in ph_all)},
+        "e2e": {"value": K / res["mixed"]["e2e_s"], "unit": "source-solves/s", "h2d_bytes_per_step": int(mesh.n_cells * 8),
+                "d2h_bytes_per_step": int(survey.nD * 8), "path": "Simulation3DNodal.dpred(m), host model -> host data"},
+        "cpu_baseline": {"value": K / t_lu, "unit": "source-solves/s", "cores": 1, "kind": "port",
+                         "sample": "the whole step: oracle assembly + SciPy SuperLU factorisation + solve of the 20 "
+                                   "sources + dpred (the reference's default solver path)"},
+        "gpu_launches": res["mixed"]["launches"], "clocks": res["mixed"]["clocks"],
+        "roofline": None,
+        "roofline_note": "18.5k nodes: every vector fits in L2, so no kernel of this size is HBM-bound; the "
+                         "roofline is reported on the 1M-cell forward line",
+    }
+    print(json.dumps(line), flush=True)
 
 
 def run_profile_solve(args):
@@ -644,6 +1053,8 @@ def main():
     args = _args()
     if args.profile_solve:
         return run_profile_solve(args)
+    if args.workload == "block":
+        return run_block(args)
     if args.workload == "batched" and args.impl != "reference":
         return run_batched(args)
     if args.workload == "gauss_newton" and args.impl != "reference":

@@ -122,6 +122,38 @@ int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *c
  * Robin assembly and the solver factorisation (simulation.py:107-108, :523-555). */
 int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream);
 
+/* Cell-centred formulation (Simulation3DCellCentered, simulation.py:321-480).
+ * The handle is created (dc_create) on the cell-centre grid: the tensor mesh
+ * whose nodes are the cell centres (widths = distances between neighbouring
+ * centres, so nx-1 x ny-1 x nz-1 "cells"), with Robin face weights of that
+ * grid for the coarse multigrid levels (NULL for Neumann).  Model update from
+ * the cell resistivity rho_dev (nC, device): the finest operator is
+ * A = Div MfRhoI Grad (getA, :355-378) with MfRhoI the inverse diagonal face
+ * inner product and the boundary term bw_f / rho_c of cell c on boundary face
+ * f; hp_dev holds the widths hx|hy|hz of the mesh, bw_dev the boundary
+ * weights (1 - a_f) A_f^2 / (V_c / 2) packed per side like the Robin face
+ * weights (a_f the ghost-point factor of cell_gradient_weak_form_robin;
+ * NULL: no boundary term, i.e. Neumann).  The coarse levels are rediscretised
+ * from the mean of 1/rho around each cell of the cell-centre grid.  dc_solve
+ * then solves A x = b; with a NULL-face handle the row-0 pin of the Neumann
+ * getA (:365-373) is reproduced as for the nodal operator. */
+int dc_set_model_cc(dc_handle *h, const double *rho_dev, const double *hp_dev, const double *bw_dev, void *stream);
+
+/* out = scale * dA[drho] u for k column-major u (nC rows): the forward
+ * getADeriv of the cell-centred simulation (simulation.py:380-391,
+ * Div MfRhoIDeriv(Grad u, v) with drho = rhoDeriv @ v), a stencil whose
+ * couplings are -(A_f^2 / Mf_f^2) dMf_f and boundary terms -bw_f drho / rho^2. */
+int dc_cc_dadm_fwd(dc_handle *h, const double *rho_dev, const double *drho_dev, const double *hp_dev,
+                   const double *bw_dev, const double *u_dev, double *out_dev, int k, double scale, void *stream);
+
+/* g = scale * drho_dm (.) sum_r dA^T[u_r, lam_r] (nC): the adjoint getADeriv of
+ * the cell-centred simulation summed over the k pairs (simulation.py:380-391,
+ * MfRhoIDeriv(Grad u, Div^T v, adjoint=True)); drho_dm_dev the diagonal of
+ * d rho / d m (NULL: with respect to rho itself). */
+int dc_cc_dadm_adj(dc_handle *h, const double *rho_dev, const double *hp_dev, const double *bw_dev,
+                   const double *u_dev, const double *lam_dev, int k, const double *drho_dm_dev, double scale,
+                   double *g_dev, void *stream);
+
 /* y = A(sigma) x for k column-major RHS, fp64.  (getA() @ x) */
 int dc_apply(dc_handle *h, const double *x_dev, double *y_dev, int k, void *stream);
 
@@ -272,6 +304,14 @@ int dc_edge_fields(dc_handle *h, const double *phi, int k, double *e, double *j,
  * permittivity in F/m (the reference uses scipy.constants.epsilon_0). */
 int dc_node_charge(dc_handle *h, const double *e, int k, double eps0, double *charge, double *charge_density,
                    void *stream);
+
+/* The launches of the last dc_stencil_timing interval split by kind: c =
+ * PREV + 3 * DOT, with PREV 0 (no momentum term), 1 (momentum, x_{k-1}
+ * read) or 2 (second step of a zero start) and DOT 1 for the step that also
+ * emits the r.z partials.  Fills launches[6], total_ms[6] and alg_bytes[6].
+ * Call after dc_stencil_timing(h, 0, ...).  Instrumentation; no reference
+ * counterpart. */
+int dc_stencil_timing_kinds(dc_handle *h, long long *launches, double *total_ms, double *alg_bytes);
 
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */

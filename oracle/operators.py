@@ -9,6 +9,10 @@ The reference calls these ``discretize`` operators (a third-party package,
   ``average_node_to_face``, ``average_cell_to_face``, ``face_areas``
   (``resistivity/simulation.py:588-644``)
 * ``get_interpolation_matrix(loc, "N")`` (``sources.py:84``, ``receivers.py:414,493``)
+* cell-centred formulation (``resistivity/simulation.py:321-480``): ``face_divergence``,
+  ``get_face_inner_product(rho, invert_matrix=True)``, ``cell_gradient_weak_form_robin``,
+  ``closest_points_index(loc, "CC")`` (``sources.py:79-81``) and
+  ``get_interpolation_matrix(loc, "CC")`` (``receivers.py:414``)
 
 Definitions used (3D, Fortran ordering, edges x|y|z, faces x|y|z):
 
@@ -150,6 +154,91 @@ class MeshOps:
             centers=np.array(cents), normals=np.array(norms), areas=np.array(areas),
             cells=np.array(cells), nodes=np.array(nodes4), kind=kind,
         )
+
+    # ---- faces (cell-centred formulation) --------------------------------
+    @property
+    def n_faces(self):
+        nx, ny, nz = self.nx, self.ny, self.nz
+        return ((nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1))
+
+    def face_areas(self):
+        """Areas of the x-, y- and z-faces (Fortran order within each)."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        ax = np.kron(self.hz, np.kron(self.hy, np.ones(nx + 1)))
+        ay = np.kron(self.hz, np.kron(np.ones(ny + 1), self.hx))
+        az = np.kron(np.ones(nz + 1), np.kron(self.hy, self.hx))
+        return np.r_[ax, ay, az]
+
+    def face_divergence_raw(self):
+        """D (nC, nF) = V * face_divergence: D[c, f] = +A_f on the cell's + side, -A_f on its - side."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        Dx = _kron3(sp.eye(nz), sp.eye(ny), _ddx(nx))
+        Dy = _kron3(sp.eye(nz), _ddx(ny), sp.eye(nx))
+        Dz = _kron3(_ddx(nz), sp.eye(ny), sp.eye(nx))
+        return (sp.hstack([Dx, Dy, Dz], format="csr") @ sp.diags(self.face_areas())).tocsr()
+
+    def face_cell_matrix(self):
+        """F (nF, nC): F[f, c] = V_c / 2 for the (one or two) cells holding face f.
+
+        The face inner product of an isotropic property p on a tensor mesh is diagonal:
+        Mf(p) = diag(F p) (each face gets V_c/8 from each of the 4 cell corners it touches)."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        Fx = _kron3(sp.eye(nz), sp.eye(ny), _adj(nx))
+        Fy = _kron3(sp.eye(nz), _adj(ny), sp.eye(nx))
+        Fz = _kron3(_adj(nz), sp.eye(ny), sp.eye(nx))
+        return (sp.vstack([Fx, Fy, Fz], format="csr") @ sp.diags(self.vol / 2.0)).tocsr()
+
+    def boundary_face_index(self):
+        """Global face index of every boundary face, in the order of :meth:`boundary_faces`."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        nfx, nfy, _ = self.n_faces
+        out = []
+        for k in range(nz):
+            for j in range(ny):
+                for i in (0, nx):
+                    out.append(i + (nx + 1) * (j + ny * k))
+        for k in range(nz):
+            for j in (0, ny):
+                for i in range(nx):
+                    out.append(nfx + i + nx * (j + (ny + 1) * k))
+        for k in (0, nz):
+            for j in range(ny):
+                for i in range(nx):
+                    out.append(nfx + nfy + i + nx * (j + ny * k))
+        return np.array(out, dtype=np.int64)
+
+    @property
+    def cell_centers(self):
+        return self.ndgrid(self.ccx, self.ccy, self.ccz)
+
+    def closest_cell(self, locs):
+        """Index of the nearest cell centre of each point (the first one on ties)."""
+        locs = np.atleast_2d(np.asarray(locs, dtype=np.float64))
+        cc = self.cell_centers
+        return np.array([int(np.argmin(((cc - p) ** 2).sum(axis=1))) for p in locs], dtype=np.int64)
+
+    def interpolation_matrix_cc(self, locs):
+        """Trilinear interpolation from the cell centres (same per-axis rule as the nodes: outside
+        the outermost centres the nearest centre gets weights 0.5 + 0.5); points outside the mesh
+        raise."""
+        locs = np.atleast_2d(np.asarray(locs, dtype=np.float64))
+        tol = 1e-10
+        for d, nd in enumerate((self.nodes_x, self.nodes_y, self.nodes_z)):
+            if np.any(locs[:, d] < nd[0] - tol) or np.any(locs[:, d] > nd[-1] + tol):
+                raise ValueError("Points outside of mesh")
+        nx, ny = self.nx, self.ny
+        rows, cols, vals = [], [], []
+        for r, p in enumerate(locs):
+            ix = self._interp1(self.ccx, p[0])
+            iy = self._interp1(self.ccy, p[1])
+            iz = self._interp1(self.ccz, p[2])
+            for a, wa in ((ix[0], ix[2]), (ix[1], ix[3])):
+                for b, wb in ((iy[0], iy[2]), (iy[1], iy[3])):
+                    for c, wc in ((iz[0], iz[2]), (iz[1], iz[3])):
+                        rows.append(r)
+                        cols.append(a + nx * (b + ny * c))
+                        vals.append(wa * wb * wc)
+        return sp.csr_matrix((vals, (rows, cols)), shape=(locs.shape[0], self.nC))
 
     # ---- interpolation -------------------------------------------------
     @staticmethod

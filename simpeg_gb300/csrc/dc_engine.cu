@@ -266,6 +266,8 @@ struct dc_handle {
   // optional timing of the fine-level fp32 Chebyshev stencil launches
   bool prof = false;
   std::vector<cudaEvent_t> prof_ev;  // start/stop pairs
+  std::vector<int> prof_kind;        // per pair: PREV + 3 * (r.z partials)
+  std::vector<double> prof_alg;      // per pair: algorithmic bytes
   int prof_used = 0;
   double prof_bytes = 0.0;
 };
@@ -572,11 +574,14 @@ void timed_cheb(const dc_handle *hc, int l, const Level &F, Rhs<T, V> r, const V
   if (!staged) Ops<T, V, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s);
   if (rec) {
     cudaEventRecord(h->prof_ev[h->prof_used + 1], s);
-    h->prof_used += 2;
     // algorithmic bytes: r (T, or V when stored narrow) and x_k (+ x_{k-1}) (V) read, x_{k+1} (V) written;
     // 16-byte coefficients and the 4-byte 1/diag per node
     const double per_lane = (r.full ? sizeof(T) : sizeof(V)) + (prev == 1 ? 3.0 : 2.0) * sizeof(V);
-    h->prof_bytes += (double)F.dims.N * (per_lane * KB * nb + 20.0);
+    const double bytes = (double)F.dims.N * (per_lane * KB * nb + 20.0);
+    h->prof_kind[h->prof_used / 2] = prev + (partial ? 3 : 0);
+    h->prof_alg[h->prof_used / 2] = bytes;
+    h->prof_bytes += bytes;
+    h->prof_used += 2;
   }
 }
 
@@ -1097,21 +1102,33 @@ int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *c
   return 0;
 }
 
-int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
-  if (!h || !sigma_dev) return fail(DC_ERR_ARG, "NULL argument");
-  cudaStream_t s = (cudaStream_t)stream;
+// The finest level of a cell-centred problem: its operator comes from the cell resistivity
+// (dc_cc.cu), the coarse levels from the dual conductivity in L0.d_sigma.
+struct CCFine {
+  const double *rho, *hp, *bw;
+};
+
+static int set_model_impl(dc_handle *h, const double *sigma_dev, const CCFine *cc, cudaStream_t s) {
   if (!h->built) {
     int rc = build_hierarchy(h);
     if (rc) return rc;
   }
   Level &L0 = h->lv[0];
   const long long nC = (long long)L0.nx * L0.ny * L0.nz;
-  CK(cudaMemcpyAsync(L0.d_sigma, sigma_dev, sizeof(double) * nC, cudaMemcpyDeviceToDevice, s));
+  if (cc)
+    cc_dual_sigma(cc->rho, L0.dims.Nx, L0.dims.Ny, L0.dims.Nz, L0.d_sigma, s);
+  else
+    CK(cudaMemcpyAsync(L0.d_sigma, sigma_dev, sizeof(double) * nC, cudaMemcpyDeviceToDevice, s));
   for (size_t l = 0; l + 1 < h->lv.size(); ++l) coarsen_sigma(h->lv[l], h->lv[l + 1], s);
   // coefficients of every level, then one read-back of the levels' Gershgorin bounds
   const size_t nl = h->lv.size();
   CK(cudaMemsetAsync(h->d_lmax, 0, sizeof(unsigned long long) * nl, s));
-  for (size_t l = 0; l < nl; ++l) coef_build(h->lv[l], h->robin, h->d_lmax + l, s);
+  for (size_t l = 0; l < nl; ++l) {
+    if (l == 0 && cc)
+      cc_coef_build(L0, cc->rho, cc->hp, cc->bw, h->d_lmax, s);
+    else
+      coef_build(h->lv[l], h->robin, h->d_lmax + l, s);
+  }
   std::vector<unsigned long long> bits(nl, 0);
   CK(cudaMemcpyAsync(bits.data(), h->d_lmax, sizeof(unsigned long long) * nl, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -1140,6 +1157,19 @@ int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
   if (flag) return fail(DC_ERR_ARG, "coarsest operator is not positive definite (bad sigma)");
   h->model_set = true;
   return 0;
+}
+
+int dc_set_model(dc_handle *h, const double *sigma_dev, void *stream) {
+  if (!h || !sigma_dev) return fail(DC_ERR_ARG, "NULL argument");
+  return set_model_impl(h, sigma_dev, nullptr, (cudaStream_t)stream);
+}
+
+int dc_set_model_cc(dc_handle *h, const double *rho_dev, const double *hp_dev, const double *bw_dev, void *stream) {
+  if (!h || !rho_dev || !hp_dev) return fail(DC_ERR_ARG, "NULL argument");
+  if (h->lv[0].nx < 1 || h->lv[0].ny < 1 || h->lv[0].nz < 1)
+    return fail(DC_ERR_ARG, "the cell-centre grid needs at least 2 cells per axis");
+  CCFine cc{rho_dev, hp_dev, bw_dev};
+  return set_model_impl(h, nullptr, &cc, (cudaStream_t)stream);
 }
 
 int dc_apply(dc_handle *h, const double *x, double *y, int k, void *stream) {
@@ -1414,6 +1444,39 @@ int dc_dadm_fwd(dc_handle *h, const double *u, const double *dsig, double *out, 
   return 0;
 }
 
+int dc_cc_dadm_fwd(dc_handle *h, const double *rho, const double *drho, const double *hp, const double *bw,
+                   const double *u, double *out, int k, double scale, void *stream) {
+  if (!h || !rho || !drho || !hp || !u || !out || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model_cc first");
+  int rc = ensure_dlev(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Level D = h->lv[0];  // the cell-centre grid, coefficients of dA[drho]
+  D.d_coef64 = h->dlev.d_coef64;
+  D.d_coef32 = h->dlev.d_coef32;
+  D.d_invd64 = h->dlev.d_invd64;
+  D.d_invd32 = h->dlev.d_invd32;
+  cc_dcoef_build(D.dims, rho, drho, hp, bw, D.d_coef64, s);
+  Ops<double, double, 1>::apply(D, u, out, k, nullptr, 0, s);
+  if (scale != 1.0) scale_vec(D.dims.N * (long long)k, out, scale, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_cc_dadm_adj(dc_handle *h, const double *rho, const double *hp, const double *bw, const double *u,
+                   const double *lam, int k, const double *drho_dm, double scale, double *g, void *stream) {
+  if (!h || !rho || !hp || !u || !lam || !g || k < 1) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->built) return fail(DC_ERR_STATE, "dc_set_model_cc first");
+  int rc = ensure_dlev(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Level &L0 = h->lv[0];
+  edge_products(u, lam, k, L0.dims, h->d_P, h->d_Q, s);
+  cc_gradient(L0.dims, h->d_P, h->d_Q, rho, hp, bw, drho_dm, scale, g, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const double *dsig, double scale, double *g,
                 void *stream) {
   if (!h || !u || !lam || !g || k < 1) return fail(DC_ERR_ARG, "bad argument");
@@ -1480,6 +1543,8 @@ int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *lau
     if (h->prof_ev.empty()) {
       h->prof_ev.resize(8192);
       for (auto &e : h->prof_ev) CK(cudaEventCreate(&e));
+      h->prof_kind.assign(h->prof_ev.size() / 2, 0);
+      h->prof_alg.assign(h->prof_ev.size() / 2, 0.0);
     }
     h->prof_used = 0;
     h->prof_bytes = 0.0;
@@ -1497,6 +1562,25 @@ int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *lau
   if (total_ms) *total_ms = tot;
   if (launches) *launches = h->prof_used / 2;
   if (alg_bytes) *alg_bytes = h->prof_bytes;
+  return 0;
+}
+
+int dc_stencil_timing_kinds(dc_handle *h, long long *launches, double *total_ms, double *alg_bytes) {
+  if (!h || !launches || !total_ms || !alg_bytes) return fail(DC_ERR_ARG, "NULL argument");
+  if (h->prof) return fail(DC_ERR_ARG, "stencil timing is still on: stop it with dc_stencil_timing first");
+  for (int c = 0; c < 6; ++c) {
+    launches[c] = 0;
+    total_ms[c] = 0.0;
+    alg_bytes[c] = 0.0;
+  }
+  for (int i = 0; i + 1 < h->prof_used; i += 2) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, h->prof_ev[i], h->prof_ev[i + 1]));
+    const int c = h->prof_kind[i / 2];
+    launches[c] += 1;
+    total_ms[c] += ms;
+    alg_bytes[c] += h->prof_alg[i / 2];
+  }
   return 0;
 }
 

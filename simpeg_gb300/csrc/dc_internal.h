@@ -200,6 +200,16 @@ void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const
 void fill_sparse(long long nnz, const long long *idx, const double *val, double *y, cudaStream_t s);
 void scale_vec(long long n, double *y, double a, cudaStream_t s);
 void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s);
+
+// ---- dc_cc.cu: cell-centred formulation on the cell-centre grid ------------------
+// rho (nC), hp the primal widths hx|hy|hz, bw the packed boundary weights (6 sides; NULL: none)
+void cc_dual_sigma(const double *rho, int nx, int ny, int nz, double *sd, cudaStream_t s);
+void cc_coef_build(const Level &L, const double *rho, const double *hp, const double *bw,
+                   unsigned long long *d_lmax_bits, cudaStream_t s);
+void cc_dcoef_build(const Dims &d, const double *rho, const double *drho, const double *hp, const double *bw,
+                    Coef64 *c64, cudaStream_t s);
+void cc_gradient(const Dims &d, const double *P, const double *Q, const double *rho, const double *hp,
+                 const double *bw, const double *drho_dm, double scale, double *g, cudaStream_t s);
 // Fields3DNodal's derived fields for K potentials (column-major (N, K)): e, j on
 // the edges ((nE, K); either may be null; j needs L.d_sigma), the node charge
 // q ((N, K)) and, from it, the cell charge density ((nC, K); may be null).

@@ -208,6 +208,18 @@ class DCEngine:
         check(lib().dc_stencil_timing(self._h, 1 if enable else 0, C.byref(ms), C.byref(n), C.byref(b)))
         return (ms.value, n.value, b.value) if not enable else None
 
+    STENCIL_KINDS = ("plain", "momentum", "zero_start", "plain_rz", "momentum_rz", "zero_start_rz")
+
+    def stencil_timing_kinds(self):
+        """Per kind of fine-level Chebyshev step (no momentum, momentum, second step of a zero start;
+        each with or without the r.z partials) of the last timing interval:
+        {kind: (launches, total_ms, algorithmic_bytes)} for the kinds that ran."""
+        n = (C.c_longlong * 6)()
+        ms = (C.c_double * 6)()
+        b = (C.c_double * 6)()
+        check(lib().dc_stencil_timing_kinds(self._h, n, ms, b))
+        return {k: (n[i], ms[i], b[i]) for i, k in enumerate(self.STENCIL_KINDS) if n[i]}
+
     def reserve(self, k, mode="mixed"):
         """Allocate the solve workspace for k right-hand sides now (bounded, reused by later solves)."""
         need = self.workspace_bytes(k, mode)

@@ -69,11 +69,12 @@ def test_jtj_diag_vs_oracle(cuda):
     J = sim.getJ(m)
     J0 = orc.getJ(m, f=f)
     assert _rel(J, J0) < TOL
-    # reciprocity kernel: fp32 cell arithmetic on fp64 pole solutions, fp64 accumulation
+    # reciprocity kernel: fp32 cell arithmetic on fp64 pole solutions staged relative to the tile
+    # centre, fp64 accumulation of the per-thread sums (the fp64 reference is 1e-6 away at most)
     diag = sim.getJtJdiag(m)
     diag0 = orc.getJtJdiag(m, f=f)
-    assert np.max(np.abs(diag - diag0) / np.abs(diag0).max()) < 1e-5
-    assert _rel(diag, diag0) < 1e-5
+    assert np.max(np.abs(diag - diag0) / np.abs(diag0).max()) < 1e-6
+    assert _rel(diag, diag0) < 1e-6
 
 
 def test_jtj_diag_weighted_appres(cuda):
@@ -87,7 +88,7 @@ def test_jtj_diag_weighted_appres(cuda):
     orc.set_model(m)
     W = sp.diags(rng.uniform(0.5, 2.0, survey.nD))
     sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), rtol=1e-11)
-    assert _rel(sim.getJtJdiag(m, W=W), orc.getJtJdiag(m, W=W)) < 1e-5
+    assert _rel(sim.getJtJdiag(m, W=W), orc.getJtJdiag(m, W=W)) < 1e-6
 
 
 def _small_mesh():
