@@ -73,6 +73,9 @@ def _args():
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--profile-solve", action="store_true",
                     help="set up the forward workload, run one mixed solve and exit (for ncu captures; no timing)")
+    ap.add_argument("--profile-sens", action="store_true",
+                    help="a reduced Gauss-Newton workload (96x96x48 cells, --sources dipoles): one getJtJdiag and one "
+                         "Jtvec, nothing else (for ncu captures of the sensitivity kernels; no timing)")
     return ap.parse_args()
 
 
@@ -1049,10 +1052,34 @@ def run_profile_solve(args):
     print(json.dumps({"profile_solve": str(info), "sources": survey.nSrc}), flush=True)
 
 
+def run_profile_sens(args):
+    """One getJtJdiag (electrode reciprocity: pole solves + k_jtj_diag) and one Jtvec (adjoint solve +
+    k_edge_products + k_cell_gradient) on a 96x96x48-cell Gauss-Newton-type workload."""
+    import torch
+
+    from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.resistivity import Simulation3DNodal
+    from simpeg_gb300.resistivity.survey import Survey
+
+    torch.cuda.set_device(0)
+    mesh, m_true, m0, survey = workloads.gauss_newton(seed=4, n_lines=8, src_per_line=16, n_rx=24, ncore_xy=80,
+                                                     ncore_z=40)
+    if args.sources:
+        survey = Survey(survey.source_list[:args.sources])
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+    diag = sim.getJtJdiag(m_true)
+    g = sim.Jtvec(m_true, np.ones(survey.nD))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_sens": {"nodes": int(mesh.n_nodes), "sources": survey.nSrc, "data": survey.nD,
+                                       "jtj_sum": float(diag.sum()), "g_norm": float(np.linalg.norm(g))}}), flush=True)
+
+
 def main():
     args = _args()
     if args.profile_solve:
         return run_profile_solve(args)
+    if args.profile_sens:
+        return run_profile_sens(args)
     if args.workload == "block":
         return run_block(args)
     if args.workload == "batched" and args.impl != "reference":

@@ -313,6 +313,18 @@ int dc_node_charge(dc_handle *h, const double *e, int k, double eps0, double *ch
  * counterpart. */
 int dc_stencil_timing_kinds(dc_handle *h, long long *launches, double *total_ms, double *alg_bytes);
 
+/* Fields3DCellCentered derived fields (fields.py:130-185) for k cell-centred
+ * potentials phi (column-major (nC, k)) of a dc_set_model_cc handle: on the
+ * faces (x|y|z, each Fortran-ordered; column-major (nF, k)) e = MfI Grad phi
+ * and j = MfRhoI Grad phi, Grad = Div^T - B; either output may be NULL. */
+int dc_cc_face_fields(dc_handle *h, const double *rho_dev, const double *hp_dev, const double *bw_dev,
+                      const double *phi_dev, int k, double *e_dev, double *j_dev, void *stream);
+
+/* charge = eps0 Div e and charge_density = charge / V on the cells ((nC, k)) from the
+ * face field e of dc_cc_face_fields (fields.py:166-185); either output may be NULL. */
+int dc_cc_charge(dc_handle *h, const double *hp_dev, const double *e_dev, int k, double eps0, double *charge_dev,
+                 double *charge_density_dev, void *stream);
+
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */
 long long dc_kernel_launches(void);

@@ -97,6 +97,8 @@ _SIG = {
     "dc_set_model_cc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "dc_cc_dadm_fwd": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int, C.c_double, _VP]),
     "dc_cc_dadm_adj": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int, _VP, C.c_double, _VP, _VP]),
+    "dc_cc_face_fields": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int, _VP, _VP, _VP]),
+    "dc_cc_charge": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_double, _VP, _VP, _VP]),
     "dc_stencil_timing_kinds": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]),
 }

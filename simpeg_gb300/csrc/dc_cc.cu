@@ -188,6 +188,95 @@ __global__ void k_cc_dual_sigma(const double *__restrict__ rho, int nx, int ny, 
   }
 }
 
+// Fields3DCellCentered (fields.py:130-156): per face f and source s, (Grad phi)_f with
+// Grad = Div^T - B: A_f (phi_L - phi_R) across an interior face (L on the face's - side),
+// -/+ A_f (1 - a_f) phi_c on a boundary face of the mesh's -/+ side (A_f (1 - a_f) = bw_f h_n / 2);
+// e = Grad phi / Mf(1) and j = Grad phi / Mf(rho).  Faces x|y|z, each Fortran-ordered;
+// outputs column-major (nF, K).
+__global__ void k_cc_face_fields(const double *__restrict__ phi, int K, const double *__restrict__ rho,
+                                 const double *__restrict__ h, int nx, int ny, int nz, const double *__restrict__ bw,
+                                 Off6 off, double *__restrict__ eo, double *__restrict__ jo) {
+  const Geo g = geo(h, nx, ny, nz);
+  const long long nC = (long long)nx * ny * nz;
+  const long long nfx = (long long)(nx + 1) * ny * nz, nfy = (long long)nx * (ny + 1) * nz;
+  const long long nF = nfx + nfy + (long long)nx * ny * (nz + 1);
+  const long long total = nF * K;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(t / nF);
+    const long long f = t - (long long)s * nF;
+    const double *ph = phi + (long long)s * nC;
+    int ax, i, j, k;
+    long long r;
+    if (f < nfx) {
+      ax = 0; r = f;
+      i = (int)(r % (nx + 1)); r /= (nx + 1); j = (int)(r % ny); k = (int)(r / ny);
+    } else if (f < nfx + nfy) {
+      ax = 1; r = f - nfx;
+      i = (int)(r % nx); r /= nx; j = (int)(r % (ny + 1)); k = (int)(r / (ny + 1));
+    } else {
+      ax = 2; r = f - nfx - nfy;
+      i = (int)(r % nx); r /= nx; j = (int)(r % ny); k = (int)(r / ny);
+    }
+    const int pos = ax == 0 ? i : (ax == 1 ? j : k);  // face index along the axis
+    const int n_ax = ax == 0 ? nx : (ax == 1 ? ny : nz);
+    const double A = ax == 0 ? g.hy[j] * g.hz[k] : (ax == 1 ? g.hx[i] * g.hz[k] : g.hx[i] * g.hy[j]);
+    // the cells on the face's - side (L) and + side (R)
+    int li = i, lj = j, lk = k;
+    if (ax == 0) li = i - 1; else if (ax == 1) lj = j - 1; else lk = k - 1;
+    double G, mrho, mone;
+    if (pos > 0 && pos < n_ax) {
+      const long long L = g.cell(li, lj, lk), R = g.cell(i, j, k);
+      const double VL = g.vol(li, lj, lk), VR = g.vol(i, j, k);
+      G = A * (ph[L] - ph[R]);
+      mrho = 0.5 * (VL * rho[L] + VR * rho[R]);
+      mone = 0.5 * (VL + VR);
+    } else {
+      const bool lo = pos == 0;  // the mesh's - side: the cell is on the face's + side
+      const int ci = lo ? i : li, cj = lo ? j : lj, ck = lo ? k : lk;
+      const long long c = g.cell(ci, cj, ck);
+      const double V = g.vol(ci, cj, ck);
+      double one_minus_a_A = 0.0;
+      if (bw) {
+        const int side = 2 * ax + (lo ? 0 : 1);
+        const long long in = ax == 0 ? cj + (long long)ny * ck : (ax == 1 ? ci + (long long)nx * ck : ci + (long long)nx * cj);
+        const double hn = ax == 0 ? g.hx[ci] : (ax == 1 ? g.hy[cj] : g.hz[ck]);
+        one_minus_a_A = bw[off.o[side] + in] * 0.5 * hn;
+      }
+      G = (lo ? -1.0 : 1.0) * one_minus_a_A * ph[c];
+      mrho = 0.5 * V * rho[c];
+      mone = 0.5 * V;
+    }
+    if (eo) eo[t] = G / mone;
+    if (jo) jo[t] = G / mrho;
+  }
+}
+
+// charge = eps0 Div e (cells; fields.py:166-185) and charge_density = charge / V, per source.
+__global__ void k_cc_charge(const double *__restrict__ e, int K, const double *__restrict__ h, int nx, int ny, int nz,
+                            double eps0, double *__restrict__ q, double *__restrict__ qd) {
+  const Geo g = geo(h, nx, ny, nz);
+  const long long nC = (long long)nx * ny * nz;
+  const long long nfx = (long long)(nx + 1) * ny * nz, nfy = (long long)nx * (ny + 1) * nz;
+  const long long nF = nfx + nfy + (long long)nx * ny * (nz + 1);
+  const long long total = nC * K;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(t / nC);
+    const long long c = t - (long long)s * nC;
+    const int k = (int)(c / ((long long)nx * ny));
+    const int r = (int)(c - (long long)k * nx * ny);
+    const int j = r / nx, i = r - j * nx;
+    const double *es = e + (long long)s * nF;
+    const long long fx = i + (long long)(nx + 1) * (j + (long long)ny * k);
+    const long long fy = nfx + i + (long long)nx * (j + (long long)(ny + 1) * k);
+    const long long fz = nfx + nfy + c;
+    const double div = g.hy[j] * g.hz[k] * (es[fx + 1] - es[fx]) + g.hx[i] * g.hz[k] * (es[fy + nx] - es[fy]) +
+                       g.hx[i] * g.hy[j] * (es[fz + (long long)nx * ny] - es[fz]);
+    const double qv = eps0 * div;
+    if (q) q[t] = qv;
+    if (qd) qd[t] = qv / g.vol(i, j, k);
+  }
+}
+
 Off6 offsets6(int nx, int ny, int nz) {
   const long long nyz = (long long)ny * nz, nxz = (long long)nx * nz, nxy = (long long)nx * ny;
   return Off6{{0, nyz, 2 * nyz, 2 * nyz + nxz, 2 * nyz + 2 * nxz, 2 * nyz + 2 * nxz + nxy}};
@@ -212,6 +301,19 @@ void cc_dcoef_build(const Dims &d, const double *rho, const double *drho, const 
                     Coef64 *c64, cudaStream_t s) {
   k_cc_dcoef<<<count_launch(grid_flat(d.N, g_n_sm)), TPB, 0, s>>>(rho, drho, hp, d.Nx, d.Ny, d.Nz, bw,
                                                                   offsets6(d.Nx, d.Ny, d.Nz), c64);
+}
+
+void cc_face_fields(const Dims &d, const double *phi, int K, const double *rho, const double *hp, const double *bw,
+                    double *e, double *j, cudaStream_t s) {
+  const long long nF = (long long)(d.Nx + 1) * d.Ny * d.Nz + (long long)d.Nx * (d.Ny + 1) * d.Nz +
+                       (long long)d.Nx * d.Ny * (d.Nz + 1);
+  k_cc_face_fields<<<count_launch(grid_flat(nF * K, g_n_sm)), TPB, 0, s>>>(phi, K, rho, hp, d.Nx, d.Ny, d.Nz, bw,
+                                                                          offsets6(d.Nx, d.Ny, d.Nz), e, j);
+}
+
+void cc_charge(const Dims &d, const double *e, int K, const double *hp, double eps0, double *q, double *qd,
+               cudaStream_t s) {
+  k_cc_charge<<<count_launch(grid_flat(d.N * K, g_n_sm)), TPB, 0, s>>>(e, K, hp, d.Nx, d.Ny, d.Nz, eps0, q, qd);
 }
 
 void cc_gradient(const Dims &d, const double *P, const double *Q, const double *rho, const double *hp,

@@ -1477,6 +1477,22 @@ int dc_cc_dadm_adj(dc_handle *h, const double *rho, const double *hp, const doub
   return 0;
 }
 
+int dc_cc_face_fields(dc_handle *h, const double *rho, const double *hp, const double *bw, const double *phi, int k,
+                      double *e, double *j, void *stream) {
+  if (!h || !rho || !hp || !phi || k < 1 || (!e && !j)) return fail(DC_ERR_ARG, "bad argument");
+  cc_face_fields(h->lv[0].dims, phi, k, rho, hp, bw, e, j, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_cc_charge(dc_handle *h, const double *hp, const double *e, int k, double eps0, double *charge,
+                 double *charge_density, void *stream) {
+  if (!h || !hp || !e || k < 1 || (!charge && !charge_density)) return fail(DC_ERR_ARG, "bad argument");
+  cc_charge(h->lv[0].dims, e, k, hp, eps0, charge, charge_density, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int dc_dadm_adj(dc_handle *h, const double *u, const double *lam, int k, const double *dsig, double scale, double *g,
                 void *stream) {
   if (!h || !u || !lam || !g || k < 1) return fail(DC_ERR_ARG, "bad argument");

@@ -210,6 +210,10 @@ void cc_dcoef_build(const Dims &d, const double *rho, const double *drho, const 
                     Coef64 *c64, cudaStream_t s);
 void cc_gradient(const Dims &d, const double *P, const double *Q, const double *rho, const double *hp,
                  const double *bw, const double *drho_dm, double scale, double *g, cudaStream_t s);
+void cc_face_fields(const Dims &d, const double *phi, int K, const double *rho, const double *hp, const double *bw,
+                    double *e, double *j, cudaStream_t s);
+void cc_charge(const Dims &d, const double *e, int K, const double *hp, double eps0, double *q, double *qd,
+               cudaStream_t s);
 // Fields3DNodal's derived fields for K potentials (column-major (N, K)): e, j on
 // the edges ((nE, K); either may be null; j needs L.d_sigma), the node charge
 // q ((N, K)) and, from it, the cell charge density ((nC, K); may be null).

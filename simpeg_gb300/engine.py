@@ -284,6 +284,91 @@ class DCEngine:
         return g
 
 
+class CCEngine(DCEngine):
+    """The cell-centred operator ``A = Div MfRhoI Grad`` (``Simulation3DCellCentered``) of a tensor
+    mesh, solved on its cell-centre grid (``include/dcgpu.h``: ``dc_set_model_cc``): one unknown per
+    cell (``nN`` = the mesh's cells), the finest operator exact, the coarse multigrid levels
+    rediscretised on the grid of cell centres.  ``nC`` is the number of model cells (the mesh's)."""
+
+    def __init__(self, mesh, bc_type="Robin", surface_faces=None, **kw):
+        from .resistivity.boundary import cc_boundary_weights, cc_grid_face_weights, cell_centre_grid
+
+        grid = cell_centre_grid(mesh)
+        super().__init__(grid.h, cc_grid_face_weights(mesh, bc_type), **kw)
+        nx, ny, nz = (len(w) for w in mesh.h)
+        self._cells = (nx, ny, nz)
+        self.nN = nx * ny * nz  # unknowns: the cells (the grid's nodes)
+        self.nC = self.nN       # model cells
+        self.bc_type = bc_type
+        dev = torch.device("cuda")
+        self.hp = torch.from_numpy(np.concatenate([np.asarray(w, dtype=np.float64) for w in mesh.h])).to(dev)
+        bw = cc_boundary_weights(mesh, bc_type, surface_faces)
+        self.bw = None if bw is None else torch.from_numpy(np.ascontiguousarray(bw)).to(dev)
+        self.rho = None
+
+    def set_model(self, rho):
+        """Model update from the cell resistivity (device, (nC,))."""
+        rho = _dev64(rho, (self.nC,), "rho")
+        check(lib().dc_set_model_cc(self._h, _ptr(rho), _ptr(self.hp), _ptr(self.bw), _stream()))
+        self.rho = rho
+        self._model_set = True
+
+    def dadm_fwd(self, u, drho, scale=1.0):
+        """scale * dA[drho] u for u of shape (k, nN) or (nN,)."""
+        u = _dev64(u, None, "u")
+        u2 = u.reshape(-1, self.nN)
+        drho = _dev64(drho, (self.nC,), "drho")
+        out = torch.empty_like(u2)
+        check(lib().dc_cc_dadm_fwd(self._h, _ptr(self.rho), _ptr(drho), _ptr(self.hp), _ptr(self.bw), _ptr(u2),
+                                   _ptr(out), u2.shape[0], float(scale), _stream()))
+        return out.reshape(u.shape)
+
+    def dadm_adj(self, u, lam, drho_dm=None, scale=1.0):
+        """scale * drho_dm (.) sum_r dA^T[u_r, lam_r] (nC,)."""
+        u = _dev64(u, None, "u").reshape(-1, self.nN)
+        lam = _dev64(lam, None, "lam").reshape(-1, self.nN)
+        if u.shape != lam.shape:
+            raise ValueError("u and lam must have the same shape")
+        if drho_dm is not None:
+            drho_dm = _dev64(drho_dm, (self.nC,), "drho_dm")
+        g = torch.empty(self.nC, dtype=torch.float64, device=u.device)
+        check(lib().dc_cc_dadm_adj(self._h, _ptr(self.rho), _ptr(self.hp), _ptr(self.bw), _ptr(u), _ptr(lam),
+                                   u.shape[0], _ptr(drho_dm), float(scale), _ptr(g), _stream()))
+        return g
+
+    @property
+    def n_faces(self):
+        nx, ny, nz = (int(round(v)) for v in self._cells)
+        return (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1)
+
+    def face_fields(self, phi, e=True, j=True):
+        """(e, j) on the faces for cell potentials phi of shape (k, nN) or (nN,); either may be skipped."""
+        phi = _dev64(phi, None, "phi")
+        p2 = phi.reshape(-1, self.nN)
+        k = p2.shape[0]
+        eo = torch.empty(k, self.n_faces, dtype=torch.float64, device=phi.device) if e else None
+        jo = torch.empty(k, self.n_faces, dtype=torch.float64, device=phi.device) if j else None
+        check(lib().dc_cc_face_fields(self._h, _ptr(self.rho), _ptr(self.hp), _ptr(self.bw), _ptr(p2), k, _ptr(eo),
+                                      _ptr(jo), _stream()))
+        shp = (self.n_faces,) if phi.dim() == 1 else (k, self.n_faces)
+        return (eo.reshape(shp) if e else None), (jo.reshape(shp) if j else None)
+
+    def cell_charge(self, e, eps0, density=False):
+        """(charge, charge_density) on the cells from the face field e (k, nF)."""
+        e = _dev64(e, None, "e")
+        e2 = e.reshape(-1, self.n_faces)
+        k = e2.shape[0]
+        q = torch.empty(k, self.nN, dtype=torch.float64, device=e.device)
+        qd = torch.empty_like(q) if density else None
+        check(lib().dc_cc_charge(self._h, _ptr(self.hp), _ptr(e2), k, float(eps0), _ptr(q), _ptr(qd), _stream()))
+        return q, qd
+
+    def edge_fields(self, *a, **k):
+        raise NotImplementedError("the cell-centred fields live on the faces (face_fields)")
+
+    node_charge = edge_fields
+
+
 def padded_rhs(k):
     """RHS count the engine pads k to (blocks of KB lanes, at most 1/8 of them idle)."""
     for kb in (32, 16, 8, 4, 2, 1):

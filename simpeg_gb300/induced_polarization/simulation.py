@@ -1,4 +1,4 @@
-"""GPU ``Simulation3DNodal`` for induced polarization.
+"""GPU ``Simulation3DNodal`` and ``Simulation3DCellCentered`` for induced polarization.
 
 Drop-in for ``simpeg.electromagnetics.static.induced_polarization.Simulation3DNodal``
 (``simpeg/electromagnetics/static/induced_polarization/simulation.py:15-167``).
@@ -28,8 +28,9 @@ import torch
 
 from ..maps import IdentityMap
 from ..resistivity.simulation import Simulation3DNodal as _DCSimulation3DNodal
+from ..resistivity.simulation_cc import Simulation3DCellCentered as _DCSimulation3DCellCentered
 
-__all__ = ["Simulation3DNodal"]
+__all__ = ["Simulation3DNodal", "Simulation3DCellCentered"]
 
 
 class _Weights:
@@ -183,3 +184,30 @@ class Simulation3DNodal(_DCSimulation3DNodal):
 
     def jtvec_dev(self, w_dev, f=None):
         return super().jtvec_dev(self._scale_t() * w_dev, f=f)
+
+
+class Simulation3DCellCentered(Simulation3DNodal, _DCSimulation3DCellCentered):
+    """3D cell-centred IP problem on a tensor mesh, solved on the GPU
+    (``induced_polarization/simulation.py:160-163``): the IP logic of
+    :class:`Simulation3DNodal` on the cell-centred DC operator, whose property is the
+    resistivity: ``rhoDeriv = diag(rho) etaDeriv`` (``simulation.py:40-42``)."""
+
+    def _sigma_deriv(self):
+        """d rho / d m = rho * d eta / d m."""
+        mp = self.etaMap if self.etaMap is not None else IdentityMap()
+        r = 1.0 / np.asarray(self.sigma, dtype=np.float64)
+        if hasattr(mp, "diag_deriv") and getattr(mp, "is_diagonal", True):
+            m = self._model if self._model is not None else np.zeros(self.nC)
+            return r * mp.diag_deriv(m)
+        D = mp.deriv(self._model)
+        if sp.issparse(D):
+            D = D.tocsr()
+            if D.shape[0] == D.shape[1] and D.nnz == np.count_nonzero(D.diagonal()):
+                return r * np.asarray(D.diagonal(), dtype=np.float64)
+        return sp.diags(r) @ D
+
+    def _dc_fields(self):
+        if self._f is None:
+            self._ensure_model()
+            self._f = _DCSimulation3DCellCentered.fields(self, None)
+        return self._f

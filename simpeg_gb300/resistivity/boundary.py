@@ -102,3 +102,68 @@ def robin_face_weights(mesh, surface_faces=None):
         alpha[ok] = (r_vec[ok] @ n) / r[ok] ** 2
         parts.append(0.25 * alpha * a)
     return np.concatenate(parts)
+
+
+# ---------------------------------------------------------------- cell-centred formulation
+def cc_boundary_weights(mesh, bc_type="Robin", surface_faces=None):
+    """Boundary terms of the cell-centred operator ``Div MfRhoI (Div^T - B)``
+    (``resistivity/simulation.py:421-480`` with ``cell_gradient_weak_form_robin``), packed
+    per side like :func:`robin_face_weights`: ``bw_f = (1 - a_f) A_f^2 / (V_c / 2)``, so that
+    boundary face f adds ``bw_f / rho_c`` to the diagonal of its cell c.
+
+    ``a_f = (1 / h_f) / (alpha_f + 1 / h_f)`` is the ghost-point factor of the Robin condition
+    ``alpha phi + d phi / dn = 0`` (beta = 1, gamma = 0), h_f the distance from the cell centre
+    to the face (half the cell's width normal to it), alpha_f as in :func:`robin_face_weights`
+    (zero on the surface faces).  Dirichlet (phi = 0 on the boundary, the formulation's natural
+    condition): a_f = 0.  Neumann: None (no boundary term)."""
+    if bc_type == "Mixed":
+        bc_type = "Robin"
+    if bc_type == "Neumann":
+        return None
+    h, _, _ = _geom(mesh)
+    hn = [h[0][0], h[0][-1], h[1][0], h[1][-1], h[2][0], h[2][-1]]  # normal width of the boundary cells
+    p = source_point(mesh)
+    masks = surface_mask_by_side(mesh, surface_faces)
+    parts = []
+    for side, ((c, n, a), surf) in enumerate(zip(_side_faces(mesh), masks)):
+        if bc_type == "Dirichlet":
+            one_minus_a = np.ones(a.size)
+        elif bc_type == "Robin":
+            r_vec = c - p
+            r = np.linalg.norm(r_vec, axis=1)
+            alpha = np.zeros(r.size)
+            ok = ~surf
+            alpha[ok] = (r_vec[ok] @ n) / r[ok] ** 2
+            hf = 0.5 * hn[side]
+            one_minus_a = alpha * hf / (alpha * hf + 1.0)
+        else:
+            raise ValueError(f"bc_type must be Dirichlet, Neumann, Robin or Mixed, not {bc_type!r}")
+        parts.append(one_minus_a * 2.0 * a / hn[side])  # A^2 / (V/2) = 2 A / h_n
+    return np.concatenate(parts)
+
+
+def cell_centre_grid(mesh):
+    """The tensor mesh whose nodes are the cell centres of ``mesh`` (widths: the distances
+    between neighbouring centres), on which the cell-centred unknowns are solved."""
+    from ..mesh import TensorMesh
+
+    h, _, cc = _geom(mesh)
+    if min(len(w) for w in h) < 2:
+        raise ValueError("the cell-centred simulation needs at least 2 cells per axis")
+    return TensorMesh([0.5 * (w[1:] + w[:-1]) for w in h], origin=[c[0] for c in cc])
+
+
+def cc_grid_face_weights(mesh, bc_type="Robin"):
+    """Robin face weights of the cell-centre grid for the coarse multigrid levels (None for
+    Neumann): the nodal Robin weights of that grid, or for Dirichlet a Robin condition of
+    alpha = 2 / h_n (phi = 0 half a boundary cell beyond the outermost centres) on every side."""
+    if bc_type == "Mixed":
+        bc_type = "Robin"
+    if bc_type == "Neumann":
+        return None
+    grid = cell_centre_grid(mesh)
+    if bc_type == "Robin":
+        return robin_face_weights(grid)
+    h, _, _ = _geom(mesh)
+    hn = [h[0][0], h[0][-1], h[1][0], h[1][-1], h[2][0], h[2][-1]]
+    return np.concatenate([0.25 * (2.0 / hn[s]) * a for s, (_, _, a) in enumerate(_side_faces(grid))])

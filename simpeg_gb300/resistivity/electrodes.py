@@ -67,6 +67,46 @@ def interp_weights(mesh, locs, tol=1e-10):
     return idx, w
 
 
+def cc_coords(mesh):
+    return [0.5 * (n[1:] + n[:-1]) for n in node_coords(mesh)]
+
+
+def cc_interp_weights(mesh, locs, tol=1e-10):
+    """(n, 8) cell indices and weights of the interpolation from the cell centres to ``locs``
+    (``get_interpolation_matrix(loc, "CC")``): the per-axis rule of :func:`interp_weights` on the
+    cell-centre coordinates, so beyond the outermost centre the nearest one takes the value; points
+    outside the mesh raise."""
+    locs = np.atleast_2d(np.asarray(locs, dtype=np.float64))
+    if locs.shape[1] != 3:
+        raise ValueError("electrode locations must be (n, 3)")
+    nodes = node_coords(mesh)
+    for d in range(3):
+        if np.any(locs[:, d] < nodes[d][0] - tol) or np.any(locs[:, d] > nodes[d][-1] + tol):
+            raise ValueError("Points outside of mesh")
+    cc = cc_coords(mesh)
+    nx, ny = cc[0].size, cc[1].size
+    ax = [_axis_interp(cc[d], locs[:, d]) for d in range(3)]
+    idx = np.empty((locs.shape[0], 8), dtype=np.int64)
+    w = np.empty((locs.shape[0], 8), dtype=np.float64)
+    c = 0
+    for a in (0, 1):
+        for b in (0, 1):
+            for e in (0, 1):
+                idx[:, c] = ax[0][a] + nx * (ax[1][b] + ny * ax[2][e])
+                w[:, c] = ax[0][2 + a] * ax[1][2 + b] * ax[2][2 + e]
+                c += 1
+    return idx, w
+
+
+def closest_cells(mesh, locs):
+    """Index of the cell centre nearest to each point (``closest_points_index(loc, "CC")``; ties go
+    to the lowest index, which on a tensor grid is the per-axis nearest centre, lowest first)."""
+    locs = np.atleast_2d(np.asarray(locs, dtype=np.float64))
+    cc = cc_coords(mesh)
+    ijk = [np.argmin(np.abs(cc[d][None, :] - locs[:, d][:, None]), axis=1) for d in range(3)]
+    return (ijk[0] + cc[0].size * (ijk[1] + cc[1].size * ijk[2])).astype(np.int64)
+
+
 def interpolation_matrix(mesh, locs):
     idx, w = interp_weights(mesh, locs)
     n = idx.shape[0]
@@ -92,9 +132,14 @@ class SurveyTables:
       flat target indices, ``PT_ptr``/``PT_idx``/``PT_w`` the CSR over data.
     """
 
-    def __init__(self, mesh, source_list, nN):
+    def __init__(self, mesh, source_list, nN, grid="N"):
+        """``grid`` "N": nodal unknowns (trilinear electrodes); "CC": cell-centred unknowns (sources
+        at the nearest cell centre, ``sources.py:79-81``; receivers interpolated from the centres)."""
         self.nN = int(nN)
         self.nSrc = len(source_list)
+        if grid not in ("N", "CC"):
+            raise ValueError("grid must be 'N' or 'CC'")
+        interp = interp_weights if grid == "N" else cc_interp_weights
         # source term: every electrode of every source in one interpolation
         locs, curs, sidx = [], [], []
         for s, src in enumerate(source_list):
@@ -106,7 +151,17 @@ class SurveyTables:
             locs.append(L)
             curs.append(cur)
             sidx.append(np.full(L.shape[0], s, dtype=np.int64))
-        if locs:
+        if locs and grid == "CC":
+            # q[closest cell] = current: an assignment, so a later electrode in the same cell wins
+            cells = closest_cells(mesh, np.concatenate(locs))
+            keys = np.concatenate(sidx) * self.nN + cells
+            vals = np.concatenate(curs)
+            last = {}
+            for kk, vv in zip(keys.tolist(), vals.tolist()):
+                last[kk] = vv
+            qi = np.fromiter(last.keys(), dtype=np.int64, count=len(last))
+            qv = np.fromiter(last.values(), dtype=np.float64, count=len(last))
+        elif locs:
             idx, w = interp_weights(mesh, np.concatenate(locs))
             qi = (idx + (np.concatenate(sidx) * self.nN)[:, None]).ravel()
             qv = (np.concatenate(curs)[:, None] * w).ravel()
@@ -153,7 +208,7 @@ class SurveyTables:
             for locs_, rows_, src_, sign in ((m_locs, m_rows, m_src, 1.0), (n_locs, n_rows, n_src, -1.0)):
                 if not locs_:
                     continue
-                idx, w = interp_weights(mesh, np.concatenate(locs_))
+                idx, w = interp(mesh, np.concatenate(locs_))
                 parts_r.append(np.repeat(np.concatenate(rows_), 8))
                 parts_c.append((idx + (np.concatenate(src_) * self.nN)[:, None]).ravel())
                 parts_v.append(sign * w.ravel())

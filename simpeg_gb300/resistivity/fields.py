@@ -95,3 +95,38 @@ class Fields3DNodal:
             self.phi_dev[idx] = v.T
         else:
             self.phi_dev[idx] = v
+
+
+class Fields3DCellCentered(Fields3DNodal):
+    """Device-backed ``Fields3DCellCentered`` (``resistivity/fields.py:75-185``): the cell-centred
+    potential of every source, and on request ``e = MfI Grad phi`` and ``j = MfRhoI Grad phi`` on
+    the faces (x|y|z faces, each Fortran-ordered) and ``charge = eps0 Div e``,
+    ``charge_density = charge / V`` on the cells (``dc_cc_face_fields`` / ``dc_cc_charge``)."""
+
+    knownFields = {"phiSolution": "CC"}
+    aliasFields = {
+        "phi": ["phiSolution", "CC", "_phi"],
+        "j": ["phiSolution", "F", "_j"],
+        "e": ["phiSolution", "F", "_e"],
+        "charge": ["phiSolution", "CC", "_charge"],
+        "charge_density": ["phiSolution", "CC", "_charge_density"],
+    }
+
+    def _GLoc(self, fieldType):
+        if fieldType == "phi":
+            return "CC"
+        if fieldType in ("e", "j"):
+            return "F"
+        raise KeyError("Field type must be phi, e, j")
+
+    def _derived(self, idx, name):
+        from scipy.constants import epsilon_0
+
+        eng = self.simulation.engine
+        phi = self.phi_dev[idx]
+        if name in ("e", "j"):
+            e, j = eng.face_fields(phi, e=name == "e", j=name == "j")
+            return e if name == "e" else j
+        e, _ = eng.face_fields(phi, e=True, j=False)
+        q, qd = eng.cell_charge(e, epsilon_0, density=name == "charge_density")
+        return q if name == "charge" else qd

@@ -44,6 +44,9 @@ class Simulation3DNodal:
 
     _solutionType = "phiSolution"
     _formulation = "EB"
+    fieldsPair = Fields3DNodal
+    _grid = "N"  # where the unknowns live: nodes (electrodes interpolated trilinearly)
+    _bc_types = ("Robin", "Neumann")
 
     def __init__(self, mesh, survey=None, bc_type="Robin", sigma=None, sigmaMap=None, rho=None, rhoMap=None,
                  solver=None, solver_opts=None, storeJ=False, miniaturize=False, surface_faces=None,
@@ -70,10 +73,10 @@ class Simulation3DNodal:
         self.solver_opts = {} if solver_opts is None else dict(solver_opts)
         if bc_type == "Mixed":
             bc_type = "Robin"
-        if bc_type == "Dirichlet":
+        if bc_type == "Dirichlet" and "Dirichlet" not in self._bc_types:
             raise ValueError("Dirichlet conditions are not supported in the Nodal formulation")
-        if bc_type not in ("Robin", "Neumann"):
-            raise ValueError(f"bc_type must be Neumann, Robin or Mixed, not {bc_type!r}")
+        if bc_type not in self._bc_types:
+            raise ValueError(f"bc_type must be one of {self._bc_types + ('Mixed',)}, not {bc_type!r}")
         self.bc_type = bc_type
         self.surface_faces = surface_faces
         if precision not in ("mixed", "fp64"):
@@ -93,15 +96,21 @@ class Simulation3DNodal:
         self._mini_survey = None
         if self._miniaturize:
             self._dipoles, self._invs, self._mini_survey = mini_pole_pole(self.survey)
-        eo = dict(engine_opts or {})
-        # Neumann: no Robin term; the engine reproduces the reference's row-0
-        # pinned solve (simulation.py:535-540) on the symmetric operator.
-        bface = robin_face_weights(mesh, surface_faces) if bc_type == "Robin" else None
-        self.engine = DCEngine(mesh.h, bface, **eo)
+        self.engine = self._make_engine(dict(engine_opts or {}))
         self.nN = self.engine.nN
         self.nC = self.engine.nC
         self._tables = None
         self._clear()
+
+    def _make_engine(self, eo):
+        # Neumann: no Robin term; the engine reproduces the reference's row-0
+        # pinned solve (simulation.py:535-540) on the symmetric operator.
+        bface = robin_face_weights(self.mesh, self.surface_faces) if self.bc_type == "Robin" else None
+        return DCEngine(self.mesh.h, bface, **eo)
+
+    def _engine_set_property(self, sigma_dev):
+        """Model update of the engine from the conductivity on the device."""
+        self.engine.set_model(sigma_dev)
 
     # ------------------------------------------------------------ properties
     @property
@@ -181,6 +190,15 @@ class Simulation3DNodal:
         return 1.0 / self.sigma
 
     def _sigma_deriv(self):
+        """Derivative of the property the operator is built from (here the conductivity) with
+        respect to the model: its diagonal as an array, or a sparse matrix for general maps."""
+        return self._conductivity_deriv()
+
+    def _property_deriv_dev(self, d_sigma_dev):
+        """:meth:`_sigma_deriv` on the device from the diagonal of d sigma / d m on the device."""
+        return d_sigma_dev
+
+    def _conductivity_deriv(self):
         """Diagonal of d sigma / d m as an array, or a sparse matrix for general maps."""
         mp = self.sigmaMap
         if mp is None:
@@ -196,7 +214,7 @@ class Simulation3DNodal:
 
     @property
     def sigmaDeriv(self):
-        d = self._sigma_deriv()
+        d = self._conductivity_deriv()
         if d is None:
             return None
         return sp.diags(d) if isinstance(d, np.ndarray) else d
@@ -206,7 +224,7 @@ class Simulation3DNodal:
 
     def _get_tables(self):
         if self._tables is None:
-            t = SurveyTables(self.mesh, self._active_survey().source_list, self.nN)
+            t = SurveyTables(self.mesh, self._active_survey().source_list, self.nN, grid=self._grid)
             dev = self.device
             self._tables = t
             self._tq = dict(
@@ -238,7 +256,7 @@ class Simulation3DNodal:
                 if np.any(~np.isfinite(s)) or np.any(s <= 0):
                     raise ValueError("conductivity must be positive and finite")
                 self._sigma_dev = torch.from_numpy(np.ascontiguousarray(s)).to(self.device)
-            self.engine.set_model(self._sigma_dev)
+            self._engine_set_property(self._sigma_dev)
         return self._sigma_dev
 
     # device bytes the solver workspace may take per call; larger RHS sets are solved in chunks
@@ -346,8 +364,8 @@ class Simulation3DNodal:
         if not bool(((s > 0) & torch.isfinite(s)).all()):
             raise ValueError("conductivity must be positive and finite")
         self._sigma_dev = s.contiguous()
-        self.engine.set_model(self._sigma_dev)
-        f = Fields3DNodal(self, self._solve(self.getRHS()))
+        self._engine_set_property(self._sigma_dev)
+        f = self.fieldsPair(self, self._solve(self.getRHS()))
         self._f_cache = f
         return f
 
@@ -357,7 +375,7 @@ class Simulation3DNodal:
         self._ensure_model()
         Q = self.getRHS()
         U = self._solve(Q)
-        f = Fields3DNodal(self, U)
+        f = self.fieldsPair(self, U)
         self._f_cache = f
         return f
 
@@ -491,7 +509,7 @@ class Simulation3DNodal:
         if getattr(self, "_dsig_cache", None) is None or self._dsig_cache[0] is not key:
             mp = self.sigmaMap
             if self._model_dev is not None and hasattr(mp, "diag_deriv_dev") and getattr(mp, "is_diagonal", True):
-                dd = mp.diag_deriv_dev(self._model_dev).contiguous()
+                dd = self._property_deriv_dev(mp.diag_deriv_dev(self._model_dev)).contiguous()
             else:
                 d = self._sigma_deriv()
                 if not isinstance(d, np.ndarray):
