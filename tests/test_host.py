@@ -573,12 +573,12 @@ def test_simulation_sigma_derivative_selection():
     s = Stub()
     s.sigmaMap = ExpMap(mesh)
     s._model = np.linspace(-1.0, 1.0, 12)
-    d = Simulation3DNodal._sigma_deriv(s)
+    d = Simulation3DNodal._conductivity_deriv(s)
     assert isinstance(d, np.ndarray)
     np.testing.assert_allclose(d, np.exp(s._model))
     s.sigmaMap = ComboMap([ExpMap(), InjectActiveCells(mesh, act, value_inactive=-3.0)])
     s._model = m_act
-    D = Simulation3DNodal._sigma_deriv(s)
+    D = Simulation3DNodal._conductivity_deriv(s)
     assert sp_.issparse(D) and D.shape == (12, act.sum())
     np.testing.assert_allclose(D.toarray()[act], np.diag(np.exp(m_act)))
 
