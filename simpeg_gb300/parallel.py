@@ -11,8 +11,14 @@ into survey order, and ``Jtvec``/``getJtJdiag`` all-reduce an ``nC`` vector --
 the only data-path collective of this path.
 
 ``sim_factory(survey_chunk)`` builds the rank's simulation (the GPU
-``Simulation3DNodal`` in production; the tests pass CPU stand-ins with the same
+``Simulation3DNodal`` in production; the CPU tests pass stand-ins with the same
 methods so the collective logic runs under ``gloo``).
+
+The collectives move tensors: on the rank's CUDA device under NCCL (which only
+takes device tensors), on the host under gloo.  The data gather needs no size
+exchange: the round-robin split tells every rank how many data every other rank
+holds, so the pieces are padded to the largest and gathered with one
+``all_gather``.
 """
 
 from __future__ import annotations
@@ -40,13 +46,23 @@ class ShardedSimulation:
         # datum index ranges of every source in survey order
         nd = [src.nD for src in survey.source_list]
         self._starts = np.r_[0, np.cumsum(nd)].astype(np.int64)
+        self._rank_sources = [list(range(r, survey.nSrc, self.world)) for r in range(self.world)]
+        self._rank_nd = [int(sum(nd[i] for i in s)) for s in self._rank_sources]
+        backend = dist.get_backend(group) if dist.is_initialized() else "gloo"
+        self._comm_device = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" \
+            else torch.device("cpu")
 
     # --------------------------------------------------------------- helpers
     def _gather_data(self, local):
-        """Concatenate per-rank data pieces back into survey order."""
-        parts = [None] * self.world
+        """Concatenate per-rank data pieces back into survey order (one padded all_gather)."""
+        local = np.asarray(local, dtype=np.float64)
         if self.world > 1:
-            self.dist.all_gather_object(parts, (self.my_sources, local), group=self.group)
+            width = max(max(self._rank_nd), 1)
+            buf = torch.zeros(width, dtype=torch.float64, device=self._comm_device)
+            buf[:local.size] = torch.as_tensor(local, device=self._comm_device)
+            bufs = [torch.empty_like(buf) for _ in range(self.world)]
+            self.dist.all_gather(bufs, buf, group=self.group)
+            parts = [(self._rank_sources[r], bufs[r][:self._rank_nd[r]].cpu().numpy()) for r in range(self.world)]
         else:
             parts = [(self.my_sources, local)]
         out = np.zeros(self.survey.nD)
@@ -66,10 +82,11 @@ class ShardedSimulation:
             if self.my_sources else np.zeros(0)
 
     def _sum(self, vec, n):
-        t = torch.as_tensor(np.zeros(n) if vec is None else np.asarray(vec, dtype=np.float64))
+        t = torch.as_tensor(np.zeros(n) if vec is None else np.asarray(vec, dtype=np.float64),
+                            device=self._comm_device)
         if self.world > 1:
             self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
-        return t.numpy()
+        return t.cpu().numpy()
 
     # --------------------------------------------------------------- API
     def dpred(self, m):

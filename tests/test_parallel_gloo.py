@@ -1,7 +1,8 @@
 """Source-sharded simulation over two ranks (gloo, CPU): dpred/Jvec gathered
 and Jtvec/getJtJdiag all-reduced equal the single-process results
 (tests/meta/test_meta_sim.py recipe).  The per-rank simulation here is the
-CPU oracle; on GPU machines each rank runs Simulation3DNodal on its own GPU."""
+CPU oracle, or (GPU test) the GPU Simulation3DNodal; on a multi-GPU machine each rank
+runs it on its own GPU and the collectives go over NCCL with device tensors."""
 
 import os
 import socket
@@ -37,7 +38,7 @@ def _case():
     return mesh, Survey(srcs), m
 
 
-def _worker(rank, world, port, q):
+def _worker(rank, world, port, q, gpu=False):
     import scipy.sparse as sp
     import torch.distributed as dist
 
@@ -50,7 +51,13 @@ def _worker(rank, world, port, q):
         from simpeg_gb300.parallel import ShardedSimulation
 
         mesh, survey, m = _case()
-        factory = lambda sv: OracleDC3DNodal(mesh, sv, sigma_map=maps.ExpMap(mesh))
+        if gpu:  # the GPU simulation as each rank's child (both ranks share cuda:0 here)
+            from simpeg_gb300.resistivity import Simulation3DNodal
+
+            factory = lambda sv: Simulation3DNodal(mesh, survey=sv, sigmaMap=maps.ExpMap(mesh), rtol=1e-12,
+                                                   precision="fp64")
+        else:
+            factory = lambda sv: OracleDC3DNodal(mesh, sv, sigma_map=maps.ExpMap(mesh))
         sharded = ShardedSimulation(survey, factory)
         full = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
         rng = np.random.default_rng(3)
@@ -69,11 +76,11 @@ def _worker(rank, world, port, q):
         dist.destroy_process_group()
 
 
-def test_sharded_simulation_two_ranks():
+def _run_two_ranks(gpu):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q, gpu)) for r in range(2)]
     for p in procs:
         p.start()
     out = [q.get(timeout=300) for _ in procs]
@@ -83,4 +90,15 @@ def test_sharded_simulation_two_ranks():
     assert sorted(n for _, _, n in out) == [2, 3]
     for rank, errs, _ in out:
         for k, e in errs.items():
-            assert e < 1e-9, (rank, k, e)
+            assert e < (1e-8 if gpu else 1e-9), (rank, k, e)
+
+
+def test_sharded_simulation_two_ranks():
+    _run_two_ranks(gpu=False)
+
+
+@pytest.mark.gpu
+def test_sharded_simulation_two_ranks_gpu_children():
+    """The same collectives with GPU simulations as the ranks' children (gloo between the two
+    processes; no kernel of one rank waits on the other)."""
+    _run_two_ranks(gpu=True)
