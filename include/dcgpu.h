@@ -325,6 +325,37 @@ int dc_cc_face_fields(dc_handle *h, const double *rho_dev, const double *hp_dev,
 int dc_cc_charge(dc_handle *h, const double *hp_dev, const double *e_dev, int k, double eps0, double *charge_dev,
                  double *charge_density_dev, void *stream);
 
+/* Continuous-batching session of the mixed-precision solver: the serving form
+ * of fields (resistivity/simulation.py:100-113), whose Ainv * RHS solves all
+ * sources of one model together.  A session holds the refinement state of
+ * `lanes` right-hand-side lanes of one handle (its current model, Robin
+ * conditions) between calls, so that right-hand sides join and leave while
+ * the others keep iterating:
+ *   dc_lanes_open   lays out (or allocates, ws == NULL) the lanes' workspace
+ *                   (dc_solve_workspace_bytes(h, DC_MODE_MIXED, lanes));
+ *                   *capacity receives the usable lane count (lanes rounded up
+ *                   to whole RHS blocks); every lane starts empty
+ *   dc_lanes_load   writes n right-hand sides b (column-major (N, n), device)
+ *                   into lanes lanes_dev[0..n) (int, device), x = 0 there
+ *   dc_lanes_sweep  one refinement sweep over the active lanes: inner fp32
+ *                   multigrid-PCG of each lane to its own tolerance, x += d,
+ *                   double-float residual; *n_active receives the lanes still
+ *                   above rtol (a lane's iterates never depend on the others')
+ *   dc_lanes_state  per lane (capacity entries, host): active flag and the
+ *                   relative residual |b - A x| / |b| of the last sweep
+ *   dc_lanes_fetch  x of lanes lanes_dev[0..n) into x_dev (column-major (N, n))
+ * A lane is free again once its solution is fetched (load overwrites it).
+ * Calls on one session are ordered on the caller's stream; sessions of
+ * different handles run concurrently on different streams. */
+typedef struct dc_lanes dc_lanes;
+int dc_lanes_open(dc_handle *h, int lanes, double rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_lanes **out,
+                  int *capacity);
+int dc_lanes_load(dc_lanes *s, const int *lanes_dev, int n, const double *b_dev, void *stream);
+int dc_lanes_sweep(dc_lanes *s, int *n_active, int *iterations, void *stream);
+int dc_lanes_state(dc_lanes *s, int *active, double *rel_res, void *stream);
+int dc_lanes_fetch(dc_lanes *s, const int *lanes_dev, int n, double *x_dev, void *stream);
+void dc_lanes_close(dc_lanes *s);
+
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */
 long long dc_kernel_launches(void);

@@ -99,6 +99,13 @@ _SIG = {
     "dc_cc_dadm_adj": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int, _VP, C.c_double, _VP, _VP]),
     "dc_cc_face_fields": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int, _VP, _VP, _VP]),
     "dc_cc_charge": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_double, _VP, _VP, _VP]),
+    "dc_lanes_open": (C.c_int, [_VP, C.c_int, C.c_double, C.c_int, _VP, C.c_size_t, C.POINTER(_VP),
+                                C.POINTER(C.c_int)]),
+    "dc_lanes_load": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),
+    "dc_lanes_sweep": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), _VP]),
+    "dc_lanes_state": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_double), _VP]),
+    "dc_lanes_fetch": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),
+    "dc_lanes_close": (None, [_VP]),
     "dc_stencil_timing_kinds": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]),
 }

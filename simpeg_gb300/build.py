@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "libdcgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["dc_stencil.cu", "dc_ops_f64.cu", "dc_ops_f32.cu", "dc_ops_f16.cu", "dc_ops_bf16.cu", "dc_sens.cu", "dc_engine.cu",
-           "dc_noalloc.cu", "dc_csr.cu", "dc_jtj.cu", "dc_cc.cu"]
+           "dc_noalloc.cu", "dc_csr.cu", "dc_jtj.cu", "dc_cc.cu", "dc_lanes.cu"]
 
 
 def _nvcc():

@@ -956,7 +956,59 @@ int solve_dispatch(dc_handle *h, int mode, const double *b, double *x, int k, do
   }
 }
 
+// One refinement sweep of a lane session (the sweep of solve_kb's mixed
+// branch): inner fp32 PCG on the active lanes to their own tolerances,
+// x += d, double-float residual, new per-lane flags and tolerances.
+template <int KB>
+int lanes_sweep_kb(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int *it, cudaStream_t s) {
+  const Level &F = h->lv[0];
+  const long long N = F.dims.N;
+  const int nb = w.nb, Kp = w.Kp, gx = w.gx;
+  float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
+  float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
+  CK(cudaMemsetAsync(w.sc.status, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
+  int rc;
+  if (w.storage == DC_MG_FP16)
+    rc = pcg<float, __half, KB>(h, w.d32, w.r32, (__half *)w.pv, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
+                                w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+  else if (w.storage == DC_MG_BF16)
+    rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, (__nv_bfloat16 *)w.pv, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16,
+                                       w.sc, nb, gx, w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+  else
+    rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
+                               w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+  if (rc == DC_ERR_BREAKDOWN) return rc;
+  ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, s);
+  ir_residual_df<KB>(F, h->d_cdf_hi, h->d_cdf_lo, bh, bl, xh, xl, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, s);
+  sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
+  outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
+              inner_rtol * inner_rtol, kSafety2, s);
+  return 0;
+}
+
+int lanes_sweep(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int *it, cudaStream_t s) {
+  switch (w.KB) {
+    case 32: return lanes_sweep_kb<32>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    case 16: return lanes_sweep_kb<16>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    case 8: return lanes_sweep_kb<8>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    case 4: return lanes_sweep_kb<4>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    case 2: return lanes_sweep_kb<2>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    default: return lanes_sweep_kb<1>(h, w, rtol, inner_rtol, inner_cap, it, s);
+  }
+}
+
 }  // namespace
+
+// A continuous-batching session: the mixed solve's state for a fixed set of
+// lanes, kept between calls.
+struct dc_lanes {
+  dc_handle *h = nullptr;
+  SolveWS w{};
+  void *own = nullptr;
+  double rtol = 1e-9, inner_rtol = 3e-5;
+  int inner_maxit = 200;
+};
 
 // ====================================================================== C ABI
 extern "C" {
@@ -1579,6 +1631,115 @@ int dc_stencil_timing(dc_handle *h, int enable, double *total_ms, long long *lau
   if (launches) *launches = h->prof_used / 2;
   if (alg_bytes) *alg_bytes = h->prof_bytes;
   return 0;
+}
+
+int dc_lanes_open(dc_handle *h, int lanes, double rtol, int inner_maxit, void *ws, size_t ws_bytes, dc_lanes **out,
+                  int *capacity) {
+  if (!h || !out || lanes < 1 || lanes > 32 * kMaxRhsBlocks || !(rtol > 0.0)) return fail(DC_ERR_ARG, "bad argument");
+  if (!h->model_set) return fail(DC_ERR_STATE, "dc_set_model first");
+  if (!h->robin) return fail(DC_ERR_ARG, "lane sessions need Robin boundary conditions (no row-0 pin)");
+  dc_lanes *L = new dc_lanes();
+  L->h = h;
+  L->rtol = rtol;
+  L->inner_rtol = kInnerRtol;
+  L->inner_maxit = inner_maxit > 0 ? inner_maxit : 200;
+  layout_ws(h, DC_MODE_MIXED, lanes, nullptr, L->w);
+  char *base = (char *)ws;
+  if (base) {
+    if (ws_bytes < L->w.bytes) {
+      delete L;
+      return fail(DC_ERR_NOMEM, "workspace too small");
+    }
+  } else {
+    if (cudaMalloc(&L->own, L->w.bytes) != cudaSuccess) {
+      delete L;
+      return fail(DC_ERR_NOMEM, "cannot allocate the lane workspace");
+    }
+    base = (char *)L->own;
+  }
+  base = (char *)(((uintptr_t)base + 255) & ~(uintptr_t)255);
+  layout_ws(h, DC_MODE_MIXED, lanes, base, L->w);
+  const size_t n = (size_t)h->lv[0].dims.N * L->w.Kp;
+  SolveWS &w = L->w;
+  // every lane empty: b = x = r = 0, |b|^2 = 0 (inactive)
+  CK(cudaMemset(w.R64, 0, sizeof(double) * n));
+  CK(cudaMemset(w.X64, 0, sizeof(double) * n));
+  CK(cudaMemset(w.r32, 0, sizeof(float) * n));
+  CK(cudaMemset(w.sc.bb64, 0, sizeof(double) * w.Kp));
+  CK(cudaMemset(w.sc.rr64, 0, sizeof(double) * w.Kp));
+  CK(cudaMemset(w.sc.active_out, 0, sizeof(int) * w.Kp));
+  CK(cudaMemset(w.sc.n_active_out, 0, sizeof(int)));
+  CK(cudaMemset(w.sc.tol2, 0, sizeof(double) * w.Kp));
+  CK(cudaMemset(w.sc.loop, 0, 4 * sizeof(int)));
+  CK(cudaDeviceSynchronize());
+  *out = L;
+  if (capacity) *capacity = w.Kp;
+  return 0;
+}
+
+int dc_lanes_load(dc_lanes *L, const int *lanes_dev, int n, const double *b_dev, void *stream) {
+  if (!L || !lanes_dev || !b_dev || n < 1 || n > L->w.Kp) return fail(DC_ERR_ARG, "bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  SolveWS &w = L->w;
+  const long long N = L->h->lv[0].dims.N;
+  float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * w.Kp;
+  float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * w.Kp;
+  lanes_load(b_dev, n, lanes_dev, N, w.KB, bh, bl, w.r32, xh, xl, w.sc.bb64, w.sc.rr64, s);
+  outer_check(w.Kp, w.sc.rr64, w.sc.bb64, L->rtol * L->rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel,
+              w.sc.tol2, L->inner_rtol * L->inner_rtol, kSafety2, s);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_lanes_sweep(dc_lanes *L, int *n_active, int *iterations, void *stream) {
+  if (!L) return fail(DC_ERR_ARG, "NULL session");
+  cudaStream_t s = (cudaStream_t)stream;
+  dc_handle *h = L->h;
+  int it = 0;
+  int rc = lanes_sweep(h, L->w, L->rtol, L->inner_rtol, L->inner_maxit, &it, s);
+  if (rc) return rc == DC_ERR_BREAKDOWN ? fail(rc, "PCG breakdown in a lane session") : rc;
+  CK(cudaMemcpyAsync(h->h_mail, L->w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev, s));
+  CK(cudaEventSynchronize(h->ev));
+  if (n_active) *n_active = h->h_mail[0];
+  if (iterations) *iterations = it;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int dc_lanes_state(dc_lanes *L, int *active, double *rel_res, void *stream) {
+  if (!L || (!active && !rel_res)) return fail(DC_ERR_ARG, "bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int K = L->w.Kp;
+  std::vector<double> rr(K), bb(K);
+  if (active) CK(cudaMemcpyAsync(active, L->w.sc.active_out, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
+  if (rel_res) {
+    CK(cudaMemcpyAsync(rr.data(), L->w.sc.rr64, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bb.data(), L->w.sc.bb64, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (rel_res)
+    for (int j = 0; j < K; ++j) rel_res[j] = bb[j] > 0.0 ? std::sqrt(rr[j] / bb[j]) : 0.0;
+  return 0;
+}
+
+int dc_lanes_fetch(dc_lanes *L, const int *lanes_dev, int n, double *x_dev, void *stream) {
+  if (!L || !lanes_dev || !x_dev || n < 1 || n > L->w.Kp) return fail(DC_ERR_ARG, "bad argument");
+  SolveWS &w = L->w;
+  const long long N = L->h->lv[0].dims.N;
+  const float *xh = reinterpret_cast<const float *>(w.X64), *xl = xh + (size_t)N * w.Kp;
+  lanes_fetch(xh, xl, n, lanes_dev, N, w.KB, x_dev, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+void dc_lanes_close(dc_lanes *L) {
+  if (!L) return;
+  if (L->own) {
+    cudaDeviceSynchronize();
+    cudaFree(L->own);
+  }
+  delete L;
 }
 
 int dc_stencil_timing_kinds(dc_handle *h, long long *launches, double *total_ms, double *alg_bytes) {

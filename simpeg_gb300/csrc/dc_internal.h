@@ -201,6 +201,12 @@ void fill_sparse(long long nnz, const long long *idx, const double *val, double 
 void scale_vec(long long n, double *y, double a, cudaStream_t s);
 void edge_products(const double *u, const double *l, int K, const Dims &d, double *P, double *Q, cudaStream_t s);
 
+// ---- dc_lanes.cu: lanes of a continuous-batching session ------------------------
+void lanes_load(const double *b, int n, const int *lanes, long long N, int KB, float *bh, float *bl, float *r32,
+                float *xh, float *xl, double *bb, double *rr, cudaStream_t s);
+void lanes_fetch(const float *xh, const float *xl, int n, const int *lanes, long long N, int KB, double *x,
+                 cudaStream_t s);
+
 // ---- dc_cc.cu: cell-centred formulation on the cell-centre grid ------------------
 // rho (nC), hp the primal widths hx|hy|hz, bw the packed boundary weights (6 sides; NULL: none)
 void cc_dual_sigma(const double *rho, int nx, int ny, int nz, double *sd, cudaStream_t s);

@@ -284,6 +284,67 @@ class DCEngine:
         return g
 
 
+class LaneSession:
+    """A continuous-batching session of the mixed-precision solver on one engine (``dc_lanes_*`` in
+    ``include/dcgpu.h``): right-hand sides are loaded into free lanes while the other lanes keep
+    iterating, one refinement sweep at a time, and each lane's solution is fetched when it has
+    converged.  The workspace is laid out once (``capacity`` lanes) and reused."""
+
+    def __init__(self, engine, lanes, rtol=1e-9, inner_maxit=200, ws=None):
+        self.engine = engine
+        self._s = C.c_void_p()
+        cap = C.c_int()
+        if ws is None:
+            ws = torch.empty(engine.workspace_bytes(lanes, "mixed"), dtype=torch.uint8, device="cuda")
+        self._ws = ws
+        check(lib().dc_lanes_open(engine._h, int(lanes), float(rtol), int(inner_maxit), _ptr(ws), ws.numel(),
+                                  C.byref(self._s), C.byref(cap)))
+        self.capacity = cap.value
+        self.nN = engine.nN
+
+    def _idx(self, lanes):
+        return torch.as_tensor(np.asarray(lanes, dtype=np.int32), device=self._ws.device)
+
+    def load(self, lanes, B):
+        """Right-hand sides B (len(lanes), nN) (device, float64) into the given lanes."""
+        B = _dev64(B, (len(lanes), self.nN), "B")
+        idx = self._idx(lanes)
+        check(lib().dc_lanes_load(self._s, _ptr(idx), len(lanes), _ptr(B), _stream()))
+
+    def sweep(self):
+        """One refinement sweep of the active lanes; returns (lanes still active, inner iterations)."""
+        n, it = C.c_int(), C.c_int()
+        check(lib().dc_lanes_sweep(self._s, C.byref(n), C.byref(it), _stream()))
+        return n.value, it.value
+
+    def state(self):
+        """(active flags, relative residuals) of every lane (host arrays)."""
+        act = (C.c_int * self.capacity)()
+        rel = (C.c_double * self.capacity)()
+        check(lib().dc_lanes_state(self._s, act, rel, _stream()))
+        return np.frombuffer(act, dtype=np.int32).copy(), np.frombuffer(rel, dtype=np.float64).copy()
+
+    def fetch(self, lanes, out=None):
+        """Solutions of the given lanes as a (len(lanes), nN) device tensor (into ``out`` if given)."""
+        if out is None:
+            out = torch.empty(len(lanes), self.nN, dtype=torch.float64, device=self._ws.device)
+        idx = self._idx(lanes)
+        check(lib().dc_lanes_fetch(self._s, _ptr(idx), len(lanes), _ptr(out), _stream()))
+        return out
+
+    def close(self):
+        if getattr(self, "_s", None) is not None and self._s.value:
+            torch.cuda.synchronize()
+            lib().dc_lanes_close(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class CCEngine(DCEngine):
     """The cell-centred operator ``A = Div MfRhoI Grad`` (``Simulation3DCellCentered``) of a tensor
     mesh, solved on its cell-centre grid (``include/dcgpu.h``: ``dc_set_model_cc``): one unknown per

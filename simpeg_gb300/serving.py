@@ -1,48 +1,69 @@
 """Continuous-batching server for DC forward requests on one GPU.
 
 A request is ``(model, survey)`` on the server's mesh: predict the data of
-every source of ``survey`` for conductivity ``sigmaMap * model``.  The server
-keeps a fixed pool of *slots*; a slot is one engine handle (per-model stencil
-hierarchy), one CUDA stream and one solve workspace sized for ``max_rhs``
-right-hand sides, so the pool's device memory is reserved up front and
-bounded.  Worker threads (one per slot) take requests as soon as their slot
-frees up -- requests that arrive while others are on the GPU are admitted
-without waiting for a batch boundary -- and their kernels overlap on the
-device through the slots' streams.  A worker merges queued requests that share
-the same model into one multi-RHS solve (up to ``max_rhs`` sources), the
-batching the reference does with ``Ainv * RHS`` over ``(nN, nSrc)``
-(``simpeg/electromagnetics/static/resistivity/simulation.py:111``).
+every source of ``survey`` for conductivity ``sigmaMap * model``.  Every
+source is one right-hand side of the model's operator, as in the reference's
+``Ainv * RHS`` over ``(nN, nSrc)`` (``simpeg/electromagnetics/static/
+resistivity/simulation.py:100-113``).
 
-Each right-hand side of a multi-RHS solve has its own CG scalars and
-convergence flag, so a request's result does not depend on what it was
-batched with beyond rounding of the reductions (the server test checks alone
-vs. mixed within the solver tolerance).
+The server keeps a fixed pool of *slots*.  A slot is one engine handle (the
+stencil hierarchy of its current model), one CUDA stream and one *lane
+session* (``dc_lanes_*`` in ``include/dcgpu.h``): the state of a
+mixed-precision solve with ``max_rhs`` right-hand-side lanes that persists
+between refinement sweeps.  The slot's worker thread loops:
+
+1. admit: if the slot is idle it takes the oldest queued request and sets its
+   model; a running slot admits further queued requests *of its model* into
+   its free lanes -- between two sweeps of the solve that is already running;
+2. one refinement sweep of every active lane (each lane iterates to its own
+   tolerance; a lane's iterates never depend on the others', so a request's
+   result is the same alone and in any mix);
+3. every request whose lanes have all converged is fetched, gathered at its
+   receivers and answered, and its lanes are free for the next admission.
+
+Requests that arrive while others are on the GPU are therefore admitted as
+lanes free up, without waiting for the running solve to end, and the slots'
+sweeps overlap on the device through their streams.  Admission is FIFO: a
+request is not overtaken by later requests of its model, nor by requests of a
+model that is running while it has no slot to go to.
+
+Memory: each slot's engine hierarchy, lane workspace and two
+``max_rhs x nN`` staging arrays (right-hand sides in, solutions out) are
+allocated when the server starts; a request adds only its electrode tables.
 
 Failure handling is host-side: a request whose model is invalid, whose
-electrodes fall outside the mesh or that needs more right-hand sides than a
-slot holds fails with an exception on its own future; other requests and the
-slots are unaffected.  ``engine_factory`` lets tests drive the scheduler with
-a fake engine on the CPU.
+electrodes fall outside the mesh, that needs more right-hand sides than a
+slot holds or that does not converge within ``max_sweeps`` fails with an
+exception on its own future; other requests and the slots are unaffected.
+
+``engine_factory(slot_index)`` lets tests drive the scheduler on the CPU: an
+engine with ``lanes_backend(capacity)`` gets the lane scheduler with that
+backend, one with ``run_batch(models, surveys)`` a batch scheduler that merges
+queued requests of one model into one call.
 """
 
 from __future__ import annotations
 
 import hashlib
-import queue
 import threading
+import time
 from concurrent.futures import Future
 from dataclasses import dataclass, field
 
 import numpy as np
 
-__all__ = ["DCServer", "AdmissionError"]
+__all__ = ["DCServer", "AdmissionError", "NotConvergedError"]
 
 
 class AdmissionError(RuntimeError):
     """The request cannot be admitted (too many sources for a slot, or the server is closed)."""
 
 
-@dataclass
+class NotConvergedError(RuntimeError):
+    """A request's solve did not reach the tolerance within the sweep limit."""
+
+
+@dataclass(eq=False)  # requests compare by identity
 class _Request:
     model: np.ndarray
     survey: object
@@ -50,22 +71,121 @@ class _Request:
     key: str
     nsrc: int
     seq: int = 0
-    tables: object = None
+    lanes: list = field(default_factory=list)
+    state: object = None
+    sweeps: int = 0
+    t_submit: float = 0.0
 
 
 @dataclass
 class _Slot:
     index: int
     engine: object
-    stream: object = None
-    busy: bool = False
+    backend: object = None
+    key: object = None
+    free: list = field(default_factory=list)
+    running: list = field(default_factory=list)
     served: int = 0
-    batches: list = field(default_factory=list)
+    sweeps: int = 0
+    batches: list = field(default_factory=list)  # batch mode: request seqs per engine call
+    log: list = field(default_factory=list)      # lane mode: (event, seq, sweep, requests running)
+    sweep_events: list = field(default_factory=list)
 
 
 def _model_key(m):
     a = np.ascontiguousarray(m, dtype=np.float64)
     return hashlib.sha1(a.view(np.uint8)).hexdigest()
+
+
+class _CudaLanes:
+    """Lane backend of one slot on the GPU: engine, stream, lane session and staging arrays."""
+
+    def __init__(self, server, engine, capacity):
+        import torch
+
+        self.srv = server
+        self.engine = engine
+        self.stream = torch.cuda.Stream()
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.capacity = capacity
+        self.session = None
+        nN = engine.nN
+        self.Q = torch.zeros(capacity, nN, dtype=torch.float64, device=self.dev)
+        self.X = torch.empty(capacity, nN, dtype=torch.float64, device=self.dev)
+        # the engine's solve workspace for `capacity` lanes, laid out once
+        self.ws = torch.empty(engine.workspace_bytes(capacity, "mixed"), dtype=torch.uint8, device=self.dev)
+
+    def set_model(self, m):
+        import torch
+
+        from .engine import LaneSession
+
+        sigma = self.srv.sigma_map * m
+        if np.any(~np.isfinite(sigma)) or np.any(sigma <= 0):
+            raise ValueError("conductivity must be positive and finite")
+        with torch.cuda.stream(self.stream):
+            self.engine.set_model(torch.from_numpy(np.ascontiguousarray(sigma)).to(self.dev))
+            if self.session is None:
+                self.session = LaneSession(self.engine, self.capacity, rtol=self.srv.rtol, ws=self.ws)
+                self.capacity = min(self.capacity, self.session.capacity)
+
+    def prepare(self, r):
+        import torch
+
+        from .resistivity.electrodes import SurveyTables
+
+        t = SurveyTables(self.srv.mesh, r.survey.source_list, self.engine.nN)
+        to = lambda a: torch.from_numpy(a).to(self.dev)
+        return dict(t=t, q_idx=to(t.q_idx), q_val=to(t.q_val), P=(to(t.P_ptr), to(t.P_idx), to(t.P_w)))
+
+    def load(self, lanes, r):
+        import torch
+
+        from .engine import fill_sparse
+
+        n = len(lanes)
+        st = r.state
+        with torch.cuda.stream(self.stream):
+            Q = self.Q[:n]
+            Q.zero_()
+            fill_sparse(st["q_idx"], st["q_val"], Q.view(-1))
+            self.session.load(lanes, Q)
+
+    def clear(self, lanes):
+        import torch
+
+        with torch.cuda.stream(self.stream):
+            Q = self.Q[:len(lanes)]
+            Q.zero_()
+            self.session.load(lanes, Q)
+
+    def sweep(self):
+        import torch
+
+        with torch.cuda.stream(self.stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = self.session.sweep()
+            e1.record()
+        return out, (e0, e1)
+
+    def active(self):
+        import torch
+
+        with torch.cuda.stream(self.stream):
+            return self.session.state()[0]
+
+    def finish(self, lanes, r):
+        import torch
+
+        from .engine import csr_spmv
+
+        st = r.state
+        with torch.cuda.stream(self.stream):
+            X = self.session.fetch(lanes, out=self.X[:len(lanes)])
+            d = torch.empty(st["t"].nD, dtype=torch.float64, device=self.dev)
+            csr_spmv(*st["P"], X.reshape(-1), d)
+            return d.cpu().numpy()
 
 
 class DCServer:
@@ -75,14 +195,15 @@ class DCServer:
     ----------
     mesh : tensor mesh (``h``, ``origin``)
     sigma_map : model -> conductivity map (default ExpMap: models are ln sigma)
-    slots : number of concurrent requests on the device
-    max_rhs : right-hand sides per slot (sources of the merged requests)
-    precision, rtol : solver arithmetic and tolerance
+    slots : number of concurrently running models on the device
+    max_rhs : right-hand-side lanes per slot (a request's sources must fit)
+    precision, rtol : solver arithmetic and tolerance (the lane sessions are mixed precision)
+    max_sweeps : refinement sweeps after which a request fails as not converged
     engine_factory : callable(slot_index) -> engine (default: CUDA engine)
     """
 
     def __init__(self, mesh, sigma_map=None, slots=2, max_rhs=256, precision="mixed", rtol=1e-9,
-                 surface_faces=None, engine_factory=None, device=None):
+                 surface_faces=None, engine_factory=None, device=None, max_sweeps=40):
         from .maps import ExpMap
 
         self.mesh = mesh
@@ -90,20 +211,33 @@ class DCServer:
         self.max_rhs = int(max_rhs)
         self.precision = precision
         self.rtol = float(rtol)
+        self.max_sweeps = int(max_sweeps)
         self.nN = int(np.prod([len(h) + 1 for h in mesh.h]))
         self.nC = int(np.prod([len(h) for h in mesh.h]))
-        self._q = queue.Queue()
         self._pending = []
         self._lock = threading.Lock()
         self._cv = threading.Condition(self._lock)
         self._closed = False
         self._seq = 0
         self._device = device
-        if engine_factory is None:
+        cuda = engine_factory is None
+        if cuda:
+            import torch
+
+            if precision != "mixed":
+                raise ValueError("the server's lane sessions solve in mixed precision")
             engine_factory = self._cuda_engine_factory(surface_faces)
+            self._ref_event = torch.cuda.Event(enable_timing=True)
+            self._ref_event.record()
+            torch.cuda.synchronize()
         self.slots = [_Slot(i, engine_factory(i)) for i in range(int(slots))]
-        self._reserve()
-        self._threads = [threading.Thread(target=self._worker, args=(s,), daemon=True) for s in self.slots]
+        self.mode = "batch" if hasattr(self.slots[0].engine, "run_batch") else "lanes"
+        for s in self.slots:
+            if self.mode == "lanes":
+                s.backend = _CudaLanes(self, s.engine, self.max_rhs) if cuda else s.engine.lanes_backend(self.max_rhs)
+                s.free = list(range(self.max_rhs))
+        target = self._lane_worker if self.mode == "lanes" else self._batch_worker
+        self._threads = [threading.Thread(target=target, args=(s,), daemon=True) for s in self.slots]
         for t in self._threads:
             t.start()
 
@@ -118,15 +252,6 @@ class DCServer:
             return DCEngine(self.mesh.h, bface)
 
         return make
-
-    def _reserve(self):
-        """Reserve each slot's solve workspace and stream up front (bounded device memory)."""
-        for s in self.slots:
-            reserve = getattr(s.engine, "reserve", None)
-            if reserve is not None:
-                reserve(self.max_rhs, self.precision)
-            mk = getattr(s.engine, "make_stream", None)
-            s.stream = mk() if mk is not None else None
 
     # ------------------------------------------------------------ API
     def submit(self, model, survey):
@@ -145,9 +270,9 @@ class DCServer:
                 fut.set_exception(ValueError(f"model has {m.size} entries, the mesh has {self.nC} cells"))
                 return fut
             self._seq += 1
-            req = _Request(m, survey, fut, _model_key(m), nsrc, self._seq)
+            req = _Request(m, survey, fut, _model_key(m), nsrc, self._seq, t_submit=time.perf_counter())
             self._pending.append(req)
-            self._cv.notify()
+            self._cv.notify_all()
         return fut
 
     def close(self, wait=True):
@@ -164,7 +289,101 @@ class DCServer:
     def __exit__(self, *a):
         self.close()
 
-    # ------------------------------------------------------------ scheduling
+    def device_intervals(self):
+        """Per slot, the (start, end) of every refinement sweep on the device in ms since the server
+        started (CUDA events on the slot's stream; lane mode on the GPU)."""
+        out = []
+        for s in self.slots:
+            iv = []
+            for e0, e1 in s.sweep_events:
+                e1.synchronize()
+                iv.append((self._ref_event.elapsed_time(e0), self._ref_event.elapsed_time(e1)))
+            out.append(iv)
+        return out
+
+    # ------------------------------------------------------------ lane scheduling
+    def _lane_admit(self, slot):
+        """Requests admitted into the slot's free lanes now, and the model to set (idle slot)."""
+        with self._lock:
+            while not slot.running and not self._pending and not self._closed:
+                self._cv.wait()
+            if not slot.running and not self._pending:
+                return None, None
+            new_model = None
+            if not slot.running:
+                head = self._pending[0]
+                slot.key = head.key
+                new_model = head.model
+            served = {s.key for s in self.slots if s.key is not None and (s.running or s is slot)}
+            admitted, rest, blocked = [], [], False
+            for r in self._pending:
+                if not blocked and r.key == slot.key and r.nsrc <= len(slot.free):
+                    r.lanes, slot.free = slot.free[:r.nsrc], slot.free[r.nsrc:]
+                    admitted.append(r)
+                    continue
+                rest.append(r)
+                if r.key == slot.key or r.key not in served:
+                    blocked = True  # FIFO: later requests do not overtake this one
+            self._pending = rest
+            for r in admitted:
+                slot.log.append(("admit", r.seq, slot.sweeps, len(slot.running)))
+            slot.running.extend(admitted)
+            return admitted, new_model
+
+    def _release(self, slot, r):
+        with self._lock:
+            slot.running.remove(r)
+            slot.free = sorted(slot.free + r.lanes)
+            if not slot.running:
+                slot.key = None
+            self._cv.notify_all()
+
+    def _lane_worker(self, slot):
+        be = slot.backend
+        while True:
+            admitted, new_model = self._lane_admit(slot)
+            if admitted is None:
+                return
+            if new_model is not None:
+                try:
+                    be.set_model(new_model)
+                except Exception as exc:
+                    for r in admitted:
+                        r.future.set_exception(exc)
+                        self._release(slot, r)
+                    continue
+            for r in admitted:
+                try:
+                    r.state = be.prepare(r)
+                    be.load(r.lanes, r)
+                except Exception as exc:  # this request only (e.g. electrodes outside the mesh)
+                    r.future.set_exception(exc)
+                    self._release(slot, r)
+            if not slot.running:
+                continue
+            (n_active, _), evs = be.sweep()
+            slot.sweeps += 1
+            if evs is not None:
+                slot.sweep_events.append(evs)
+            slot.log.append(("sweep", None, slot.sweeps, len(slot.running)))
+            act = be.active()
+            for r in list(slot.running):
+                r.sweeps += 1
+                if not np.any(act[r.lanes]):
+                    try:
+                        r.future.set_result(be.finish(r.lanes, r))
+                    except Exception as exc:
+                        r.future.set_exception(exc)
+                    slot.log.append(("done", r.seq, slot.sweeps, len(slot.running)))
+                    slot.served += 1
+                    self._release(slot, r)
+                elif r.sweeps >= self.max_sweeps:
+                    be.clear(r.lanes)
+                    r.future.set_exception(NotConvergedError(
+                        f"request {r.seq} did not reach rtol {self.rtol:g} in {r.sweeps} refinement sweeps"))
+                    self._release(slot, r)
+
+    # ------------------------------------------------------------ batch scheduling (run_batch engines)
     def _take_batch(self):
         """Oldest pending request plus queued requests with the same model, up to max_rhs sources."""
         with self._lock:
@@ -184,73 +403,19 @@ class DCServer:
             self._pending = rest
             return batch
 
-    def _worker(self, slot):
+    def _batch_worker(self, slot):
         while True:
             batch = self._take_batch()
             if batch is None:
                 return
-            slot.busy = True
             try:
-                self._run(slot, batch)
+                outs = slot.engine.run_batch([r.model for r in batch], [r.survey for r in batch])
+                for r, d in zip(batch, outs):
+                    r.future.set_result(d)
             except Exception as exc:  # a failure belongs to the requests of this batch only
                 for r in batch:
                     if not r.future.done():
                         r.future.set_exception(exc)
             finally:
-                slot.busy = False
                 slot.served += len(batch)
                 slot.batches.append([r.seq for r in batch])
-
-    def _run(self, slot, batch):
-        eng = slot.engine
-        run = getattr(eng, "run_batch", None)
-        if run is not None:  # fake engines used by the CPU tests
-            outs = run([r.model for r in batch], [r.survey for r in batch])
-            for r, d in zip(batch, outs):
-                r.future.set_result(d)
-            return
-        self._run_cuda(slot, batch)
-
-    def _run_cuda(self, slot, batch):
-        import torch
-
-        from .engine import csr_spmv, fill_sparse
-        from .resistivity.electrodes import SurveyTables
-
-        m = batch[0].model
-        sigma = self.sigma_map * m
-        if np.any(~np.isfinite(sigma)) or np.any(sigma <= 0):
-            raise ValueError("conductivity must be positive and finite")
-        # validate every request's electrodes on its own, so one bad survey
-        # fails only its own future, not the requests it was merged with
-        ok = []
-        for r in batch:
-            try:
-                SurveyTables(self.mesh, r.survey.source_list, self.nN)
-                ok.append(r)
-            except Exception as exc:
-                r.future.set_exception(exc)
-        batch = ok
-        if not batch:
-            return
-        dev = torch.device("cuda", torch.cuda.current_device() if self._device is None else self._device)
-        stream = slot.stream if slot.stream is not None else torch.cuda.current_stream(dev)
-        src_all = []
-        for r in batch:
-            src_all.extend(r.survey.source_list)
-        tables = SurveyTables(self.mesh, src_all, self.nN)
-        with torch.cuda.stream(stream):
-            sig = torch.from_numpy(np.ascontiguousarray(sigma)).to(dev, non_blocking=False)
-            slot.engine.set_model(sig)
-            Q = torch.zeros(len(src_all), self.nN, dtype=torch.float64, device=dev)
-            fill_sparse(torch.from_numpy(tables.q_idx).to(dev), torch.from_numpy(tables.q_val).to(dev), Q.view(-1))
-            U, info = slot.engine.solve(Q, mode=self.precision, rtol=self.rtol)
-            d = torch.empty(tables.nD, dtype=torch.float64, device=dev)
-            csr_spmv(torch.from_numpy(tables.P_ptr).to(dev), torch.from_numpy(tables.P_idx).to(dev),
-                     torch.from_numpy(tables.P_w).to(dev), U.view(-1), d)
-            out = d.cpu().numpy()
-        start = 0
-        for r in batch:
-            nd = sum(rx.nD for s in r.survey.source_list for rx in s.receiver_list)
-            r.future.set_result(out[start:start + nd].copy())
-            start += nd

@@ -1,8 +1,14 @@
-"""The DC server on the GPU: each request's result is the same alone and in
-the mix (concurrent slots, same-model requests merged into one solve).
+"""The DC server on the GPU (continuous batching over lane sessions).
 
-Tolerance: solves run to rtol 1e-10, so alone and mixed results agree to
-1e-8 relative; one request is also checked against the CPU oracle (1e-6)."""
+Each request's result is the same alone and in the mix (its lanes iterate independently of the
+others'), requests join a solve that is already running, the slots' sweeps overlap on the device,
+the device memory does not grow with the number of requests served, and a bad request fails alone.
+
+Tolerance: solves run to rtol 1e-10; alone and mixed results agree to 1e-12 relative (the lane
+arithmetic does not depend on the other lanes); one request is checked against the CPU oracle
+(1e-6)."""
+
+import time
 
 import numpy as np
 import pytest
@@ -34,28 +40,61 @@ def _setup():
         return Survey(srcs)
 
     reqs = [(models[0], survey(0, 3)), (models[1], survey(1, 5)), (models[0], survey(2, 2)),
-            (models[2], survey(3, 4)), (models[1], survey(4, 1)), (models[2], survey(5, 6))]
+            (models[2], survey(3, 4)), (models[1], survey(4, 1)), (models[2], survey(5, 6)),
+            (models[0], survey(1, 4)), (models[1], survey(3, 2))]
     return mesh, reqs
 
 
-def test_alone_equals_mixed(cuda):
+def test_continuous_batching(cuda):
     mesh, reqs = _setup()
     alone = []
     with DCServer(mesh, slots=1, max_rhs=16, rtol=1e-10) as srv:
         for m, sv in reqs:
             alone.append(srv.submit(m, sv).result(timeout=120))
-    with DCServer(mesh, slots=3, max_rhs=16, rtol=1e-10) as srv:
-        futs = [srv.submit(m, sv) for m, sv in reqs]
+    with DCServer(mesh, slots=2, max_rhs=16, rtol=1e-10) as srv:
+        futs = [srv.submit(m, sv) for m, sv in reqs[:6]]
+        # two more requests arrive while the first ones are on the device
+        while min(s.sweeps for s in srv.slots) < 1:
+            time.sleep(0.0005)
+        futs += [srv.submit(m, sv) for m, sv in reqs[6:]]
         mixed = [f.result(timeout=120) for f in futs]
-        merged = [b for s in srv.slots for b in s.batches if len(b) > 1]
+        intervals = srv.device_intervals()
+        logs = [s.log for s in srv.slots]
     for a, b in zip(alone, mixed):
-        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-8
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-12
     m, sv = reqs[3]
     orc = OracleDC3DNodal(mesh, sv, sigma_map=maps.ExpMap(mesh))
     orc.set_model(m)
     d0 = orc.dpred()
     assert np.linalg.norm(mixed[3] - d0) / np.linalg.norm(d0) < 1e-6
-    assert isinstance(merged, list)
+    # requests were admitted into solves that were already running (between two sweeps)
+    joined = [(seq, sweep) for lg in logs for ev, seq, sweep, running in lg if ev == "admit" and running > 0]
+    assert joined, logs
+    # a sweep advanced the lanes of more than one request
+    assert max(running for lg in logs for ev, _, _, running in lg if ev == "sweep") > 1
+    # the two slots' sweeps overlapped on the device
+    a_iv, b_iv = intervals
+    assert any(a0 < b1 and b0 < a1 for a0, a1 in a_iv for b0, b1 in b_iv)
+
+
+def test_memory_bounded(cuda):
+    """Serving more requests does not grow the device memory beyond what the slots reserved at start
+    (lane workspaces, staging arrays) plus the requests' electrode tables."""
+    import torch
+
+    mesh, reqs = _setup()
+    with DCServer(mesh, slots=2, max_rhs=16, rtol=1e-10) as srv:
+        for f in [srv.submit(m, sv) for m, sv in reqs]:
+            f.result(timeout=120)
+        torch.cuda.synchronize()
+        base = torch.cuda.memory_allocated()
+        torch.cuda.reset_peak_memory_stats()
+        for _ in range(3):
+            for f in [srv.submit(m, sv) for m, sv in reqs]:
+                f.result(timeout=120)
+        torch.cuda.synchronize()
+        peak = torch.cuda.max_memory_allocated()
+    assert peak - base < 4 << 20, (peak - base)
 
 
 def test_bad_request_does_not_poison_others(cuda):

@@ -87,3 +87,107 @@ def test_failure_is_isolated_and_slots_overlap():
     for i, o in enumerate(out):
         np.testing.assert_array_equal(o, [64.0 * i] * 2)
     assert len({tid for tid, _ in log}) > 1  # more than one slot worked concurrently
+
+
+# ---------------------------------------------------------------- lane scheduling (continuous batching)
+class FakeLanes:
+    """Lane backend: a lane of request r converges after r.nsrc + 1 sweeps; the datum value of source
+    i is sum(model) + i.  NaN models fail in set_model; a request with 'diverge' never converges."""
+
+    def __init__(self, capacity, delay=0.005):
+        self.capacity = capacity
+        self.left = np.zeros(capacity, dtype=int)
+        self.val = np.zeros(capacity)
+        self.delay = delay
+        self.model = None
+
+    def set_model(self, m):
+        if np.any(~np.isfinite(m)):
+            raise ValueError("conductivity must be positive and finite")
+        self.model = m
+
+    def prepare(self, r):
+        return None
+
+    def load(self, lanes, r):
+        for i, l in enumerate(lanes):
+            self.left[l] = 10 ** 6 if getattr(r.survey, "diverge", False) else r.nsrc + 1
+            self.val[l] = self.model.sum() + i
+
+    def clear(self, lanes):
+        self.left[lanes] = 0
+
+    def sweep(self):
+        time.sleep(self.delay)
+        self.left[self.left > 0] -= 1
+        return (int((self.left > 0).sum()), 1), None
+
+    def active(self):
+        return (self.left > 0).astype(np.int32)
+
+    def finish(self, lanes, r):
+        vals = []
+        for i, s in enumerate(r.survey.source_list):
+            for rx in s.receiver_list:
+                vals.extend([self.val[lanes[i]]] * rx.nD)
+        return np.array(vals)
+
+
+class FakeLaneEngine:
+    def lanes_backend(self, capacity):
+        return FakeLanes(capacity)
+
+
+def _admits(srv):
+    return [(seq, sweep, running) for s in srv.slots for ev, seq, sweep, running in s.log if ev == "admit"]
+
+
+def test_lanes_admit_into_running_solve_and_route_results():
+    mesh = _mesh()
+    m1 = np.zeros(mesh.n_cells)
+    with DCServer(mesh, slots=1, max_rhs=8, engine_factory=lambda i: FakeLaneEngine()) as srv:
+        a = srv.submit(m1, _survey(4))          # 5 sweeps
+        while srv.slots[0].sweeps < 2:
+            time.sleep(0.001)
+        b = srv.submit(m1, _survey(2))          # joins the running solve
+        ra, rb = a.result(timeout=10), b.result(timeout=10)
+    np.testing.assert_array_equal(ra, [0, 0, 1, 1, 2, 2, 3, 3])
+    np.testing.assert_array_equal(rb, [0, 0, 1, 1])
+    adm = {seq: (sweep, running) for seq, sweep, running in _admits(srv)}
+    assert adm[1] == (0, 0)
+    assert adm[2][0] >= 2 and adm[2][1] == 1  # admitted between sweeps, next to a running request
+
+
+def test_lanes_fifo_no_overtaking():
+    """With one slot running model 1, a model-2 request that has nowhere to go is not overtaken by a
+    later model-1 request; a model-1 request that does not fit the free lanes is not overtaken either."""
+    mesh = _mesh()
+    m1, m2 = np.zeros(mesh.n_cells), np.ones(mesh.n_cells)
+    with DCServer(mesh, slots=1, max_rhs=4, engine_factory=lambda i: FakeLaneEngine()) as srv:
+        a = srv.submit(m1, _survey(3))
+        while srv.slots[0].sweeps < 1:
+            time.sleep(0.001)
+        c = srv.submit(m2, _survey(1))
+        d = srv.submit(m1, _survey(1))
+        for f in (a, c, d):
+            f.result(timeout=10)
+    order = [seq for seq, _, _ in sorted(_admits(srv), key=lambda x: (x[1], x[0]))]
+    assert order.index(2) < order.index(3)
+
+
+def test_lanes_failures_are_isolated():
+    mesh = _mesh()
+    sv_bad = _survey(1)
+    sv_bad.diverge = True
+    with DCServer(mesh, slots=2, max_rhs=8, max_sweeps=6, engine_factory=lambda i: FakeLaneEngine()) as srv:
+        nan = srv.submit(np.full(mesh.n_cells, np.nan), _survey(1))
+        stuck = srv.submit(np.zeros(mesh.n_cells), sv_bad)
+        good = [srv.submit(np.full(mesh.n_cells, float(i)), _survey(2)) for i in range(3)]
+        with pytest.raises(ValueError):
+            nan.result(timeout=10)
+        from simpeg_gb300.serving import NotConvergedError
+
+        with pytest.raises(NotConvergedError):
+            stuck.result(timeout=10)
+        for i, g in enumerate(good):
+            np.testing.assert_array_equal(g.result(timeout=10), [64.0 * i] * 2 + [64.0 * i + 1] * 2)
