@@ -288,3 +288,239 @@ class _Diag:
 
     def diagonal(self):
         return self._w
+
+
+# ---------------------------------------------------------------- the minimiser
+class BaseInvProblem:
+    """``phi(m) = phi_d(m) + beta phi_m(m)`` and its derivatives on the device
+    (``simpeg/inverse_problem.py`` ``BaseInvProblem.evalFunction``): the gradient as a device
+    tensor and the Gauss-Newton Hessian as a callable on device vectors (one batched Jvec and one
+    batched Jtvec per product)."""
+
+    def __init__(self, dmisfit, reg, beta=1.0):
+        self.dmisfit = dmisfit
+        self.reg = reg
+        self.beta = float(beta)
+        self.phi_d = self.phi_m = None
+
+    def evalFunction(self, m, return_g=True, return_H=True):
+        m = np.asarray(m, dtype=np.float64)
+        self.phi_d = self.dmisfit(m)
+        self.phi_m = self.reg(m)
+        f = self.phi_d + self.beta * self.phi_m
+        if not return_g and not return_H:
+            return f
+        out = (f,)
+        if return_g:
+            m_dev = torch.as_tensor(m, device=self.dmisfit.simulation.device)
+            out += (self.dmisfit.deriv_dev(m) + self.beta * self.reg.deriv_dev(m_dev),)
+        if return_H:
+            beta, dmis, reg = self.beta, self.dmisfit, self.reg
+            out += (lambda v: dmis.deriv2_dev(m, v) + beta * reg.deriv2_dev(v),)
+        return out
+
+
+def jacobi_preconditioner(dmisfit, reg, beta, m):
+    """``diag(1 / (getJtJdiag(m, W) + beta diag(reg.deriv2)))`` as a callable on device vectors: the
+    preconditioner the ``UpdatePreconditioner`` directive sets (``directives/_directives.py:2180-2260``)."""
+    sim = dmisfit.simulation
+    dev = sim.device
+    jtj = torch.as_tensor(sim.getJtJdiag(m, W=_Diag(dmisfit.W)), device=dev)
+    dA = jtj + beta * reg.diag_deriv2()
+    Minv = torch.where(dA != 0, 1.0 / dA, torch.zeros_like(dA))
+    return lambda v: Minv * v
+
+
+class InexactGaussNewton:
+    """The reference's ``InexactGaussNewton`` (``simpeg/optimization.py:1345-1415``) with the loop of
+    ``Minimize.minimize`` (``:462-530``), its Armijo backtracking line search (``:724-783``), its
+    stopping criteria (``tolerance_f``, ``moving_x``, ``tolerance_g`` all met, or ``norm_g`` or
+    ``iteration``; in the line search ``armijoGoldstein`` or ``iterationLS``), the ``BFGS``
+    preconditioner kept from the iterates (``:1265-1331``, identity ``bfgsH0``) unless ``approxHinv``
+    is given, and ``Remember`` (``:853-907``).  Models are host arrays; gradients, search directions
+    and the CG vectors of ``H p = -g`` live on the device.
+
+    ``evalFunction(x, return_g, return_H)`` returns ``f`` or ``(f, g, H)`` with g a device tensor and
+    H a callable on device vectors (:class:`BaseInvProblem`)."""
+
+    name = "Inexact Gauss Newton"
+
+    def __init__(self, *, maxIter=20, maxIterLS=10, maxStep=np.inf, LSreduction=1e-4, LSshorten=0.5, tolF=1e-1,
+                 tolX=1e-1, tolG=1e-1, eps=1e-5, require_decrease=True, cg_rtol=1e-1, cg_atol=0.0, cg_maxiter=5,
+                 nbfgs=10, approxHinv=None, callback=None):
+        self.maxIter, self.maxIterLS, self.maxStep = maxIter, maxIterLS, maxStep
+        self.LSreduction, self.LSshorten = LSreduction, LSshorten
+        self.tolF, self.tolX, self.tolG, self.eps = tolF, tolX, tolG, eps
+        self.require_decrease = require_decrease
+        self.cg_rtol, self.cg_atol, self.cg_maxiter = cg_rtol, cg_atol, cg_maxiter
+        self.nbfgs = nbfgs
+        self.approxHinv = approxHinv
+        self.callback = callback
+        self._rememberThese = ()
+        self.stopNextIteration = False
+
+    # ---------------------------------------------------------- Remember
+    def remember(self, *args):
+        self._rememberThese = args
+
+    def recall(self, param):
+        if param not in self._rememberList:
+            raise KeyError(f"{param!r} was not remembered: name it in remember() first")
+        return self._rememberList[param]
+
+    def _remember_now(self):
+        for p in self._rememberThese:
+            if isinstance(p, str):
+                self._rememberList[p].append(getattr(self, p, None))
+            else:
+                self._rememberList[p[0]].append(p[1](self))
+
+    # ---------------------------------------------------------- stoppers
+    @staticmethod
+    def _norm(v):
+        return float(torch.linalg.vector_norm(v)) if isinstance(v, torch.Tensor) else float(np.linalg.norm(v))
+
+    def _stop(self):
+        if self.iter == 0:
+            self.f0 = self.f
+        gn = self._norm(self.g)
+        optimal = [
+            self.iter != 0 and abs(self.f - self.f_last) <= self.tolF * (1 + abs(self.f0)),
+            self.iter != 0 and np.linalg.norm(self.xc - self.x_last) <= self.tolX * (1 + np.linalg.norm(self.x0)),
+            gn <= self.tolG,
+        ]
+        critical = [gn <= 1e3 * self.eps, self.maxIter <= self.iter]
+        self.stopped_by = ("optimal" if all(optimal) else "norm_g" if critical[0] else
+                           "iteration" if critical[1] else None)
+        return all(optimal) or any(critical)
+
+    def _stop_ls(self):
+        return self._LS_ft <= self.f + self.LSreduction * self._LS_descent or self.maxIterLS <= self.iterLS
+
+    # ---------------------------------------------------------- BFGS
+    def _bfgs(self, d):
+        n = self._bfgscnt
+        nn = ktop = min(self.nbfgs, n)
+        return self._bfgsrec(ktop, n, nn, d)
+
+    def _bfgsrec(self, k, n, nn, d):
+        if k < 0:
+            return d  # identity bfgsH0
+        khat = 0 if nn == 0 else (n - nn + k) % nn
+        S, Y = self._S[khat], self._Y[khat]
+        ys = float((Y * S).sum())
+        gamma = float((S * d).sum()) / ys
+        d = d - gamma * Y
+        d = self._bfgsrec(k - 1, n, nn, d)
+        return d + (gamma - float((Y * d).sum()) / ys) * S
+
+    def _end_iteration_bfgs(self, xt):
+        if not self._was_default_hinv:
+            return
+        if self.iter == 0:
+            self.g_last = self.g
+            return
+        yy = self.g - self.g_last
+        ss = torch.as_tensor(self.xc - xt, device=self.g.device)
+        self.g_last = self.g
+        if float((yy * ss).sum()) > 0:
+            self._bfgscnt += 1
+            ktop = self._bfgscnt % self.nbfgs
+            self._Y[ktop] = yy
+            self._S[ktop] = ss
+            self.comment = ""
+        else:
+            self.comment = "Skip BFGS"
+
+    # ---------------------------------------------------------- search direction
+    def findSearchDirection(self):
+        """CG on ``H p = -g`` from p = 0 with ``approxHinv`` (BFGS by default) as the preconditioner,
+        stopped at ``|r| <= max(cg_rtol |g|, cg_atol)`` or after ``cg_maxiter`` iterations."""
+        self._was_default_hinv = self.approxHinv is None
+        M = self._bfgs if self.approxHinv is None else self.approxHinv
+        b = -self.g
+        x = torch.zeros_like(b)
+        r = b.clone()
+        tol = max(self.cg_rtol * self._norm(b), self.cg_atol)
+        z = M(r)
+        p = z.clone()
+        rz = float((r * z).sum())
+        self.cg_iterations = 0
+        for _ in range(self.cg_maxiter):
+            if self._norm(r) <= tol:
+                break
+            q = self.H(p)
+            alpha = rz / float((p * q).sum())
+            x = x + alpha * p
+            r = r - alpha * q
+            self.cg_iterations += 1
+            if self._norm(r) <= tol:
+                break
+            z = M(r)
+            rz_new = float((r * z).sum())
+            p = z + (rz_new / rz) * p
+            rz = rz_new
+        return x
+
+    def scaleSearchDirection(self, p):
+        pmax = float(p.max())
+        if self.maxStep < abs(pmax):
+            p = self.maxStep * p / abs(pmax)
+        return p
+
+    def modifySearchDirection(self, p):
+        """Armijo backtracking: t = 1, 1/2, ... until f(x + t p) <= f + LSreduction g.(x_t - x)."""
+        p_host = p.cpu().numpy()
+        g_host = self.g.cpu().numpy()
+        self._LS_t = 1.0
+        self.iterLS = 0
+        while self.iterLS < self.maxIterLS:
+            self._LS_xt = self.xc + self._LS_t * p_host
+            self._LS_ft = self.evalFunction(self._LS_xt, return_g=False, return_H=False)
+            self._LS_descent = float(np.inner(g_host, self._LS_xt - self.xc))
+            if self._stop_ls():
+                break
+            self.iterLS += 1
+            self._LS_t = self.LSshorten * self._LS_t
+        return self._LS_xt, self.iterLS < self.maxIterLS
+
+    # ---------------------------------------------------------- the loop
+    def minimize(self, evalFunction, x0):
+        self.evalFunction = evalFunction
+        x0 = np.asarray(x0, dtype=np.float64)
+        if np.any(np.isnan(x0)):
+            raise ValueError("x0 has a nan.")
+        self.iter = self.iterLS = 0
+        self.stopNextIteration = False
+        self.x0 = self.xc = self.x_last = x0
+        self.f_last = np.nan
+        self._rememberList = {(p if isinstance(p, str) else p[0]): [] for p in self._rememberThese}
+        self._bfgscnt = -1
+        self._S = [None] * self.nbfgs
+        self._Y = [None] * self.nbfgs
+        self._was_default_hinv = self.approxHinv is None
+        self.comment = ""
+        self.f = evalFunction(self.xc, return_g=False, return_H=False)
+        while True:
+            self.f, self.g, self.H = evalFunction(self.xc, return_g=True, return_H=True)
+            if self._stop():
+                break
+            self.searchDirection = self.findSearchDirection()
+            del self.H
+            p = self.scaleSearchDirection(self.searchDirection)
+            xt, passLS = self.modifySearchDirection(p)
+            if not passLS and self.require_decrease:
+                self.stopped_by = "line search"
+                return self.xc
+            # end of the iteration: the hooks first (BFGS pair, remembered values), then the shuffle
+            self._end_iteration_bfgs(xt)
+            self._remember_now()
+            self.f_last = self.f
+            self.f = self._LS_ft
+            self.x_last, self.xc = self.xc, xt
+            self.iter += 1
+            if self.callback is not None:
+                self.callback(xt)
+            if self.stopNextIteration:
+                break
+        return self.xc

@@ -67,3 +67,33 @@ def test_gauss_newton_direction_matches_oracle(cuda):
     assert rel(info["g"].cpu().numpy(), g0) < 1e-6
     assert rel(info["jtj_diag"].cpu().numpy(), jtj0) < 1e-6
     assert rel(p.cpu().numpy(), p0) < 1e-6
+
+
+def test_inexact_gauss_newton_minimiser(cuda):
+    """The minimiser on the DC problem: with the UpdatePreconditioner Jacobi and 10 CG iterations its
+    first search direction is the Gauss-Newton direction above, and three iterations with the Armijo
+    line search decrease phi = phi_d + beta phi_m at every step."""
+    from simpeg_gb300.inversion import (BaseInvProblem, InexactGaussNewton, L2DataMisfit, WeightedLeastSquares,
+                                        inexact_gauss_newton_direction, jacobi_preconditioner)
+
+    mesh, survey, m_true, m0, rng = _case()
+    orc = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh))
+    orc.set_model(m_true)
+    dobs = orc.dpred()
+    W = 1.0 / (0.05 * np.abs(dobs) + 1e-6)
+    beta = 1e-2
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), rtol=1e-11)
+    dmis = L2DataMisfit(sim, dobs, W=W)
+    reg = WeightedLeastSquares(mesh, sim)
+    p_ref, _ = inexact_gauss_newton_direction(dmis, reg, beta, m0, cg_maxiter=10)
+    prob = BaseInvProblem(dmis, reg, beta)
+    opt = InexactGaussNewton(maxIter=1, cg_maxiter=10, cg_rtol=0.0,
+                             approxHinv=jacobi_preconditioner(dmis, reg, beta, m0))
+    opt.minimize(prob.evalFunction, m0)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(opt.searchDirection.cpu().numpy(), p_ref.cpu().numpy()) < 1e-10
+    opt = InexactGaussNewton(maxIter=3, cg_maxiter=5, approxHinv=jacobi_preconditioner(dmis, reg, beta, m0))
+    opt.remember("f")
+    m = opt.minimize(prob.evalFunction, m0)
+    f = opt.recall("f") + [prob.evalFunction(m, return_g=False, return_H=False)]
+    assert all(b < a for a, b in zip(f, f[1:])), f
