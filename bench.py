@@ -862,11 +862,13 @@ def run_batched(args):
     for p in bf.problems:
         p.engine.stencil_timing(True)
     torch.cuda.synchronize()
+    n_seq0 = kernel_launches()
     e0.record()
     for p in bf.problems:
         p.engine.solve(p.Q, mode="mixed", rtol=RTOL, ws=p.ws)
     e1.record()
     torch.cuda.synchronize()
+    seq_launches = kernel_launches() - n_seq0
     ms_seq = e0.elapsed_time(e1)
     tot = [0.0, 0, 0.0]
     for p in bf.problems:
@@ -889,7 +891,12 @@ def run_batched(args):
                       "nodes_range": [min(p[0].n_nodes for p in probs), max(p[0].n_nodes for p in probs)],
                       "rtol": RTOL, "l2": "inputs larger than L2 (all problems' vectors, ~2 GB)"},
            "autotune": {"kb": sorted({t["kb"] for t in tunes if t}), "nu": sorted({t["nu"] for t in tunes if t})},
-           "clocks": clk.summary(), "gpu_launches": launches,
+           "clocks": clk.summary(),
+           # a graph launch replays the problems' kernels without passing the host launch counter; the
+           # graph runs every solve as far as the host-driven solver does (same iterations), whose
+           # kernel launches are counted in the sequential pass
+           "gpu_launches": seq_launches * args.steps, "graph_launches": args.steps,
+           "host_counted_launches_in_timed_region": launches,
            "roofline": _stencil_roofline(*tot, what="fine-level Chebyshev steps of every problem, timed in the "
                                                     "sequential pass (events cannot bracket single kernels inside "
                                                     "the graph)"),

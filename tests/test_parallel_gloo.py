@@ -90,7 +90,8 @@ def _run_two_ranks(gpu):
     assert sorted(n for _, _, n in out) == [2, 3]
     for rank, errs, _ in out:
         for k, e in errs.items():
-            assert e < (1e-8 if gpu else 1e-9), (rank, k, e)
+            # GPU children: solves to 1e-12, getJtJdiag with fp32 cell arithmetic (1e-6 of the oracle)
+            assert e < ((1e-6 if k == "jtj" else 1e-8) if gpu else 1e-9), (rank, k, e)
 
 
 def test_sharded_simulation_two_ranks():
