@@ -556,7 +556,7 @@ def _peak_hbm():
     return 6800.0, "fallback"
 
 
-def _stencil_roofline(ms, n, alg_bytes, kinds=None, what="fine-level Chebyshev steps"):
+def _stencil_roofline(ms, n, alg_bytes, kinds=None, what="fine-level Chebyshev steps", scaled_traffic=False):
     """Roofline of the fine-level Chebyshev steps timed with CUDA events inside a timed region."""
     if not n:
         return None
@@ -568,6 +568,17 @@ def _stencil_roofline(ms, n, alg_bytes, kinds=None, what="fine-level Chebyshev s
     if kinds:
         out["by_kind"] = {k: {"launches": c, "us_per_launch": t / c * 1e3, "achieved": b / (t * 1e-3) / 1e9,
                               "frac": b / (t * 1e-3) / 1e9 / peak} for k, (c, t, b) in kinds.items()}
+        if scaled_traffic:
+            # DRAM bytes over algorithmic bytes of each kind in the profiled 1M-node, 256-RHS solve (fp16 lanes:
+            # 8 B per node-RHS with the momentum term, 6 B without, plus 20 B per node), applied to this run's
+            # algorithmic bytes of that kind
+            tbk = _traffic_by_kind()
+            if all(k in tbk for k in kinds):
+                alg_nr = {k: ((8.0 if k.startswith("momentum") else 6.0) * 256 + 20.0) / 256 for k in kinds}
+                out["traffic"] = sum(b * tbk[k] / alg_nr[k] for k, (_, _, b) in kinds.items()) / n
+                out["traffic_source"] = ("ncu DRAM bytes / algorithmic bytes of each kind of step in the profiled "
+                                         "1M-node 256-RHS solve (profiles/cheb_step_fp16_dc3d.md), times this run's "
+                                         "algorithmic bytes of that kind")
     return out
 
 
@@ -665,7 +676,7 @@ def run_differentiation(args):
             out["ms_per_step"] = t_dev * 1e3
             out["clocks"] = clk.summary()
             out["gpu_launches"] = launches
-            out["roofline"] = _stencil_roofline(*st, kinds)
+            out["roofline"] = _stencil_roofline(*st, kinds, scaled_traffic=True)
             out["e2e"] = {"value": 1.0 / t_e2e, "unit": "gradients/s",
                           "h2d_bytes_per_step": int(m.size * 8 + 2 * survey.nD * 8),
                           "d2h_bytes_per_step": int(m.size * 8 + survey.nD * 8),
@@ -770,7 +781,7 @@ def run_gauss_newton(args):
             out["ms_per_step"] = dt * 1e3
             out["clocks"] = clk.summary()
             out["gpu_launches"] = launches
-            out["roofline"] = _stencil_roofline(*st, kinds)
+            out["roofline"] = _stencil_roofline(*st, kinds, scaled_traffic=True)
             out["e2e"] = {"value": 1.0 / dt_e2e, "unit": "Gauss-Newton steps/s",
                           "h2d_bytes_per_step": int(m0.size * 8), "d2h_bytes_per_step": int(m0.size * 8),
                           "path": "inexact_gauss_newton_direction(dmis, reg, beta, m) from a host model; the "

@@ -109,9 +109,10 @@ int dc_set_smoother(dc_handle *h, int kind);
  * asynchronous copies (slabs of node rows marched through the z planes),
  * 0 (default) uses the direct-load kernel; a value 10 * rows + depth
  * (12, 13, 22, 23) forces the slab height and copy depth.  Same arithmetic
- * either way.  Measured on the 1M-node, 256-RHS solve: 182 ms staged (best
- * layout) vs 164 ms direct, the per-plane CTA barrier of the slab march
- * costing more than the latency it hides. */
+ * either way.  Measured on the 1M-node, 256-RHS forward solve: 102 ms staged
+ * (best layout: two-row slabs, copy depth 2; 114 ms automatic) vs 85 ms
+ * direct, the per-plane CTA barrier of the slab march costing more than the
+ * latency it hides. */
 int dc_set_staging(dc_handle *h, int enable);
 
 /* Number of multigrid levels and nodes of level `lvl`. */

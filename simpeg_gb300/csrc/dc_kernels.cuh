@@ -35,22 +35,6 @@ namespace {
 
 constexpr int TPB = 256;
 
-// Minimum resident blocks per SM requested from the compiler (0 = no request)
-// for a Chebyshev step with fp32 arithmetic on 16-bit storage (and a 16-bit
-// right-hand side, as on the finest level).  Left to itself
-// the compiler gives the second step of a zero-start sequence (PREV = 2) 53
-// registers: 4 blocks of TPB per SM instead of 5, fewer loads in flight for a
-// kernel bound by load latency (5 blocks: 48 registers, no spill, 466 -> 440
-// us per finest-level launch at 1M nodes x 256 RHS).  The step without
-// momentum (PREV = 0) spills at 5 blocks and measured slower (396 -> 428 us),
-// the PCG apply with p.q partials did not change (403 -> 400 us at 4 blocks);
-// both are left to the compiler.
-template <typename T, typename S>
-constexpr int stencil_min_blocks(int want) {
-  return (sizeof(T) == 4 && sizeof(S) == 2) ? want : 0;
-}
-
-
 // floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
 __device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
   if (d == 1) return n;
@@ -135,19 +119,51 @@ __device__ __forceinline__ float2 pair(const Vec<float, W> &v, int p) {
   return make_float2(v.a[2 * p], v.a[2 * p + 1]);
 }
 __device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
-// The seven-point stencil at element t of node n = (i, j, k), x stored as S:
-// acc0 + sign * (A x) for the W lanes, with sign = +1 and acc0 = 0 (A x) or
-// sign = -1 and acc0 = r (r - A x, the smoothers' residual in one chain of
-// fused multiply-adds).  Branch-free: all seven loads are issued
+// Seven-point stencil arithmetic for W lanes: d v0 - sum of c* times the six
+// neighbours, in this fixed order.  With PACK (fp32) lane pairs go through
+// Blackwell's two-lane FMA: one instruction per pair and coupling, each lane
+// rounded as the scalar FMA rounds it.
+template <typename T, int W, bool PACK>
+__device__ __forceinline__ Vec<T, W> stencil_terms(T cd, T cxp, T cxm, T cyp, T cym, T czp, T czm,
+                                                    const Vec<T, W> &v0, const Vec<T, W> &vxp, const Vec<T, W> &vxm,
+                                                    const Vec<T, W> &vyp, const Vec<T, W> &vym, const Vec<T, W> &vzp,
+                                                    const Vec<T, W> &vzm) {
+  Vec<T, W> acc;
+  if constexpr (PACK && std::is_same<T, float>::value && W % 2 == 0) {
+    // couplings enter negated so that every term is one FMA
+    const float2 kd = dup2(cd), kxp = dup2(-cxp), kxm = dup2(-cxm), kyp = dup2(-cyp), kym = dup2(-cym),
+                 kzp = dup2(-czp), kzm = dup2(-czm);
+#pragma unroll
+    for (int p = 0; p < W / 2; ++p) {
+      float2 a = __fmul2_rn(kd, pair(v0, p));
+      a = __ffma2_rn(kxp, pair(vxp, p), a);
+      a = __ffma2_rn(kxm, pair(vxm, p), a);
+      a = __ffma2_rn(kyp, pair(vyp, p), a);
+      a = __ffma2_rn(kym, pair(vym, p), a);
+      a = __ffma2_rn(kzp, pair(vzp, p), a);
+      a = __ffma2_rn(kzm, pair(vzm, p), a);
+      acc.a[2 * p] = a.x;
+      acc.a[2 * p + 1] = a.y;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < W; ++e)
+      acc.a[e] = cd * v0.a[e] - cxp * vxp.a[e] - cxm * vxm.a[e] - cyp * vyp.a[e] - cym * vym.a[e] -
+                 czp * vzp.a[e] - czm * vzm.a[e];
+  }
+  return acc;
+}
+
+// The seven-point stencil (A x) at element t of node n = (i, j, k) for the W
+// lanes, x stored as S.  Branch-free: all seven loads are issued
 // unconditionally (off-mesh neighbours are redirected to the node itself and
 // get weight 0; c* is zero on the last node of its axis), so they are all in
 // flight at once.
-template <typename T, int KB, int W, typename S, bool SUB, bool PACK = true>
-__device__ __forceinline__ Vec<T, W> stencil_core(const typename CoefT<T>::type *__restrict__ coef,
-                                                   const S *__restrict__ x, long long t, int n, int i, int j, int k,
-                                                   const Dims &d, const Vec<T, W> *acc0) {
+template <typename T, int KB, int W, typename S, bool PACK = true>
+__device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *__restrict__ coef,
+                                                  const S *__restrict__ x, long long t, int n, int i, int j, int k,
+                                                  const Dims &d) {
   const int sxn = 1, syn = d.Nx, szn = d.Nx * d.Ny;
   const bool hx = i > 0, hy = j > 0, hz = k > 0;
   const bool px = i + 1 < d.Nx, py = j + 1 < d.Ny, pz = k + 1 < d.Nz;
@@ -160,51 +176,8 @@ __device__ __forceinline__ Vec<T, W> stencil_core(const typename CoefT<T>::type 
   const Vec<T, W> vym = ld<T, W>(x + t - (hy ? (long long)syn * KB : 0));
   const Vec<T, W> vzp = ld<T, W>(x + t + (pz ? (long long)szn * KB : 0));
   const Vec<T, W> vzm = ld<T, W>(x + t - (hz ? (long long)szn * KB : 0));
-  const T cxp = px ? c.cx : (T)0, cyp = py ? c.cy : (T)0, czp = pz ? c.cz : (T)0;
-  const T cxm = hx ? wxm : (T)0, cym = hy ? wym : (T)0, czm = hz ? wzm : (T)0;
-  Vec<T, W> acc;
-  if constexpr (PACK && std::is_same<T, float>::value && W % 2 == 0) {
-    // couplings enter with the sign that makes every term one FMA
-    const float sg = SUB ? 1.f : -1.f;
-    const float2 cd = dup2(-sg * c.d), kxp = dup2(sg * cxp), kxm = dup2(sg * cxm), kyp = dup2(sg * cyp),
-                 kym = dup2(sg * cym), kzp = dup2(sg * czp), kzm = dup2(sg * czm);
-#pragma unroll
-    for (int p = 0; p < W / 2; ++p) {
-      float2 a = SUB ? __ffma2_rn(cd, pair(v0, p), pair(*acc0, p)) : __fmul2_rn(cd, pair(v0, p));
-      a = __ffma2_rn(kxp, pair(vxp, p), a);
-      a = __ffma2_rn(kxm, pair(vxm, p), a);
-      a = __ffma2_rn(kyp, pair(vyp, p), a);
-      a = __ffma2_rn(kym, pair(vym, p), a);
-      a = __ffma2_rn(kzp, pair(vzp, p), a);
-      a = __ffma2_rn(kzm, pair(vzm, p), a);
-      acc.a[2 * p] = a.x;
-      acc.a[2 * p + 1] = a.y;
-    }
-  } else {
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      const T ax = c.d * v0.a[e] - cxp * vxp.a[e] - cxm * vxm.a[e] - cyp * vyp.a[e] - cym * vym.a[e] -
-                   czp * vzp.a[e] - czm * vzm.a[e];
-      acc.a[e] = SUB ? acc0->a[e] - ax : ax;
-    }
-  }
-  return acc;
-}
-
-// (A x) for the W lanes at element t of node n = (i, j, k); x stored as S.
-template <typename T, int KB, int W, typename S, bool PACK = true>
-__device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *__restrict__ coef,
-                                                  const S *__restrict__ x, long long t, int n, int i, int j, int k,
-                                                  const Dims &d) {
-  return stencil_core<T, KB, W, S, false, PACK>(coef, x, t, n, i, j, k, d, nullptr);
-}
-
-// (r - A x) for the W lanes at element t of node n = (i, j, k); x stored as S.
-template <typename T, int KB, int W, typename S, bool PACK = true>
-__device__ __forceinline__ Vec<T, W> stencil_sub(const typename CoefT<T>::type *__restrict__ coef,
-                                                  const S *__restrict__ x, long long t, int n, int i, int j, int k,
-                                                  const Dims &d, const Vec<T, W> &r) {
-  return stencil_core<T, KB, W, S, true, PACK>(coef, x, t, n, i, j, k, d, &r);
+  return stencil_terms<T, W, PACK>(c.d, px ? c.cx : (T)0, hx ? wxm : (T)0, py ? c.cy : (T)0, hy ? wym : (T)0,
+                                   pz ? c.cz : (T)0, hz ? wzm : (T)0, v0, vxp, vxm, vyp, vym, vzp, vzm);
 }
 
 // Right-hand side r (type R) of a smoothing kernel at element t, times the
@@ -427,85 +400,39 @@ __global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, 
 // five of the d-vector form.  With DOT (finest level), also per-block partials
 // of r . x_{k+1} with the unscaled PCG residual r.
 template <typename T, typename V, typename R, int KB, bool DOT, int PREV>
-__global__ void __launch_bounds__(TPB, (stencil_min_blocks<T, V>(!DOT && PREV == 2 && sizeof(R) == 2 ? 5 : 0))) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
+__global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
                                                    const R *__restrict__ r, const float *__restrict__ scale,
                                                    const V *__restrict__ zin, V *zout, Dims d, int nb, T c1, T c2,
                                                    double *__restrict__ partial, int gs) {
   constexpr int W = Lanes<V, KB>::W;
-  constexpr bool PACK = true;  // two-lane fp32 instructions in the steps without partials
   const auto *coef = coef_of<T, KB>(cf);
   auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    if constexpr (DOT) {
-      // with the r.z partials (register-bound): scalar lanes, r loaded after the stencil's seven loads
-      const Vec<T, W> az = stencil_vec<T, KB, W, V, false>(coef, zin, t, n, i, j, k, d);
-      const Vec<T, W> rv = ld<T, W>(r + t);
-      const Vec<T, W> zc = ld<T, W>(zin + t);
-      Vec<T, W> zo;
-      if (PREV == 1) zo = ld<T, W>(zout + t);
-      const T s = c2 * invd[n];
+    // A x_k (two lanes per instruction without the partials; with them the
+    // kernel is register-bound and keeps scalar lanes), r loaded after the
+    // stencil's seven loads, then the scalar update.  Registers are left to
+    // the compiler (64, 4 blocks of TPB per SM): at 1M nodes x 256 RHS this
+    // measured faster than 48 registers at 5 blocks, and than the zero-start
+    // step as one r - A x chain of two-lane FMAs (405 -> 384 us per launch).
+    const Vec<T, W> az = stencil_vec<T, KB, W, V, !DOT>(coef, zin, t, n, i, j, k, d);
+    const Vec<T, W> rv = ld<T, W>(r + t);
+    const Vec<T, W> zc = ld<T, W>(zin + t);
+    Vec<T, W> zo;
+    if (PREV == 1) zo = ld<T, W>(zout + t);
+    const T s = c2 * invd[n];
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        T mom = (T)0;
-        if (PREV == 1) mom = c1 * (zc.a[e] - zo.a[e]);
-        if (PREV == 2) mom = c1 * zc.a[e];
-        const T re = scale ? rv.a[e] * (T)scale[b * KB + q * W + e] : rv.a[e];
-        zo.a[e] = zc.a[e] + mom + s * (re - az.a[e]);
-      }
-      st<T, W>(zout + t, zo);
+    for (int e = 0; e < W; ++e) {
+      const T mom = PREV == 1 ? c1 * (zc.a[e] - zo.a[e]) : (PREV == 2 ? c1 * zc.a[e] : (T)0);
+      const T re = scale ? rv.a[e] * (T)scale[b * KB + q * W + e] : rv.a[e];
+      zo.a[e] = zc.a[e] + mom + s * (re - az.a[e]);
+    }
+    st<T, W>(zout + t, zo);
+    if constexpr (DOT) {
       // r . z with z as stored (rounded to V): the preconditioned vector PCG uses
       const Vec<T, W> zs = rounded<V>(zo);
 #pragma unroll
       for (int e = 0; e < W; ++e) acc[e] += rv.a[e] * zs.a[e];
-    } else if constexpr (PREV != 2) {
-      // A x_k with two lanes per instruction, then the scalar update (with the compiler's register
-      // allocation: 64 registers, 4 blocks per SM, measured faster than 48 registers at 5 blocks)
-      const Vec<T, W> az = stencil_vec<T, KB, W, V, PACK>(coef, zin, t, n, i, j, k, d);
-      const Vec<T, W> rv = ld<T, W>(r + t);
-      const Vec<T, W> zc = ld<T, W>(zin + t);
-      Vec<T, W> zo;
-      if (PREV == 1) zo = ld<T, W>(zout + t);
-      const T s = c2 * invd[n];
-#pragma unroll
-      for (int e = 0; e < W; ++e) {
-        const T mom = PREV == 1 ? c1 * (zc.a[e] - zo.a[e]) : (T)0;
-        const T re = scale ? rv.a[e] * (T)scale[b * KB + q * W + e] : rv.a[e];
-        zo.a[e] = zc.a[e] + mom + s * (re - az.a[e]);
-      }
-      st<T, W>(zout + t, zo);
-    } else {
-      // second step of a zero start: u = r - A x_k in one FMA chain, two lanes per instruction
-      Vec<T, W> re = ld<T, W>(r + t);
-      if (scale) {
-#pragma unroll
-        for (int e = 0; e < W; ++e) re.a[e] *= (T)scale[b * KB + q * W + e];
-      }
-      const Vec<T, W> u = stencil_sub<T, KB, W, V, PACK>(coef, zin, t, n, i, j, k, d, re);
-      const Vec<T, W> zc = ld<T, W>(zin + t);
-      Vec<T, W> zo;
-      if (PREV == 1) zo = ld<T, W>(zout + t);
-      const T s = c2 * invd[n];
-      if constexpr (PACK && std::is_same<T, float>::value && W % 2 == 0) {
-        const float2 s2 = dup2(s), c12 = dup2(c1);
-#pragma unroll
-        for (int p = 0; p < W / 2; ++p) {
-          float2 w = __ffma2_rn(s2, pair(u, p), pair(zc, p));  // x_k + s (r - A x_k)
-          if (PREV == 1) w = __ffma2_rn(c12, __fadd2_rn(pair(zc, p), neg2(pair(zo, p))), w);
-          if (PREV == 2) w = __ffma2_rn(c12, pair(zc, p), w);
-          zo.a[2 * p] = w.x;
-          zo.a[2 * p + 1] = w.y;
-        }
-      } else {
-#pragma unroll
-        for (int e = 0; e < W; ++e) {
-          T w = fma(s, u.a[e], zc.a[e]);
-          if (PREV == 1) w = fma(c1, zc.a[e] - zo.a[e], w);
-          if (PREV == 2) w = fma(c1, zc.a[e], w);
-          zo.a[e] = w;
-        }
-      }
-      st<T, W>(zout + t, zo);
     }
   };
   auto pf = [&](long long tn) {
