@@ -35,6 +35,11 @@ namespace {
 
 constexpr int TPB = 256;
 
+// Per-thread dot-product sums of the fp32 stencil kernels with partials
+// (k_apply, k_cheb_step) kept in shared memory, which frees the registers the
+// two-lane stencil needs.
+constexpr bool DOT_SMEM = true;
+
 // floor(n / d) for 0 <= n < 2^31 with m = div_magic(d).
 __device__ __forceinline__ int fast_div(int n, int d, unsigned m) {
   if (d == 1) return n;
@@ -293,15 +298,20 @@ struct NoPf {
 // grid on one RHS block at a time, as in the flat sweep), each closed by the
 // block reduction of that RHS block's per-thread sums.
 // body(b, n, q, t, acc): RHS block, node, lane group, element offset, sums.
-template <typename T, int KB, int W, typename Body, typename Pf = NoPf>
+// With SM the per-thread sums live in shared memory (the thread's own W
+// entries, same operations in the same order: identical sums) instead of W
+// registers across the sweep, which leaves those registers to the body.
+template <typename T, int KB, int W, bool SM = false, typename Body, typename Pf = NoPf>
 __device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int gs, Body body, Pf pf = Pf()) {
   constexpr int LPN = KB / W;
   __shared__ T red[(TPB / 32) * KB];
+  __shared__ Vec<T, W> sacc[SM ? TPB : 1];
   const int q = threadIdx.x % LPN;
   const long long per = (long long)N * LPN;
   const long long stride = (long long)gridDim.x * TPB;
   for (int b = 0; b < nb; ++b) {
-    T acc[W];
+    T racc[W];
+    T(&acc)[W] = SM ? sacc[SM ? threadIdx.x : 0].a : racc;
 #pragma unroll
     for (int e = 0; e < W; ++e) acc[e] = (T)0;
     const long long base = (long long)b * N;
@@ -310,7 +320,11 @@ __device__ __forceinline__ void sweep_reduce(int N, int nb, double *partial, int
       if (g + stride < per) pf((base + (g + stride) / LPN) * KB + q * W);
       body(b, n, q, (base + n) * KB + q * W, acc);
     }
-    block_reduce<T, KB, W>(acc, red, b, partial, gs);
+    if constexpr (SM) {
+#pragma unroll
+      for (int e = 0; e < W; ++e) racc[e] = acc[e];
+    }
+    block_reduce<T, KB, W>(racc, red, b, partial, gs);
   }
 }
 
@@ -333,7 +347,7 @@ __device__ __forceinline__ void sweep_flat(int N, unsigned mn, int nb, Body body
 // ---------------------------------------------------------------- stencil ops
 // y = A x (y in T, x stored as S); with DOT also per-block partials of x.y.
 template <typename T, typename S, int KB, bool DOT>
-__global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, const S *__restrict__ x,
+__global__ void __launch_bounds__(TPB, (DOT && sizeof(T) == 4 && sizeof(S) == 2) ? 4 : 0) k_apply(const void *__restrict__ cf, const S *__restrict__ x,
                                                T *__restrict__ y, Dims d, int nb, double *__restrict__ partial,
                                                int gs) {
   constexpr int W = Lanes<S, KB>::W;
@@ -341,7 +355,7 @@ __global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, cons
   auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    const Vec<T, W> v = stencil_vec<T, KB, W, S, !DOT>(coef, x, t, n, i, j, k, d);
+    const Vec<T, W> v = stencil_vec<T, KB, W, S, !DOT || DOT_SMEM>(coef, x, t, n, i, j, k, d);
     st<T, W>(y + t, v);
     if (DOT) {
       const Vec<T, W> xv = ld<T, W>(x + t);
@@ -354,7 +368,7 @@ __global__ void __launch_bounds__(TPB) k_apply(const void *__restrict__ cf, cons
     if constexpr (sizeof(T) == 4) pf_line(x, tn);
   };
   if (DOT)
-    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body, pf);
+    sweep_reduce<T, KB, W, DOT_SMEM && sizeof(T) == 4>(d.N, nb, partial, gs, body, pf);
   else
     sweep_flat<T, KB, W>(d.N, d.mn, nb, body, pf);
 }
@@ -409,13 +423,12 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
   auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
-    // A x_k (two lanes per instruction without the partials; with them the
-    // kernel is register-bound and keeps scalar lanes), r loaded after the
-    // stencil's seven loads, then the scalar update.  Registers are left to
+    // A x_k (two lanes per instruction), r loaded after the stencil's seven
+    // loads, then the scalar update.  Registers are left to
     // the compiler (64, 4 blocks of TPB per SM): at 1M nodes x 256 RHS this
     // measured faster than 48 registers at 5 blocks, and than the zero-start
     // step as one r - A x chain of two-lane FMAs (405 -> 384 us per launch).
-    const Vec<T, W> az = stencil_vec<T, KB, W, V, !DOT>(coef, zin, t, n, i, j, k, d);
+    const Vec<T, W> az = stencil_vec<T, KB, W, V, !DOT || DOT_SMEM>(coef, zin, t, n, i, j, k, d);
     const Vec<T, W> rv = ld<T, W>(r + t);
     const Vec<T, W> zc = ld<T, W>(zin + t);
     Vec<T, W> zo;
@@ -443,7 +456,7 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
     }
   };
   if (DOT)
-    sweep_reduce<T, KB, W>(d.N, nb, partial, gs, body, pf);
+    sweep_reduce<T, KB, W, DOT_SMEM && sizeof(T) == 4>(d.N, nb, partial, gs, body, pf);
   else
     sweep_flat<T, KB, W>(d.N, d.mn, nb, body, pf);
 }

@@ -55,11 +55,60 @@ __device__ __forceinline__ void df_acc(float &sh, float &sl, float ph, float pl)
   sl = e - (sh - s);
 }
 
-// (ph, pl) = (ah, al) * (bh, bl) up to the al * bl term
-__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float &ph, float &pl) {
-  ph = ah * bh;
-  pl = fmaf(ah, bh, -ph);
-  pl = fmaf(ah, bl, fmaf(al, bh, pl));
+// Accurate dot product in the manner of Ogita, Rump and Oishi ("Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26, 2005; Dot2): the high parts of
+// the products are summed with Knuth's error-free two-sum into s, and every
+// low-order quantity (the products' exact rounding errors from an FMA, the
+// cross terms w_hi v_lo and w_lo v_hi, the two-sum errors) into one plain
+// fp32 sum c; s + c is the result.  Each term is w * v with w = wh + wl one
+// coefficient of the node and v = vh + vl per lane.  Lane pairs go through the
+// two-lane fp32 instructions; a - b is written fma(b, -1, a) (one instruction,
+// the same rounding as the subtraction).
+__device__ __forceinline__ void dot2_pair(float wh, float wl, float2 vh, float2 vl, float2 &s, float2 &c) {
+  const float2 m1 = make_float2(-1.f, -1.f), kw = make_float2(wh, wh), kwl = make_float2(wl, wl),
+               knw = make_float2(-wh, -wh);
+  const float2 ph = __fmul2_rn(kw, vh);
+  const float2 npe = __ffma2_rn(knw, vh, ph);  // -(wh vh - ph), exactly
+  c = __ffma2_rn(kw, vl, c);
+  c = __ffma2_rn(kwl, vh, c);
+  c = __ffma2_rn(npe, m1, c);
+  const float2 s1 = __fadd2_rn(s, ph);          // two-sum of s and ph
+  const float2 bb = __ffma2_rn(s, m1, s1);      // s1 - s
+  const float2 ea = __ffma2_rn(__ffma2_rn(bb, m1, s1), m1, s);  // s - (s1 - bb)
+  const float2 eb = __ffma2_rn(bb, m1, ph);     // ph - bb
+  c = __fadd2_rn(c, __fadd2_rn(ea, eb));
+  s = s1;
+}
+
+__device__ __forceinline__ void dot2_one(float wh, float wl, float vh, float vl, float &s, float &c) {
+  const float ph = wh * vh;
+  const float npe = fmaf(-wh, vh, ph);
+  c = fmaf(wh, vl, c);
+  c = fmaf(wl, vh, c);
+  c -= npe;
+  float s1, e;
+  two_sum(s, ph, s1, e);
+  c += e;
+  s = s1;
+}
+
+template <int W>
+__device__ __forceinline__ void dot2_terms(float wh, float wl, const Vec<float, W> &vh, const Vec<float, W> &vl,
+                                           Vec<float, W> &s, Vec<float, W> &c) {
+  if constexpr (W % 2 == 0) {
+#pragma unroll
+    for (int p = 0; p < W / 2; ++p) {
+      float2 sp = pair(s, p), cp = pair(c, p);
+      dot2_pair(wh, wl, pair(vh, p), pair(vl, p), sp, cp);
+      s.a[2 * p] = sp.x;
+      s.a[2 * p + 1] = sp.y;
+      c.a[2 * p] = cp.x;
+      c.a[2 * p + 1] = cp.y;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < W; ++e) dot2_one(wh, wl, vh.a[e], vl.a[e], s.a[e], c.a[e]);
+  }
 }
 
 // hi = fp32(v), lo = fp32(v - hi) with fp64 instructions: a call of its own, so
@@ -137,7 +186,7 @@ __global__ void __launch_bounds__(TPB) k_ir_residual_df(const Coef32 *__restrict
                                                         int gs) {
   using T = float;
   constexpr int W = Lanes<T, KB>::W;
-  sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
+  sweep_reduce<T, KB, W, true>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
     node_ijk(n, d, i, j, k);
     const bool hx = i > 0, px = i + 1 < d.Nx, hy = j > 0, py = j + 1 < d.Ny, hz = k > 0, pz = k + 1 < d.Nz;
@@ -153,29 +202,18 @@ __global__ void __launch_bounds__(TPB) k_ir_residual_df(const Coef32 *__restrict
                               pz ? (long long)sz * KB : 0,  hz ? -(long long)sz * KB : 0};
     const Vec<T, W> b0h = ld<T, W>(bh + t), b0l = ld<T, W>(bl + t);
     const Vec<T, W> x0h = ld<T, W>(xh + t), x0l = ld<T, W>(xl + t);
-    float rh[W], rl[W];
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      rh[e] = b0h.a[e];
-      rl[e] = b0l.a[e];
-      float ph, pl;
-      df_mul(c0h.d, c0l.d, x0h.a[e], x0l.a[e], ph, pl);
-      df_acc(rh[e], rl[e], -ph, -pl);
-    }
+    // sum (s, c): s = b_hi, c = b_lo; the centre term enters with negated coefficients
+    Vec<T, W> sv = b0h, cv = b0l;
+    dot2_terms<W>(-c0h.d, -c0l.d, x0h, x0l, sv, cv);
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
       const Vec<T, W> vh = ld<T, W>(xh + t + off[m]), vl = ld<T, W>(xl + t + off[m]);
-#pragma unroll
-      for (int e = 0; e < W; ++e) {
-        float ph, pl;
-        df_mul(wh[m], wl[m], vh.a[e], vl.a[e], ph, pl);
-        df_acc(rh[e], rl[e], ph, pl);
-      }
+      dot2_terms<W>(wh[m], wl[m], vh, vl, sv, cv);
     }
     Vec<T, W> out;
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const float rv = rh[e] + rl[e];
+      const float rv = sv.a[e] + cv.a[e];
       acc[e] += rv * rv;
       out.a[e] = active[b * KB + q * W + e] ? rv : 0.0f;
     }
