@@ -624,6 +624,21 @@ class Simulation3DNodal:
         rn[has_n] = e_n
         wm = fac.astype(np.float64).copy()
         wn = np.where(has_n, -fac, 0.0)
+        # Electrodes numbered by first appearance in datum order (A, B, M, N of each datum): the electrodes
+        # that consecutive data use then have consecutive numbers, so the dc_jtj_diag kernel's reads of their
+        # staged pole values (one warp = 32 consecutive data) fall in distinct shared-memory banks.  np.unique
+        # numbers them by coordinates, which on line surveys puts consecutive stations a line count apart.
+        seq = np.stack([sa, sb, rm, rn], axis=1).ravel()
+        seq = seq[seq >= 0]
+        old_ids, first = np.unique(seq, return_index=True)
+        old_of_new = old_ids[np.argsort(first, kind="stable")]
+        unused = np.setdiff1d(np.arange(uniq.shape[0]), old_of_new)
+        old_of_new = np.concatenate([old_of_new, unused]).astype(np.int64)
+        new_of_old = np.empty(uniq.shape[0], np.int32)
+        new_of_old[old_of_new] = np.arange(uniq.shape[0], dtype=np.int32)
+        renum = lambda e: np.where(e >= 0, new_of_old[np.maximum(e, 0)], -1).astype(np.int32)
+        uniq = uniq[old_of_new]
+        sa, sb, rm, rn = renum(sa), renum(sb), renum(rm), renum(rn)
         return uniq, dict(sa=sa, sb=sb, rm=rm, rn=rn, ia=ia, ib=ib, wm=wm, wn=wn)
 
     def _jtj_diag_reciprocity(self, w):

@@ -642,3 +642,39 @@ def test_solver_argument_warns():
         except Exception:
             pass  # no CUDA here: the engine may fail to build after the warning
     assert any("SolverLU" in str(w.message) and "not used" in str(w.message) for w in rec)
+
+
+def test_electrode_tables_numbered_by_first_appearance():
+    """The reciprocity tables of getJtJdiag: every datum's A, B, M, N indices point at its electrode
+    positions, and electrodes are numbered in order of first appearance over the data, so that along a
+    survey line consecutive data use consecutive electrode numbers (distinct shared-memory banks in the
+    dc_jtj_diag kernel)."""
+    from types import SimpleNamespace
+
+    from simpeg_gb300.resistivity.simulation import Simulation3DNodal
+
+    n_lines, n_st, n_rx = 3, 12, 4
+    src_list = []
+    for yv in (0.0, 10.0, 20.0):
+        for i in range(n_st - n_rx - 2):
+            js = i + 1 + np.arange(1, n_rx + 1)
+            M = np.c_[5.0 * js, np.full(n_rx, yv), np.zeros(n_rx)]
+            N = np.c_[5.0 * (js + 1), np.full(n_rx, yv), np.zeros(n_rx)]
+            src_list.append(sources.Dipole([receivers.Dipole(M, N)], np.r_[5.0 * i, yv, 0.0],
+                                           np.r_[5.0 * (i + 1), yv, 0.0]))
+    survey = Survey(src_list)
+    uniq, t = Simulation3DNodal._electrode_tables(SimpleNamespace(survey=survey))
+    d = 0
+    for src in survey.source_list:
+        A, B = np.atleast_2d(src.location)
+        for rx in src.receiver_list:
+            for r in range(rx.nD):
+                np.testing.assert_array_equal(uniq[t["sa"][d]], A)
+                np.testing.assert_array_equal(uniq[t["sb"][d]], B)
+                np.testing.assert_array_equal(uniq[t["rm"][d]], rx.locations[0][r])
+                np.testing.assert_array_equal(uniq[t["rn"][d]], rx.locations[1][r])
+                d += 1
+    assert d == t["sa"].size
+    # every electrode appears once in uniq; along one source's receivers M numbers are consecutive
+    assert np.unique(uniq, axis=0).shape[0] == uniq.shape[0]
+    assert np.all(np.diff(t["rm"][:n_rx]) == 1)
