@@ -68,7 +68,7 @@ def _args():
     ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
     ap.add_argument("--sources", type=int, default=0, help="use only the first N sources (profiling runs)")
     ap.add_argument("--workload", default="forward",
-                    choices=["forward", "block", "differentiation", "gauss_newton", "batched"],
+                    choices=["forward", "block", "differentiation", "gauss_newton", "batched", "cc"],
                     help="forward: the headline 1M-cell line; differentiation: the 96x96x48 gradient checks")
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--profile-solve", action="store_true",
@@ -209,11 +209,28 @@ def _oracle_spot_worker(mesh, m, src, v_s, rtol):
     return d, g, time.perf_counter() - t0
 
 
+def _oracle_spot_worker_cc(mesh, m, src, v_s, rtol):
+    """One source of the cell-centred oracle (``oracle/cc3d.py``: Robin ``Div MfRhoI Grad``, fp64 SciPy
+    CG + Jacobi to ``rtol``): the source's data and ``J^T v_s`` with respect to m = ln sigma.  Runs in a
+    spawned process (never the product path)."""
+    from oracle.cc3d import OracleDC3DCellCentered
+    from simpeg_gb300 import maps
+    from simpeg_gb300.resistivity.survey import Survey
+
+    t0 = time.perf_counter()
+    o = OracleDC3DCellCentered(mesh, Survey([src]), sigma_map=maps.ExpMap(mesh), solver="cg", cg_rtol=rtol)
+    o.set_model(m)
+    f = o.fields()
+    d = o.dpred(f=f)
+    g = o.Jtvec(m, v_s, f=f) if v_s is not None else None
+    return d, g, time.perf_counter() - t0
+
+
 class OracleSpots:
     """Independent at-scale parity: a few sources of the workload solved by the oracle on the host
     (spawned processes, one per source, overlapping the GPU work), compared with the GPU path."""
 
-    def __init__(self, mesh, m, survey, idx, v, rtol=ORACLE_RTOL):
+    def __init__(self, mesh, m, survey, idx, v, rtol=ORACLE_RTOL, worker=_oracle_spot_worker):
         import multiprocessing as mp
 
         self.idx = list(idx)
@@ -236,7 +253,7 @@ class OracleSpots:
             s_ = sl[src, rx] if sl is not None else None
             self.slices.append(s_)
             vs = None if v is None else np.ascontiguousarray(v[s_])
-            self.jobs.append(self.pool.apply_async(_oracle_spot_worker, (mesh, m, src, vs, rtol)))
+            self.jobs.append(self.pool.apply_async(worker, (mesh, m, src, vs, rtol)))
 
     def compare(self, d_gpu, jtvec_gpu_fn, timeout=1800):
         """d_gpu: the GPU data of the whole survey; jtvec_gpu_fn(i, v_s): the GPU J^T v_s of source i
@@ -711,13 +728,15 @@ def run_gauss_newton(args):
     gradient plus smallness + smoothness regularisation, exact getJtJdiag
     (electrode reciprocity) for the Jacobi preconditioner, and 10 CG iterations
     on 2 J^T W^2 J + 2 beta R, each one batched Jvec and one batched Jtvec.
-    Run in mixed precision and in plain fp64 on the same GPU; prints times and
+    Run in mixed precision and in plain fp64 on the same GPU, each with the
+    smoother the autotuner picks for this mesh (untimed); prints times and
     the relative differences of g, diag(J^T J) and the search direction, and
     for two sources the data and J^T v against the oracle (SciPy CG to 1e-12).
     """
     import torch
 
     from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.autotune import tune_engine
     from simpeg_gb300.engine import kernel_launches
     from simpeg_gb300.inversion import L2DataMisfit, WeightedLeastSquares, inexact_gauss_newton_direction
     from simpeg_gb300.resistivity import Simulation3DNodal
@@ -758,6 +777,14 @@ def run_gauss_newton(args):
     res = {}
     for precision in ("mixed", "fp64"):
         sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=precision, rtol=RTOL)
+        # untimed: the autotuner picks the smoother (Chebyshev degree and interval) for this mesh and
+        # source count, in each precision, from sample solves at the starting model
+        t_tune = time.perf_counter()
+        sim.model = m0
+        sim._ensure_model()
+        tuned = tune_engine(sim.engine, survey.nSrc, precision, rtol=RTOL,
+                            cands=[(0, 2, 15.0), (0, 2, 30.0), (0, 3, 15.0), (0, 3, 30.0)])
+        t_tune = time.perf_counter() - t_tune
         dmis = L2DataMisfit(sim, dobs, W=W)
         reg = WeightedLeastSquares(mesh, sim)
         torch.cuda.synchronize()
@@ -775,7 +802,9 @@ def run_gauss_newton(args):
         launches = kernel_launches() - n0
         res[precision] = (p_host, info["g"].cpu().numpy(), info["jtj_diag"].cpu().numpy())
         out[precision] = {"seconds": dt, "cg_rel_res": info["cg_rel_res"][-1],
-                          "phases_seconds": {k: round(v, 3) for k, v in info["seconds"].items()}}
+                          "phases_seconds": {k: round(v, 3) for k, v in info["seconds"].items()},
+                          "smoother": {"degree": tuned["nu"], "interval": f"lmax/{tuned['cheb_ratio']:g}",
+                                       "tuning_seconds_untimed": round(t_tune, 1)}}
         if precision == "mixed":
             out["value"] = 1.0 / dt
             out["ms_per_step"] = dt * 1e3
@@ -961,6 +990,149 @@ def _superlu_step(mesh, sigma, survey):
     return d, {"assembly_s": t1 - t0, "factor_s": t2 - t1, "solve_s": t3 - t2, "dpred_s": t4 - t3, "total_s": t4 - t0}
 
 
+def run_cc(args):
+    """The headline workload (1M cells, 256 pole sources, 10,240 data, rtol 1e-9) in the cell-centred
+    formulation: ``Simulation3DCellCentered`` (Robin), 1,048,576 unknowns on the grid of cell
+    centres, and the induced-polarization data of the same formulation.
+
+    ``value``: mixed source-solves/s of the cell-centred forward solve with the source terms on the
+    device; ``e2e``: ``dpred(m)`` from a host model to host data.  Jtvec/s and the IP prediction
+    (``induced_polarization.Simulation3DCellCentered.dpred(eta)``: one multi-RHS solve with the DC
+    fields kept) ride along, mixed and fp64, with relative errors against fp64 solves at 1e-12 and,
+    for two sources, against the cell-centred oracle (SciPy CG to 1e-12).  Prints one JSON line.
+    """
+    import torch
+
+    from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.engine import kernel_launches
+    from simpeg_gb300.induced_polarization import Simulation3DCellCentered as IPSimulation3DCellCentered
+    from simpeg_gb300.resistivity import Simulation3DCellCentered
+    from simpeg_gb300.resistivity.survey import Survey
+
+    mesh, sigma, survey = workloads.scale_forward(seed=1, n_side=args.n_side)
+    m = np.log(sigma)
+    K = survey.nSrc
+    rng = np.random.default_rng(21)
+    v_host = rng.standard_normal(survey.nD)
+    eta = 0.1 * rng.random(mesh.n_cells)
+    m2 = m + 1e-3 * rng.standard_normal(m.size)
+    spots = None if args.no_oracle else OracleSpots(mesh, m, survey, [0, K - 1], v_host,
+                                                    worker=_oracle_spot_worker_cc)
+    torch.cuda.set_device(0)
+
+    def timed_loop(fn, steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / steps, r
+
+    res, out = {}, {}
+    for precision, rtol in (("mixed", RTOL), ("fp64", RTOL), ("ref", 1e-12)):
+        prec = "fp64" if precision == "ref" else precision
+        sim = Simulation3DCellCentered(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision=prec,
+                                       rtol=rtol)
+        sim.model = m
+        sim._ensure_model()
+        eng = sim.engine
+        Q = sim.getRHS()
+        if precision != "ref":
+            for _ in range(max(1, args.warmup)):
+                eng.solve(Q, mode=prec, rtol=rtol)
+            torch.cuda.synchronize()
+            n0 = kernel_launches()
+            if precision == "mixed":
+                eng.stencil_timing(True)
+            with Clocks(0) as clk:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(args.steps):
+                    U, info = eng.solve(Q, mode=prec, rtol=rtol)
+                e1.record()
+                torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            launches = kernel_launches() - n0
+            out[precision] = {"ms_per_solve": ms, "source_solves_per_s": K / (ms / 1e3),
+                              "inner_iterations": info.iterations, "outer": info.outer, "levels": info.n_levels}
+            if precision == "mixed":
+                st = eng.stencil_timing(False)
+                kinds = eng.stencil_timing_kinds()
+                out["clocks"] = clk.summary()
+                out["gpu_launches"] = launches  # kernels of the timed solves
+        f = sim.fields(m)
+        d = sim.dpred(m, f=f)
+        sim.Jtvec(m, v_host, f=f)
+        t_jt, g = timed_loop(lambda: sim.Jtvec(m, v_host, f=f), 1 if precision == "ref" else args.steps)
+        ip = IPSimulation3DCellCentered(mesh, survey=survey, sigma=sigma, precision=prec, rtol=rtol,
+                                        _f=f)
+        ip.dpred(eta)
+        t_ip, d_ip = timed_loop(lambda: ip.dpred(eta), 1 if precision == "ref" else args.steps)
+        res[precision] = (np.asarray(d), np.asarray(g), np.asarray(d_ip))
+        if precision != "ref":
+            out[precision]["jtvec_per_s"] = 1.0 / t_jt
+            out[precision]["ip_dpred_per_s"] = 1.0 / t_ip
+        if precision == "mixed":
+            sim.dpred(m2)
+            t_e2e, _ = timed_loop(lambda: (sim.dpred(m), sim.dpred(m2)), args.steps)
+            out["e2e"] = {"value": 2 * K / t_e2e, "unit": "source-solves/s",
+                          "h2d_bytes_per_step": int(mesh.n_cells * 8), "d2h_bytes_per_step": int(survey.nD * 8),
+                          "path": "Simulation3DCellCentered.dpred(m): host model -> H2D -> exp map on device -> "
+                                  "dc_set_model_cc -> solve -> gather -> D2H"}
+        del sim, eng, Q, ip, f
+        torch.cuda.empty_cache()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    mixed, fp64 = out.pop("mixed"), out.pop("fp64")
+    line = {"metric": "source-solves/s, 1M-cell DC3D cell-centred (Simulation3DCellCentered): mixed vs fp64",
+            "value": mixed["source_solves_per_s"], "unit": "source-solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mixed["ms_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement",
+            "data": "synthetic (seeded Gaussian random field, 16x16 pole grid; eta uniform in [0, 0.1))",
+            "config": {"workload": "dc3d_cell_centred_128x128x64", "mesh_cells": list(mesh.shape_cells),
+                       "unknowns": int(mesh.n_cells), "sources": K, "data": survey.nD, "bc_type": "Robin",
+                       "rtol": RTOL, "l2": "inputs larger than L2 (fp16 multigrid vectors 537 MB per RHS block "
+                                           "set)"},
+            "mixed": mixed, "fp64": fp64,
+            "speedup_vs_fp64": {"forward": fp64["ms_per_solve"] / mixed["ms_per_solve"],
+                                "jtvec": mixed["jtvec_per_s"] / fp64["jtvec_per_s"],
+                                "ip_dpred": mixed["ip_dpred_per_s"] / fp64["ip_dpred_per_s"]},
+            "rel_err_vs_fp64_1e-12": {"dpred": rel(res["mixed"][0], res["ref"][0]),
+                                      "jtvec_m": rel(res["mixed"][1], res["ref"][1]),
+                                      "ip_dpred": rel(res["mixed"][2], res["ref"][2])},
+            "roofline": _stencil_roofline(*st, kinds, what="fine-level Chebyshev steps on the grid of cell "
+                                                         "centres", scaled_traffic=True),
+            **out}
+    if spots is not None:
+        def jt_one(i, s_):
+            one = Simulation3DCellCentered(mesh, survey=Survey([survey.source_list[i]]),
+                                           sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+            return one.Jtvec(m, v_host[s_])
+
+        line["rel_err_vs_oracle_cg"] = spots.compare(res["mixed"][0], jt_one)
+    if not args.no_cpu_baseline:
+        from oracle.cc3d import OracleDC3DCellCentered
+
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+
+        o = OracleDC3DCellCentered(mesh, Survey([survey.source_list[0]]), sigma=sigma, solver="cg", cg_rtol=RTOL)
+        t0 = time.perf_counter()
+        A = o.getA()
+        Mj = sp.diags(1.0 / A.diagonal())
+        q = o.getRHS()[:, 0]
+        t_asm = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, cg_info = spla.cg(A, q, rtol=RTOL, atol=0.0, M=Mj, maxiter=200000)
+        t_cg = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / t_cg, "unit": "source-solves/s", "cores": 1, "kind": "port",
+                                "sample": (f"1 of {K} sources: the cell-centred oracle's assembly ({t_asm:.1f} s, "
+                                           f"excluded) + SciPy CG/Jacobi to rtol {RTOL:g} ({t_cg:.1f} s, "
+                                           f"info={cg_info})"),
+                                "solver": "SciPy CG + Jacobi (an iterative plug-in; SuperLU does not fit at this "
+                                          "size)"}
+    print(json.dumps(line), flush=True)
+
+
 def run_block(args):
     """32x32x16 cells of 10 m (18,513 nodes), 0.01 S/m with a 0.1 and a 0.001 S/m block, dipole-dipole
     line of 20 sources x 15 receivers (300 data): the size where the reference's default direct solver
@@ -1113,6 +1285,8 @@ def main():
         return run_batched(args)
     if args.workload == "gauss_newton" and args.impl != "reference":
         return run_gauss_newton(args)
+    if args.workload == "cc" and args.impl != "reference":
+        return run_cc(args)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "differentiation":

@@ -28,7 +28,9 @@ def _sample_rhs(nN, k, seed, device):
 
 def candidates(k):
     kbs = sorted({kb for kb in (8, 16, 32) if (k + kb - 1) // kb <= 32} | {0})
-    return list(itertools.product(kbs, (2, 3, 4), (30.0, 60.0)))
+    # intervals lmax/15 and lmax/30: on the 1M- and 2M-cell solves lmax/60 was slower at every degree, and
+    # degree 2 wants the wider interval (lmax/15)
+    return list(itertools.product(kbs, (2, 3, 4), (15.0, 30.0)))
 
 
 def tune_engine(engine, k, precision="mixed", rtol=1e-9, sigma=None, cands=None, seed=0):
@@ -52,7 +54,7 @@ def tune_engine(engine, k, precision="mixed", rtol=1e-9, sigma=None, cands=None,
             torch.cuda.synchronize()
             if info.status == 0:
                 times[(kb, nu, ratio)] = e0.elapsed_time(e1)
-        best = min(times, key=times.get) if times else (0, 3, 60.0)
+        best = min(times, key=times.get) if times else (0, 3, 30.0)
         _CACHE[key] = best
     kb, nu, ratio = best
     engine.set_rhs_block(kb)
