@@ -115,6 +115,17 @@ int dc_set_smoother(dc_handle *h, int kind);
  * latency it hides. */
 int dc_set_staging(dc_handle *h, int enable);
 
+/* Coarse-level operators (takes effect at the next dc_set_model / dc_set_model_cc):
+ * 0 rediscretises every coarse level from the volume-averaged conductivity;
+ * 1 forms it from the next finer level's operator, the Galerkin product with
+ * the linear prolongation collapsed onto seven points; 2 (default) the same
+ * with the fine couplings along a coarse edge combined in series.  The
+ * operator of the finest level, and so every result, does not change; the
+ * iterations a solve needs do (1M-cell solves, 256 RHS: cell-centred 19 -> 12
+ * PCG iterations, nodal with the log-conductivity contrast doubled 31 -> 20,
+ * the nodal headline solve 12 either way). */
+int dc_set_coarse_operator(dc_handle *h, int mode);
+
 /* Number of multigrid levels and nodes of level `lvl`. */
 int dc_level_info(dc_handle *h, int lvl, int *n_levels, long long *nodes, int *cells3);
 

@@ -63,6 +63,7 @@ _SIG = {
     "dc_set_mg_storage": (C.c_int, [_VP, C.c_int]),
     "dc_set_smoother": (C.c_int, [_VP, C.c_int]),
     "dc_set_staging": (C.c_int, [_VP, C.c_int]),
+    "dc_set_coarse_operator": (C.c_int, [_VP, C.c_int]),
     "dc_level_info": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
     "dc_set_model": (C.c_int, [_VP, _DP, _VP]),
     "dc_apply": (C.c_int, [_VP, _DP, _DP, C.c_int, _VP]),

@@ -247,6 +247,7 @@ struct dc_handle {
   int check_every = 1;
   int mg_storage = DC_MG_FP16;  // mixed solve: storage of the multigrid vectors (dc_set_mg_storage)
   int smoother_kind = 1;  // Chebyshev polynomials of the first or fourth kind (dc_set_smoother)
+  int coarse_op = 2;           // coarse operators: 0 rediscretised, 1 collapsed Galerkin, 2 series (dc_set_coarse_operator)
   bool bulk_staging = false;  // finest-level smoothing with bulk-copy staged shared-memory tiles (dc_set_staging)
   int bulk_shape = 0;        // forced slab layout of the staged kernel (10 * rows + copy depth; 0 = automatic)
   int kb_force = 0;  // RHS-block width override (0: pick_kb)
@@ -1133,6 +1134,13 @@ int dc_set_smoother(dc_handle *h, int kind) {
   return 0;
 }
 
+int dc_set_coarse_operator(dc_handle *h, int mode) {
+  if (!h) return fail(DC_ERR_ARG, "null handle");
+  if (mode < 0 || mode > 2) return fail(DC_ERR_ARG, "coarse operator mode must be 0, 1 or 2");
+  h->coarse_op = mode;
+  return 0;
+}
+
 int dc_set_staging(dc_handle *h, int enable) {
   if (!h) return fail(DC_ERR_ARG, "null handle");
   h->bulk_staging = enable != 0;
@@ -1178,6 +1186,8 @@ static int set_model_impl(dc_handle *h, const double *sigma_dev, const CCFine *c
   for (size_t l = 0; l < nl; ++l) {
     if (l == 0 && cc)
       cc_coef_build(L0, cc->rho, cc->hp, cc->bw, h->d_lmax, s);
+    else if (l > 0 && h->coarse_op)
+      coef_galerkin(h->lv[l - 1], h->lv[l], h->coarse_op, h->d_lmax + l, s);
     else
       coef_build(h->lv[l], h->robin, h->d_lmax + l, s);
   }

@@ -179,6 +179,9 @@ void outer_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_activ
 
 void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s);
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s);
+// Coarse level c's operator from the finer level f's coefficients (mode 1: collapsed Galerkin product with
+// the linear prolongation; mode 2: fine couplings in series along each coarse edge).
+void coef_galerkin(const Level &f, const Level &c, int mode, unsigned long long *d_lmax_bits, cudaStream_t s);
 void dense_assemble(const Level &L, double *dense, cudaStream_t s);
 void dense_cholesky_inverse(double *dense, double *work, int n, double *Ainv64, float *Ainv32, int *flag,
                             cudaStream_t s);

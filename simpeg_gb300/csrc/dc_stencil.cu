@@ -326,6 +326,143 @@ __global__ void k_coarsen_sigma(const double *__restrict__ sf, const double *__r
   }
 }
 
+// ---------------------------------------------------------------- operator-based coarse levels
+// A coarse level's seven-point operator formed from the finer level's
+// couplings instead of rediscretised from an averaged conductivity (mode 1: the
+// Galerkin product P^T A P with the engine's linear prolongation, collapsed
+// onto the seven-point pattern; mode 2: the fine couplings along a coarse edge
+// combined in series).  The energy of every fine edge goes to the coarse edge
+// of its direction: along the edge with the squared prolongation weights of
+// the fine nodes it joins (mode 1) or as resistors in series (mode 2), across
+// it with the transverse nodes' linear prolongation weights (the cross terms
+// P^T A P would put on diagonal neighbours are summed onto the axis ones).
+// The diagonal excess of the fine rows (the Robin term) is lumped with the
+// linear weights.  On a uniform mesh with a constant conductivity mode 1
+// reproduces the rediscretised interior couplings.
+struct AxisTab {
+  const int *fi;      // coarse node -> fine node, per axis at fo[a]
+  const int *pl;      // fine node -> left coarse node, per axis at po[a]
+  const double *pw;   // weight of the left coarse node, per axis at po[a]
+  long long fo[3], po[3];
+};
+
+__device__ __forceinline__ double pwgt(const AxisTab &t, int a, int f, int J) {
+  const int L = t.pl[t.po[a] + f];
+  const double w = t.pw[t.po[a] + f];
+  return L == J ? w : (L + 1 == J ? 1.0 - w : 0.0);
+}
+
+// fine coupling along axis a at fine node (f0, f1, f2) (to its + neighbour)
+__device__ __forceinline__ double fcpl(const Coef64 *c, const Dims &d, int a, int i, int j, int k) {
+  const Coef64 v = c[i + (long long)d.Nx * (j + (long long)d.Ny * k)];
+  return a == 0 ? v.cx : (a == 1 ? v.cy : v.cz);
+}
+
+// coarse coupling along axis a from coarse node (I0, I1, I2) to its + neighbour
+__device__ double ccpl(const Coef64 *fc, const Dims &fd, const Dims &cd, const AxisTab &t, int mode, int a, int I0,
+                       int I1, int I2) {
+  const int I[3] = {I0, I1, I2};
+  const int fN[3] = {fd.Nx, fd.Ny, fd.Nz};
+  const int f[3] = {t.fi[t.fo[0] + I0], t.fi[t.fo[1] + I1], t.fi[t.fo[2] + I2]};
+  const int fnext = t.fi[t.fo[a] + I[a] + 1];
+  const int b = (a + 1) % 3, c = (a + 2) % 3;  // transverse axes
+  double sum = 0.0;
+  for (int db = -1; db <= 1; ++db) {
+    const int fb = f[b] + db;
+    if (fb < 0 || fb >= fN[b]) continue;
+    const double wb = pwgt(t, b, fb, I[b]);
+    if (wb == 0.0) continue;
+    for (int dc = -1; dc <= 1; ++dc) {
+      const int fc2 = f[c] + dc;
+      if (fc2 < 0 || fc2 >= fN[c]) continue;
+      const double wc = pwgt(t, c, fc2, I[c]);
+      if (wc == 0.0) continue;
+      int p[3];
+      p[a] = f[a];
+      p[b] = fb;
+      p[c] = fc2;
+      const double T1 = fcpl(fc, fd, a, p[0], p[1], p[2]);
+      double tv = T1;
+      if (fnext == f[a] + 2) {
+        p[a] = f[a] + 1;
+        const double T2 = fcpl(fc, fd, a, p[0], p[1], p[2]);
+        if (mode == 1) {
+          const double w = t.pw[t.po[a] + f[a] + 1];  // weight of the middle fine node on coarse node I[a]
+          tv = T1 * (1.0 - w) * (1.0 - w) + T2 * w * w;
+        } else {
+          tv = (T1 > 0.0 && T2 > 0.0) ? T1 * T2 / (T1 + T2) : 0.0;
+        }
+      }
+      sum += wb * wc * tv;
+    }
+  }
+  (void)cd;
+  return sum;
+}
+
+__global__ void k_coef_galerkin(const Coef64 *__restrict__ fc, Dims fd, Dims cd, AxisTab t, int mode,
+                                Coef64 *__restrict__ c64, Coef32 *__restrict__ c32, double *__restrict__ invd64,
+                                float *__restrict__ invd32, unsigned long long *__restrict__ lmax_bits) {
+  double gmax = 0.0;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < cd.N; n += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(n / ((long long)cd.Nx * cd.Ny));
+    const int r = (int)(n - (long long)K * cd.Nx * cd.Ny);
+    const int J = r / cd.Nx, I = r - J * cd.Nx;
+    const double cxp = I + 1 < cd.Nx ? ccpl(fc, fd, cd, t, mode, 0, I, J, K) : 0.0;
+    const double cxm = I > 0 ? ccpl(fc, fd, cd, t, mode, 0, I - 1, J, K) : 0.0;
+    const double cyp = J + 1 < cd.Ny ? ccpl(fc, fd, cd, t, mode, 1, I, J, K) : 0.0;
+    const double cym = J > 0 ? ccpl(fc, fd, cd, t, mode, 1, I, J - 1, K) : 0.0;
+    const double czp = K + 1 < cd.Nz ? ccpl(fc, fd, cd, t, mode, 2, I, J, K) : 0.0;
+    const double czm = K > 0 ? ccpl(fc, fd, cd, t, mode, 2, I, J, K - 1) : 0.0;
+    // lumped diagonal excess of the fine rows around the coarse node
+    const int fx = t.fi[t.fo[0] + I], fy = t.fi[t.fo[1] + J], fz = t.fi[t.fo[2] + K];
+    double ex = 0.0;
+    for (int dk = -1; dk <= 1; ++dk) {
+      const int k = fz + dk;
+      if (k < 0 || k >= fd.Nz) continue;
+      const double wz = pwgt(t, 2, k, K);
+      if (wz == 0.0) continue;
+      for (int dj = -1; dj <= 1; ++dj) {
+        const int j = fy + dj;
+        if (j < 0 || j >= fd.Ny) continue;
+        const double wy = pwgt(t, 1, j, J);
+        if (wy == 0.0) continue;
+        for (int di = -1; di <= 1; ++di) {
+          const int i = fx + di;
+          if (i < 0 || i >= fd.Nx) continue;
+          const double wx = pwgt(t, 0, i, I);
+          if (wx == 0.0) continue;
+          const long long m = i + (long long)fd.Nx * (j + (long long)fd.Ny * k);
+          const Coef64 v = fc[m];
+          double off = v.cx + v.cy + v.cz;
+          if (i > 0) off += fc[m - 1].cx;
+          if (j > 0) off += fc[m - fd.Nx].cy;
+          if (k > 0) off += fc[m - (long long)fd.Nx * fd.Ny].cz;
+          // the last node of an axis stores no + coupling of that axis
+          if (i + 1 >= fd.Nx) off -= v.cx;
+          if (j + 1 >= fd.Ny) off -= v.cy;
+          if (k + 1 >= fd.Nz) off -= v.cz;
+          ex += wx * wy * wz * fmax(v.d - off, 0.0);
+        }
+      }
+    }
+    const double off = cxp + cxm + cyp + cym + czp + czm;
+    const double dg = off + ex;
+    Coef64 c;
+    c.cx = cxp; c.cy = cyp; c.cz = czp; c.d = dg;
+    c64[n] = c;
+    Coef32 f;
+    f.cx = (float)cxp; f.cy = (float)cyp; f.cz = (float)czp; f.d = (float)dg;
+    c32[n] = f;
+    const double id = dg > 0.0 ? 1.0 / dg : 0.0;
+    invd64[n] = id;
+    invd32[n] = (float)id;
+    if (dg > 0.0) gmax = fmax(gmax, 1.0 + off / dg);
+  }
+  for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(gmax));
+}
+
 // ---------------------------------------------------------------- coarsest level
 __global__ void k_dense_assemble(const Coef64 *__restrict__ coef, Dims d, double *__restrict__ A) {
   const int N = (int)d.N;
@@ -607,6 +744,20 @@ void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cuda
   k_coef_build<<<count_launch(grid_flat(L.dims.N, g_n_sm)), TPB, 0, s>>>(L.d_sigma, L.d_h, L.nx, L.ny, L.nz, bf, robin,
                                                             L.d_coef64, L.d_coef32, L.d_invd64, L.d_invd32,
                                                             d_lmax_bits);
+}
+
+void coef_galerkin(const Level &f, const Level &c, int mode, unsigned long long *d_lmax_bits, cudaStream_t s) {
+  AxisTab t;
+  t.fi = f.d_r_fi;
+  t.pl = f.d_pl_idx;
+  t.pw = f.d_pl_w;
+  for (int a = 0; a < 3; ++a) {
+    t.fo[a] = f.r_off[a];
+    t.po[a] = f.pl_off[a];
+  }
+  k_coef_galerkin<<<count_launch(grid_flat(c.dims.N, g_n_sm)), TPB, 0, s>>>(f.d_coef64, f.dims, c.dims, t, mode,
+                                                                            c.d_coef64, c.d_coef32, c.d_invd64,
+                                                                            c.d_invd32, d_lmax_bits);
 }
 
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s) {

@@ -130,6 +130,13 @@ class DCEngine:
         an int 10 * rows + depth forces the slab layout."""
         check(lib().dc_set_staging(self._h, int(enable)))
 
+    def set_coarse_operator(self, mode):
+        """Coarse multigrid operators (``dc_set_coarse_operator``): "series" (default: formed from the finer
+        level, its couplings in series along each coarse edge), "galerkin" (collapsed P^T A P of the finer
+        level) or "rediscretised" (from the volume-averaged conductivity); applies at the next set_model."""
+        modes = {"rediscretised": 0, "galerkin": 1, "series": 2}
+        check(lib().dc_set_coarse_operator(self._h, modes[mode]))
+
     def set_model(self, sigma):
         sigma = _dev64(sigma, (self.nC,), "sigma")
         check(lib().dc_set_model(self._h, _ptr(sigma), _stream()))

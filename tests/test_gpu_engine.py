@@ -258,3 +258,45 @@ def test_fixed_iteration_solve_equals_adaptive(cuda, mode):
     mr, na = eng.check_fixed(ws, 20, mode)
     assert na == 0 and mr <= 1e-10
     torch.testing.assert_close(Xf, X, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("coarse", ["rediscretised", "galerkin", "series"])
+@pytest.mark.parametrize("kind", ["uniform", "padded", "odd"])
+def test_coarse_operator_modes_match_direct(cuda, coarse, kind):
+    """The coarse multigrid operators change the preconditioner only: with each of the three
+    (rediscretised, collapsed Galerkin, series from the finer level) a mixed solve of a model with
+    four decades of conductivity contrast reaches the direct solution, for the Robin and the
+    Neumann operator."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = _mesh(kind)
+    rng = np.random.default_rng(11)
+    sigma = 10 ** rng.uniform(-4, 0, mesh.n_cells)
+    A = _oracle(mesh, sigma).getA().tocsc()
+    lu = spla.splu(A)
+    B = rng.standard_normal((6, mesh.n_nodes))
+    X0 = lu.solve(B.T).T
+    eng = DCEngine(mesh.h, robin_face_weights(mesh))
+    eng.set_coarse_operator(coarse)
+    eng.set_model(torch.from_numpy(sigma).to(cuda))
+    X, info = eng.solve(torch.from_numpy(B).to(cuda), mode="mixed", rtol=1e-11)
+    assert info.status == 0 and info.max_rel_res <= 1e-11
+    err = np.linalg.norm(X.cpu().numpy() - X0, axis=1) / np.linalg.norm(X0, axis=1)
+    assert err.max() < 1e-8, (coarse, err.max(), info)
+    # Neumann (the reference pins row 0, simulation.py:535-540) through the simulation, against the oracle
+    from simpeg_gb300 import maps
+    from simpeg_gb300.resistivity import Simulation3DNodal
+
+    survey = Survey([sources.Pole([receivers.Pole(np.c_[[10.0, 20.0], [0.0, 5.0], [0.0, 0.0]])], np.r_[0.0, 0.0, 0.0])])
+    m = np.log(sigma)
+    orc = OracleDC3DNodal(mesh, survey, sigma_map=maps.ExpMap(mesh), bc_type="Neumann")
+    orc.set_model(m)
+    f = orc.fields()
+    sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), bc_type="Neumann", precision="mixed",
+                            rtol=1e-11)
+    sim.engine.set_coarse_operator(coarse)
+    phi = np.ravel(sim.fields(m)[:, "phi"])
+    f = np.ravel(f)
+    assert np.linalg.norm(phi - f) / np.linalg.norm(f) < 1e-7, coarse
