@@ -15,7 +15,8 @@
 // in fp32, so gradients keep fp32 relative accuracy), then streams the data,
 // accumulating W_d^2 J_dc^2 per cell in fp32 per thread (sums of positive
 // terms; the per-thread sums are combined in fp64).  The per-datum arithmetic
-// is fp32 (the Robin term of boundary cells aside), and the per-datum currents
+// is fp32, the Robin term of boundary cells included (the tile-centre values
+// and the cells' boundary weights are staged in fp32 once per tile), and the per-datum currents
 // and weights are converted to fp32 once per call, not once per tile: on this
 // part fp64 arithmetic and the fp64 <-> fp32 conversions issue at 1/64 of the
 // fp32 rate.  Cost: nE pole solves plus O(nD * nC) fp32 arithmetic with no J
@@ -28,7 +29,7 @@
 namespace dc {
 namespace {
 
-constexpr int JTPB = 512;
+constexpr int JTPB = 384;
 
 struct JtjData {
   const int *sa, *sb, *rm, *rn;  // electrode indices (-1 = none)
@@ -58,8 +59,10 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
                                                     double *__restrict__ diag) {
   extern __shared__ unsigned char smem_raw[];
   double *ref = reinterpret_cast<double *>(smem_raw);        // nE
-  float *dphi = reinterpret_cast<float *>(ref + nE);         // nE * 27
+  float *reff = reinterpret_cast<float *>(ref + nE);         // nE: ref in fp32
+  float *dphi = reff + nE;                                   // nE * 27
   __shared__ double red[JTPB / 32][8];
+  __shared__ float bwf[8][6];  // Robin face weights of the tile's cells (0 off the boundary)
   const double *hx = h, *hy = h + nx, *hz = h + nx + ny;
   const int Nx = nx + 1, Ny = ny + 1;
   const int tx = (nx + 1) / 2, ty = (ny + 1) / 2;
@@ -72,7 +75,25 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
     return (long long)i + (long long)Nx * (j + (long long)Ny * k);
   };
   const long long centre = node(1, 1, 1);
-  for (int k = threadIdx.x; k < nE; k += JTPB) ref[k] = phi[(long long)k * N + centre];
+  for (int k = threadIdx.x; k < nE; k += JTPB) {
+    ref[k] = phi[(long long)k * N + centre];
+    reff[k] = (float)ref[k];
+  }
+  if (threadIdx.x < 48) {
+    // face f of tile cell c: x-lo, x-hi, y-lo, y-hi, z-lo, z-hi
+    const int c = threadIdx.x / 6, f = threadIdx.x % 6;
+    const int ci = i0 + (c & 1), cj = j0 + ((c >> 1) & 1), ck = k0 + (c >> 2);
+    float w = 0.f;
+    if (bface && ci < nx && cj < ny && ck < nz) {
+      if (f == 0 && ci == 0) w = (float)bface[bo0 + cj + (long long)ny * ck];
+      if (f == 1 && ci == nx - 1) w = (float)bface[bo1 + cj + (long long)ny * ck];
+      if (f == 2 && cj == 0) w = (float)bface[bo2 + ci + (long long)nx * ck];
+      if (f == 3 && cj == ny - 1) w = (float)bface[bo3 + ci + (long long)nx * ck];
+      if (f == 4 && ck == 0) w = (float)bface[bo4 + ci + (long long)nx * cj];
+      if (f == 5 && ck == nz - 1) w = (float)bface[bo5 + ci + (long long)nx * cj];
+    }
+    bwf[c][f] = w;
+  }
   __syncthreads();
   for (int e = threadIdx.x; e < nE * 27; e += JTPB) {
     const int k = e / 27, j = e % 27;
@@ -132,22 +153,23 @@ __global__ void __launch_bounds__(JTPB) k_jtj_diag(const double *__restrict__ ph
         }
       float a = wx[c] * sx + wy[c] * sy + wz[c] * sz;
       if (bnd[c]) {
-        // Robin part: absolute potentials on the boundary faces of the cell
-        const double ur = (double)ia * ref[sa] + (sb >= 0 ? (double)ib * ref[sb] : 0.0);
-        const double lr = (double)wm * ref[rm] + (rn >= 0 ? (double)wn * ref[rn] : 0.0);
+        // Robin part: absolute potentials (tile-centre value + relative one) on the boundary faces of
+        // the cell, in fp32 like the rest of the per-datum arithmetic (weights and centre values staged
+        // in fp32 once per tile)
+        const float ur = ia * reff[sa] + (sb >= 0 ? ib * reff[sb] : 0.f);
+        const float lr = wm * reff[rm] + (rn >= 0 ? wn * reff[rn] : 0.f);
         auto ul = [&](int a2, int b2, int e2) {
           const int j = id(a2, b2, e2);
-          return ((double)u[j] + ur) * ((double)l[j] + lr);
+          return (u[j] + ur) * (l[j] + lr);
         };
-        const int ci = i0 + a0, cj = j0 + b0, ck = k0 + c0;
-        double ab = 0.0;
-        if (bnd[c] & 1) ab += bface[bo0 + cj + (long long)ny * ck] * (ul(0, 0, 0) + ul(0, 1, 0) + ul(0, 0, 1) + ul(0, 1, 1));
-        if (bnd[c] & 2) ab += bface[bo1 + cj + (long long)ny * ck] * (ul(1, 0, 0) + ul(1, 1, 0) + ul(1, 0, 1) + ul(1, 1, 1));
-        if (bnd[c] & 4) ab += bface[bo2 + ci + (long long)nx * ck] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 0, 1) + ul(1, 0, 1));
-        if (bnd[c] & 8) ab += bface[bo3 + ci + (long long)nx * ck] * (ul(0, 1, 0) + ul(1, 1, 0) + ul(0, 1, 1) + ul(1, 1, 1));
-        if (bnd[c] & 16) ab += bface[bo4 + ci + (long long)nx * cj] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 1, 0) + ul(1, 1, 0));
-        if (bnd[c] & 32) ab += bface[bo5 + ci + (long long)nx * cj] * (ul(0, 0, 1) + ul(1, 0, 1) + ul(0, 1, 1) + ul(1, 1, 1));
-        a += (float)ab;
+        float ab = 0.f;
+        if (bnd[c] & 1) ab += bwf[c][0] * (ul(0, 0, 0) + ul(0, 1, 0) + ul(0, 0, 1) + ul(0, 1, 1));
+        if (bnd[c] & 2) ab += bwf[c][1] * (ul(1, 0, 0) + ul(1, 1, 0) + ul(1, 0, 1) + ul(1, 1, 1));
+        if (bnd[c] & 4) ab += bwf[c][2] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 0, 1) + ul(1, 0, 1));
+        if (bnd[c] & 8) ab += bwf[c][3] * (ul(0, 1, 0) + ul(1, 1, 0) + ul(0, 1, 1) + ul(1, 1, 1));
+        if (bnd[c] & 16) ab += bwf[c][4] * (ul(0, 0, 0) + ul(1, 0, 0) + ul(0, 1, 0) + ul(1, 1, 0));
+        if (bnd[c] & 32) ab += bwf[c][5] * (ul(0, 0, 1) + ul(1, 0, 1) + ul(0, 1, 1) + ul(1, 1, 1));
+        a += ab;
       }
       const float jv = sg[c] * a;
       acc[c] += w2 * jv * jv;
@@ -180,14 +202,14 @@ namespace dc {
 int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD, const int *sa, const int *sb,
                     const double *ia, const double *ib, const int *rm, const int *rn, const double *wm,
                     const double *wn, const double *w2, const double *dsig, double *diag, cudaStream_t stream) {
-  const size_t smem = (size_t)nE * (sizeof(double) + 27 * sizeof(float));
+  const size_t smem = (size_t)nE * (sizeof(double) + 28 * sizeof(float));
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t static_smem = 8 * 8 * (JTPB / 32);
+  const size_t static_smem = 8 * 8 * (JTPB / 32) + 8 * 6 * sizeof(float);
   if (smem + static_smem > (size_t)maxsm) {
     last_error() = "dc_jtj_diag: " + std::to_string(nE) + " unique electrodes exceed the shared-memory tile (max " +
-                   std::to_string((maxsm - static_smem) / (sizeof(double) + 27 * sizeof(float))) + ")";
+                   std::to_string((maxsm - static_smem) / (sizeof(double) + 28 * sizeof(float))) + ")";
     return DC_ERR_ARG;
   }
   cudaError_t e = cudaFuncSetAttribute(k_jtj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -655,7 +655,7 @@ class Simulation3DNodal:
             return None
         uniq, t = tab
         nE = uniq.shape[0]
-        if nE * 116 > 220 * 1024:
+        if nE * 120 > 220 * 1024:  # the kernel's shared-memory tile: 8 + 4 + 27 * 4 bytes per electrode
             return None
         self._ensure_model()
         dev = self.device
