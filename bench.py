@@ -73,6 +73,8 @@ def _args():
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--profile-solve", action="store_true",
                     help="set up the forward workload, run one mixed solve and exit (for ncu captures; no timing)")
+    ap.add_argument("--sens-full-survey", action="store_true",
+                    help="with --profile-sens: the full Gauss-Newton survey on a 64x64x32-cell mesh")
     ap.add_argument("--profile-sens", action="store_true",
                     help="a reduced Gauss-Newton workload (96x96x48 cells, --sources dipoles): one getJtJdiag and one "
                          "Jtvec, nothing else (for ncu captures of the sensitivity kernels; no timing)")
@@ -1253,7 +1255,8 @@ def run_profile_solve(args):
 
 def run_profile_sens(args):
     """One getJtJdiag (electrode reciprocity: pole solves + k_jtj_diag) and one Jtvec (adjoint solve +
-    k_edge_products + k_cell_gradient) on a 96x96x48-cell Gauss-Newton-type workload."""
+    k_edge_products + k_cell_gradient) on a 96x96x48-cell Gauss-Newton-type workload (with
+    ``--sens-full-survey``: the Gauss-Newton workload's survey on a 64x64x32-cell mesh)."""
     import torch
 
     from simpeg_gb300 import maps, workloads
@@ -1261,8 +1264,12 @@ def run_profile_sens(args):
     from simpeg_gb300.resistivity.survey import Survey
 
     torch.cuda.set_device(0)
-    mesh, m_true, m0, survey = workloads.gauss_newton(seed=4, n_lines=8, src_per_line=16, n_rx=24, ncore_xy=80,
-                                                     ncore_z=40)
+    if args.sens_full_survey:
+        # the Gauss-Newton survey (512 dipoles x 48 receivers, 1,312 electrodes) on a 64x64x32-cell mesh
+        mesh, m_true, m0, survey = workloads.gauss_newton(seed=4, ncore_xy=48, ncore_z=24)
+    else:
+        mesh, m_true, m0, survey = workloads.gauss_newton(seed=4, n_lines=8, src_per_line=16, n_rx=24, ncore_xy=80,
+                                                         ncore_z=40)
     if args.sources:
         survey = Survey(survey.source_list[:args.sources])
     sim = Simulation3DNodal(mesh, survey=survey, sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
