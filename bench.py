@@ -68,7 +68,7 @@ def _args():
     ap.add_argument("--n-side", type=int, default=16, help="sources per side of the surface grid")
     ap.add_argument("--sources", type=int, default=0, help="use only the first N sources (profiling runs)")
     ap.add_argument("--workload", default="forward",
-                    choices=["forward", "block", "differentiation", "gauss_newton", "batched", "cc"],
+                    choices=["forward", "block", "differentiation", "gauss_newton", "batched", "cc", "serving"],
                     help="forward: the headline 1M-cell line; differentiation: the 96x96x48 gradient checks")
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--profile-solve", action="store_true",
@@ -1135,6 +1135,134 @@ def run_cc(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args):
+    """Continuous-batching serving of dpred requests (``simpeg_gb300.serving.DCServer``, lane mode).
+
+    96x96x48 cells (the differentiation mesh), four models, 96 requests of 8-32 dipole sources (30
+    receivers each), chosen and sized by a seeded generator.  Each request is a host model and a
+    host survey in and host data out, so the whole run is end to end.  ``value``: source-solves/s
+    with every request queued at once (the server's capacity, first submission to last answer);
+    ``poisson_70pct``: the same requests as a Poisson stream offering 70 % of that capacity, with
+    submit-to-answer latency percentiles.  The same
+    requests solved one after another through ``Simulation3DNodal.dpred`` (one simulation per model,
+    its operator built once, the request's survey swapped in: a request queue without batching) ride
+    along, and every request's data are compared with that sequential result.  Prints one JSON line.
+    """
+    import torch
+
+    from simpeg_gb300 import maps, workloads
+    from simpeg_gb300.engine import kernel_launches
+    from simpeg_gb300.resistivity import Simulation3DNodal
+    from simpeg_gb300.resistivity.survey import Survey
+    from simpeg_gb300.serving import DCServer
+
+    mesh, m_base, survey_all = workloads.differentiation(seed=2)
+    rng = np.random.default_rng(31)
+    models = [m_base + 0.3 * rng.standard_normal(m_base.size) for _ in range(4)]
+    n_req = 96
+    reqs = []
+    for _ in range(n_req):
+        k = int(rng.integers(8, 33))
+        start = int(rng.integers(0, survey_all.nSrc - k + 1))
+        reqs.append((int(rng.integers(0, len(models))), Survey(survey_all.source_list[start:start + k])))
+    total_src = sum(r[1].nSrc for r in reqs)
+    torch.cuda.set_device(0)
+
+    # sequential: one request after another through the simulation API, one simulation per model kept
+    # set up (its model's operator built once, warmed), the request's survey swapped in
+    sims = [Simulation3DNodal(mesh, survey=reqs[0][1], sigmaMap=maps.ExpMap(mesh), precision="mixed", rtol=RTOL)
+            for _ in models]
+    for sim, m in zip(sims, models):
+        sim.dpred(m)
+    torch.cuda.synchronize()
+
+    def one(mi, sv):
+        sims[mi].survey = sv
+        return sims[mi].dpred(models[mi])
+
+    t0 = time.perf_counter()
+    seq = [one(mi, sv) for mi, sv in reqs]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    del sims
+    torch.cuda.empty_cache()
+
+    def serve(srv, gaps):
+        """Submit the requests after the given gaps; returns (seconds, answers, submit-to-answer latencies)."""
+        t0 = time.perf_counter()
+        futs, t_sub = [], []
+        for (mi, sv), g in zip(reqs, gaps):
+            if g > 0:
+                time.sleep(g)
+            t_sub.append(time.perf_counter())
+            futs.append(srv.submit(models[mi], sv))
+        out, lat = [], []
+        for f, ts in zip(futs, t_sub):
+            out.append(f.result(timeout=1800))
+            lat.append(time.perf_counter() - ts)
+        return time.perf_counter() - t0, out, lat
+
+    with DCServer(mesh, slots=2, max_rhs=128, rtol=RTOL) as srv:
+        # warm-up request per slot (workspaces and kernels), untimed
+        for f in [srv.submit(models[i], reqs[i][1]) for i in range(2)]:
+            f.result(timeout=600)
+        # capacity: every request queued at once
+        for sl in srv.slots:
+            sl.engine.stencil_timing(True)
+        n0 = kernel_launches()
+        with Clocks(0) as clk:
+            t_srv, out, lat_burst = serve(srv, np.zeros(n_req))
+        launches = kernel_launches() - n0
+        st = [sl.engine.stencil_timing(False) for sl in srv.slots]
+        kinds = {}
+        for sl in srv.slots:
+            for k, (c, t, b) in sl.engine.stencil_timing_kinds().items():
+                kc, kt, kb = kinds.get(k, (0, 0.0, 0.0))
+                kinds[k] = (kc + c, kt + t, kb + b)
+        # latency: Poisson arrivals offering 70 % of that capacity
+        mean_gap = t_srv / n_req / 0.7
+        t_poisson, out_p, lat = serve(srv, rng.exponential(mean_gap, n_req))
+    ms = sum(a for a, _, _ in st)
+    n = sum(b for _, b, _ in st)
+    by = sum(c for _, _, c in st)
+    rel = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(out + out_p, seq + seq)]
+    lat_ms = np.array(lat) * 1e3
+    line = {"metric": "served source-solves/s, continuous batching (DCServer lane mode), 96 requests on 96x96x48 cells",
+            "value": total_src / t_srv, "unit": "source-solves/s", "n_gpus": 1, "steps": 1, "warmup": 2,
+            "ms_per_step": t_srv * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 refinement",
+            "data": "synthetic (seeded Gaussian random fields, 4 models; 96 requests of 8-32 dipoles x 30 receivers, "
+                    "Poisson arrivals)",
+            "config": {"workload": "dc3d_serving_96x96x48", "mesh_cells": list(mesh.shape_cells),
+                       "nodes": int(mesh.n_nodes), "requests": n_req, "sources": total_src, "models": len(models),
+                       "slots": 2, "lanes_per_slot": 128, "rtol": RTOL,
+                       "value": "all requests queued at once (capacity)"},
+            "poisson_70pct": {"mean_arrival_gap_ms": mean_gap * 1e3, "seconds": t_poisson,
+                              "source_solves_per_s": total_src / t_poisson,
+                              "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                                             "p90": float(np.percentile(lat_ms, 90)),
+                                             "p99": float(np.percentile(lat_ms, 99)), "max": float(lat_ms.max())},
+                              "sequential_request_ms": {"mean": t_seq / n_req * 1e3}},
+            "burst_latency_ms": {"p50": float(np.percentile(np.array(lat_burst) * 1e3, 50)),
+                                 "max": float(np.max(lat_burst) * 1e3)},
+            "sequential": {"seconds": t_seq, "source_solves_per_s": total_src / t_seq,
+                           "path": "Simulation3DNodal.dpred(m) per request, one after another, one simulation per "
+                                   "model (operator built once), the request's survey swapped in"},
+            "speedup_vs_sequential": t_seq / t_srv,
+            "rel_err_vs_sequential": {"max": max(rel), "median": float(np.median(rel))},
+            "clocks": clk.summary(), "gpu_launches": launches,
+            "roofline": _stencil_roofline(ms, n, by, kinds or None, what="fine-level Chebyshev steps of the "
+                                                                          "slots' lane sweeps", scaled_traffic=True),
+            "e2e": {"value": total_src / t_srv, "unit": "source-solves/s",
+                    "h2d_bytes_per_step": int(sum(mesh.n_cells * 8 for _ in reqs)),
+                    "d2h_bytes_per_step": int(sum(sv.nD * 8 for _, sv in reqs)),
+                    "path": "DCServer.submit(host model, host survey) -> Future -> host data, every request"}}
+    if not args.no_cpu_baseline:
+        cb = _cpu_baseline(mesh, np.exp(models[0]), survey_all)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+
+
 def run_block(args):
     """32x32x16 cells of 10 m (18,513 nodes), 0.01 S/m with a 0.1 and a 0.001 S/m block, dipole-dipole
     line of 20 sources x 15 receivers (300 data): the size where the reference's default direct solver
@@ -1294,6 +1422,8 @@ def main():
         return run_gauss_newton(args)
     if args.workload == "cc" and args.impl != "reference":
         return run_cc(args)
+    if args.workload == "serving" and args.impl != "reference":
+        return run_serving(args)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "differentiation":

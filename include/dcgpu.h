@@ -368,6 +368,12 @@ int dc_lanes_state(dc_lanes *s, int *active, double *rel_res, void *stream);
 int dc_lanes_fetch(dc_lanes *s, const int *lanes_dev, int n, double *x_dev, void *stream);
 void dc_lanes_close(dc_lanes *s);
 
+/* Sweeps cover only the lanes [0, n_lanes) from now on, rounded up to whole
+ * RHS blocks (0 or the capacity: all lanes).  The caller promises that no lane
+ * beyond is active; their state is left untouched.  Lanes handed out lowest
+ * first keep a lightly loaded session's sweeps to the blocks in use. */
+int dc_lanes_set_extent(dc_lanes *s, int n_lanes);
+
 /* Number of CUDA kernels this library has launched since it was loaded
  * (all handles, all threads).  Instrumentation; no reference counterpart. */
 long long dc_kernel_launches(void);

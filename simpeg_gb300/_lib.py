@@ -103,6 +103,7 @@ _SIG = {
     "dc_lanes_open": (C.c_int, [_VP, C.c_int, C.c_double, C.c_int, _VP, C.c_size_t, C.POINTER(_VP),
                                 C.POINTER(C.c_int)]),
     "dc_lanes_load": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),
+    "dc_lanes_set_extent": (C.c_int, [_VP, C.c_int]),
     "dc_lanes_sweep": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), _VP]),
     "dc_lanes_state": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_double), _VP]),
     "dc_lanes_fetch": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),

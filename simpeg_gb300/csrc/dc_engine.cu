@@ -961,12 +961,15 @@ int solve_dispatch(dc_handle *h, int mode, const double *b, double *x, int k, do
 // branch): inner fp32 PCG on the active lanes to their own tolerances,
 // x += d, double-float residual, new per-lane flags and tolerances.
 template <int KB>
-int lanes_sweep_kb(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int *it, cudaStream_t s) {
+int lanes_sweep_kb(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int nb_use, int *it,
+                   cudaStream_t s) {
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
-  const int nb = w.nb, Kp = w.Kp, gx = w.gx;
-  float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
-  float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
+  // only the leading nb_use RHS blocks hold active lanes (the caller's promise): the sweep's kernels,
+  // partial sums and flags cover those; the other lanes' state is left as it is
+  const int nb = nb_use > 0 && nb_use < w.nb ? nb_use : w.nb, Kp = nb * KB, gx = w.gx;
+  float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * w.Kp;
+  float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * w.Kp;
   CK(cudaMemsetAsync(w.sc.status, 0, sizeof(int), s));
   CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
   int rc;
@@ -988,14 +991,15 @@ int lanes_sweep_kb(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int
   return 0;
 }
 
-int lanes_sweep(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int *it, cudaStream_t s) {
+int lanes_sweep(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int inner_cap, int nb_use, int *it,
+                cudaStream_t s) {
   switch (w.KB) {
-    case 32: return lanes_sweep_kb<32>(h, w, rtol, inner_rtol, inner_cap, it, s);
-    case 16: return lanes_sweep_kb<16>(h, w, rtol, inner_rtol, inner_cap, it, s);
-    case 8: return lanes_sweep_kb<8>(h, w, rtol, inner_rtol, inner_cap, it, s);
-    case 4: return lanes_sweep_kb<4>(h, w, rtol, inner_rtol, inner_cap, it, s);
-    case 2: return lanes_sweep_kb<2>(h, w, rtol, inner_rtol, inner_cap, it, s);
-    default: return lanes_sweep_kb<1>(h, w, rtol, inner_rtol, inner_cap, it, s);
+    case 32: return lanes_sweep_kb<32>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
+    case 16: return lanes_sweep_kb<16>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
+    case 8: return lanes_sweep_kb<8>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
+    case 4: return lanes_sweep_kb<4>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
+    case 2: return lanes_sweep_kb<2>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
+    default: return lanes_sweep_kb<1>(h, w, rtol, inner_rtol, inner_cap, nb_use, it, s);
   }
 }
 
@@ -1009,6 +1013,7 @@ struct dc_lanes {
   void *own = nullptr;
   double rtol = 1e-9, inner_rtol = 3e-5;
   int inner_maxit = 200;
+  int nb_use = 0;  // RHS blocks the sweeps cover (0: all; dc_lanes_set_extent)
 };
 
 // ====================================================================== C ABI
@@ -1701,12 +1706,20 @@ int dc_lanes_load(dc_lanes *L, const int *lanes_dev, int n, const double *b_dev,
   return 0;
 }
 
+int dc_lanes_set_extent(dc_lanes *L, int n_lanes) {
+  if (!L) return fail(DC_ERR_ARG, "NULL session");
+  if (n_lanes < 0) return fail(DC_ERR_ARG, "negative lane extent");
+  const int KB = L->w.KB;
+  L->nb_use = (n_lanes <= 0 || n_lanes >= L->w.Kp) ? 0 : (n_lanes + KB - 1) / KB;
+  return 0;
+}
+
 int dc_lanes_sweep(dc_lanes *L, int *n_active, int *iterations, void *stream) {
   if (!L) return fail(DC_ERR_ARG, "NULL session");
   cudaStream_t s = (cudaStream_t)stream;
   dc_handle *h = L->h;
   int it = 0;
-  int rc = lanes_sweep(h, L->w, L->rtol, L->inner_rtol, L->inner_maxit, &it, s);
+  int rc = lanes_sweep(h, L->w, L->rtol, L->inner_rtol, L->inner_maxit, L->nb_use, &it, s);
   if (rc) return rc == DC_ERR_BREAKDOWN ? fail(rc, "PCG breakdown in a lane session") : rc;
   CK(cudaMemcpyAsync(h->h_mail, L->w.sc.n_active_out, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev, s));

@@ -318,6 +318,10 @@ class LaneSession:
         idx = self._idx(lanes)
         check(lib().dc_lanes_load(self._s, _ptr(idx), len(lanes), _ptr(B), _stream()))
 
+    def set_extent(self, n_lanes):
+        """Sweeps cover lanes [0, n_lanes) only (whole RHS blocks; 0: all); no lane beyond may be active."""
+        check(lib().dc_lanes_set_extent(self._s, int(n_lanes)))
+
     def sweep(self):
         """One refinement sweep of the active lanes; returns (lanes still active, inner iterations)."""
         n, it = C.c_int(), C.c_int()

@@ -159,12 +159,13 @@ class _CudaLanes:
             Q.zero_()
             self.session.load(lanes, Q)
 
-    def sweep(self):
+    def sweep(self, extent=0):
         import torch
 
         with torch.cuda.stream(self.stream):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
+            self.session.set_extent(extent)
             out = self.session.sweep()
             e1.record()
         return out, (e0, e1)
@@ -361,7 +362,9 @@ class DCServer:
                     self._release(slot, r)
             if not slot.running:
                 continue
-            (n_active, _), evs = be.sweep()
+            # lanes are handed out lowest first: the sweep covers the blocks up to the highest lane in use
+            extent = 1 + max(l for r in slot.running for l in r.lanes)
+            (n_active, _), evs = be.sweep(extent)
             slot.sweeps += 1
             if evs is not None:
                 slot.sweep_events.append(evs)

@@ -60,7 +60,7 @@ def test_superlu_extrapolation_passes_through_the_probes(bench):
 
 
 def test_workload_choices(bench, monkeypatch):
-    for w in ("forward", "block", "differentiation", "gauss_newton", "batched", "cc"):
+    for w in ("forward", "block", "differentiation", "gauss_newton", "batched", "cc", "serving"):
         monkeypatch.setattr(sys, "argv", ["bench.py", "--workload", w])
         assert bench._args().workload == w
     monkeypatch.setattr(sys, "argv", ["bench.py"])

@@ -117,7 +117,9 @@ class FakeLanes:
     def clear(self, lanes):
         self.left[lanes] = 0
 
-    def sweep(self):
+    def sweep(self, extent=0):
+        # the scheduler promises that no lane at or beyond the extent is active
+        assert extent <= 0 or not np.any(self.left[extent:] > 0), "an active lane lies beyond the sweep extent"
         time.sleep(self.delay)
         self.left[self.left > 0] -= 1
         return (int((self.left > 0).sum()), 1), None
