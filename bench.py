@@ -1141,9 +1141,9 @@ def run_serving(args):
     96x96x48 cells (the differentiation mesh), four models, 96 requests of 8-32 dipole sources (30
     receivers each), chosen and sized by a seeded generator.  Each request is a host model and a
     host survey in and host data out, so the whole run is end to end.  ``value``: source-solves/s
-    with every request queued at once (the server's capacity, first submission to last answer);
-    ``poisson_70pct``: the same requests as a Poisson stream offering 70 % of that capacity, with
-    submit-to-answer latency percentiles.  The same
+    with every request queued at once (the server's capacity, first submission to last answer) and
+    one slot per model; ``by_slots``: that capacity, and the same requests as a Poisson stream
+    offering 70 % of it with submit-to-answer latency percentiles, for 2 and 4 slots.  The same
     requests solved one after another through ``Simulation3DNodal.dpred`` (one simulation per model,
     its operator built once, the request's survey swapped in: a request queue without batching) ride
     along, and every request's data are compared with that sequential result.  Prints one JSON line.
@@ -1202,58 +1202,62 @@ def run_serving(args):
             lat.append(time.perf_counter() - ts)
         return time.perf_counter() - t0, out, lat
 
-    with DCServer(mesh, slots=2, max_rhs=128, rtol=RTOL) as srv:
-        # warm-up request per slot (workspaces and kernels), untimed
-        for f in [srv.submit(models[i], reqs[i][1]) for i in range(2)]:
-            f.result(timeout=600)
-        # capacity: every request queued at once
-        for sl in srv.slots:
-            sl.engine.stencil_timing(True)
-        n0 = kernel_launches()
-        with Clocks(0) as clk:
-            t_srv, out, lat_burst = serve(srv, np.zeros(n_req))
-        launches = kernel_launches() - n0
-        st = [sl.engine.stencil_timing(False) for sl in srv.slots]
-        kinds = {}
-        for sl in srv.slots:
-            for k, (c, t, b) in sl.engine.stencil_timing_kinds().items():
-                kc, kt, kb = kinds.get(k, (0, 0.0, 0.0))
-                kinds[k] = (kc + c, kt + t, kb + b)
-        # latency: Poisson arrivals offering 70 % of that capacity
-        mean_gap = t_srv / n_req / 0.7
-        t_poisson, out_p, lat = serve(srv, rng.exponential(mean_gap, n_req))
-    ms = sum(a for a, _, _ in st)
-    n = sum(b for _, b, _ in st)
-    by = sum(c for _, _, c in st)
-    rel = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(out + out_p, seq + seq)]
-    lat_ms = np.array(lat) * 1e3
-    line = {"metric": "served source-solves/s, continuous batching (DCServer lane mode), 96 requests on 96x96x48 cells",
-            "value": total_src / t_srv, "unit": "source-solves/s", "n_gpus": 1, "steps": 1, "warmup": 2,
-            "ms_per_step": t_srv * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 inner / f64 refinement",
-            "data": "synthetic (seeded Gaussian random fields, 4 models; 96 requests of 8-32 dipoles x 30 receivers, "
-                    "Poisson arrivals)",
-            "config": {"workload": "dc3d_serving_96x96x48", "mesh_cells": list(mesh.shape_cells),
-                       "nodes": int(mesh.n_nodes), "requests": n_req, "sources": total_src, "models": len(models),
-                       "slots": 2, "lanes_per_slot": 128, "rtol": RTOL,
-                       "value": "all requests queued at once (capacity)"},
-            "poisson_70pct": {"mean_arrival_gap_ms": mean_gap * 1e3, "seconds": t_poisson,
-                              "source_solves_per_s": total_src / t_poisson,
-                              "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
-                                             "p90": float(np.percentile(lat_ms, 90)),
-                                             "p99": float(np.percentile(lat_ms, 99)), "max": float(lat_ms.max())},
-                              "sequential_request_ms": {"mean": t_seq / n_req * 1e3}},
+    by_slots = {}
+    for n_slots in (2, 4):
+        with DCServer(mesh, slots=n_slots, max_rhs=128, rtol=RTOL) as srv:
+            # warm-up request per slot (workspaces and kernels), untimed
+            for f in [srv.submit(models[i % len(models)], reqs[i][1]) for i in range(n_slots)]:
+                f.result(timeout=600)
+            # capacity: every request queued at once
+            for sl in srv.slots:
+                sl.engine.stencil_timing(True)
+            n0 = kernel_launches()
+            with Clocks(0) as clk:
+                t_srv, out, lat_burst = serve(srv, np.zeros(n_req))
+            launches = kernel_launches() - n0
+            st = [sl.engine.stencil_timing(False) for sl in srv.slots]
+            kinds = {}
+            for sl in srv.slots:
+                for k, (c, t, b) in sl.engine.stencil_timing_kinds().items():
+                    kc, kt, kb = kinds.get(k, (0, 0.0, 0.0))
+                    kinds[k] = (kc + c, kt + t, kb + b)
+            # latency: Poisson arrivals offering 70 % of that capacity
+            mean_gap = t_srv / n_req / 0.7
+            t_poisson, out_p, lat = serve(srv, rng.exponential(mean_gap, n_req))
+        lat_ms = np.array(lat) * 1e3
+        by_slots[n_slots] = {
+            "source_solves_per_s": total_src / t_srv, "seconds": t_srv,
             "burst_latency_ms": {"p50": float(np.percentile(np.array(lat_burst) * 1e3, 50)),
                                  "max": float(np.max(lat_burst) * 1e3)},
+            "poisson_70pct": {"mean_arrival_gap_ms": mean_gap * 1e3, "source_solves_per_s": total_src / t_poisson,
+                              "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                                             "p90": float(np.percentile(lat_ms, 90)),
+                                             "p99": float(np.percentile(lat_ms, 99)), "max": float(lat_ms.max())}},
+            "rel_err_vs_sequential_max": max(float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_))
+                                             for a_, b_ in zip(out + out_p, seq + seq))}
+    ms = sum(x for x, _, _ in st)
+    n = sum(x for _, x, _ in st)
+    by = sum(x for _, _, x in st)
+    best = by_slots[4]
+    line = {"metric": "served source-solves/s, continuous batching (DCServer lane mode), 96 requests on 96x96x48 cells",
+            "value": best["source_solves_per_s"], "unit": "source-solves/s", "n_gpus": 1, "steps": 1, "warmup": 4,
+            "ms_per_step": best["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 refinement",
+            "data": "synthetic (seeded Gaussian random fields, 4 models; 96 requests of 8-32 dipoles x 30 receivers)",
+            "config": {"workload": "dc3d_serving_96x96x48", "mesh_cells": list(mesh.shape_cells),
+                       "nodes": int(mesh.n_nodes), "requests": n_req, "sources": total_src, "models": len(models),
+                       "slots": 4, "lanes_per_slot": 128, "rtol": RTOL,
+                       "value": "4 slots (one per model), all requests queued at once (capacity)"},
+            "by_slots": {str(k): v for k, v in by_slots.items()},
             "sequential": {"seconds": t_seq, "source_solves_per_s": total_src / t_seq,
                            "path": "Simulation3DNodal.dpred(m) per request, one after another, one simulation per "
                                    "model (operator built once), the request's survey swapped in"},
-            "speedup_vs_sequential": t_seq / t_srv,
-            "rel_err_vs_sequential": {"max": max(rel), "median": float(np.median(rel))},
+            "speedup_vs_sequential": t_seq / best["seconds"],
+            "rel_err_vs_sequential_max": max(v["rel_err_vs_sequential_max"] for v in by_slots.values()),
             "clocks": clk.summary(), "gpu_launches": launches,
             "roofline": _stencil_roofline(ms, n, by, kinds or None, what="fine-level Chebyshev steps of the "
                                                                           "slots' lane sweeps", scaled_traffic=True),
-            "e2e": {"value": total_src / t_srv, "unit": "source-solves/s",
+            "e2e": {"value": best["source_solves_per_s"], "unit": "source-solves/s",
                     "h2d_bytes_per_step": int(sum(mesh.n_cells * 8 for _ in reqs)),
                     "d2h_bytes_per_step": int(sum(sv.nD * 8 for _, sv in reqs)),
                     "path": "DCServer.submit(host model, host survey) -> Future -> host data, every request"}}
