@@ -816,7 +816,9 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
   const int nb = w.nb, Kp = w.Kp, gx = w.gx;
-  pack_colmajor<double>(b, N, k, KB, nb, w.B64, s);
+  // the mixed Robin solve splits b straight from the column-major input (below); the others pack it
+  const bool fused_split = mode != DC_MODE_FP64 && h->robin;
+  if (!fused_split) pack_colmajor<double>(b, N, k, KB, nb, w.B64, s);
   if (!h->robin) {
     // Neumann: the reference pins row 0 of A to the identity
     // (resistivity/simulation.py:535-540).  Its solution solves the symmetric
@@ -849,7 +851,11 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     // Refinement in double-float: b and x as (hi, lo) fp32 pairs in the B64-sized regions R64 and X64.
     float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * Kp;
     float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * Kp;
-    split_df(w.B64, (long long)N * Kp, bh, bl, w.r32, s);  // also r32 = fp32(b), the first residual
+    // also r32 = fp32(b), the first residual
+    if (fused_split)
+      pack_split_df(b, N, k, KB, nb, bh, bl, w.r32, s);
+    else
+      split_df(w.B64, (long long)N * Kp, bh, bl, w.r32, s);
     // |b|^2 from the fp32 copy of b (the stopping test needs it to ~1e-6 relatively; an fp64 dot runs at
     // the fp64 rate), initial outer flags
     Ops<float, float, KB>::dot(N, nb, w.r32, w.r32, w.sc.part_b, gx, s);

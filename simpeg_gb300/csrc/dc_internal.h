@@ -196,6 +196,9 @@ void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst
 template <typename T>
 void unpack_colmajor(const T *src, long long N, int K, int KB, double *dst, cudaStream_t s);
 void unpack_colmajor_df(const float *hi, const float *lo, long long N, int K, int KB, double *dst, cudaStream_t s);
+// pack_colmajor and split_df in one pass (column-major fp64 -> RHS-blocked (hi, lo) pairs and r32 = hi)
+void pack_split_df(const double *src, long long N, int K, int KB, int nb, float *hi, float *lo, float *r32,
+                   cudaStream_t s);
 
 // ---- dc_sens.cu -------------------------------------------------------------
 void csr_spmv(int nrows, const long long *rowptr, const long long *in_idx, const double *w, const double *x,

@@ -611,6 +611,44 @@ __global__ void __launch_bounds__(TT *TR) k_pack(const double *__restrict__ src,
   }
 }
 
+// (double)v split into fp32 (hi, lo) with the fp64 instructions, in a call of its
+// own (kept out of the common path of k_pack_split_df).
+__device__ __noinline__ void split_fp64_call(double v, float &h, float &l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// k_pack and the double-float split in one pass: column-major fp64 (K, N) ->
+// RHS-blocked fp32 (hi, lo) pairs (split_df_bits, the fp64 instructions only
+// for values outside its range) and r32 = hi, lanes r >= K zero.
+__global__ void __launch_bounds__(TT *TR) k_pack_split_df(const double *__restrict__ src, long long N, int K, int KB,
+                                                         int Kp, float *__restrict__ hi, float *__restrict__ lo,
+                                                         float *__restrict__ r32) {
+  __shared__ double tile[TT][TT + 1];
+  const long long n0 = (long long)blockIdx.x * TT;
+  const int r0 = blockIdx.y * TT;
+  for (int i = threadIdx.y; i < TT; i += TR) {
+    const int r = r0 + i;
+    const long long n = n0 + threadIdx.x;
+    tile[i][threadIdx.x] = (r < K && n < N) ? src[(long long)r * N + n] : 0.0;
+  }
+  __syncthreads();
+  const int r = r0 + threadIdx.x;
+  if (r >= Kp) return;
+  const int b = r / KB, l = r % KB;
+  for (int j = threadIdx.y; j < TT; j += TR) {
+    const long long n = n0 + j;
+    if (n < N) {
+      float h, w;
+      if (__builtin_expect(!split_df_bits(tile[threadIdx.x][j], h, w), 0)) split_fp64_call(tile[threadIdx.x][j], h, w);
+      const long long e = ((long long)b * N + n) * KB + l;
+      hi[e] = h;
+      lo[e] = w;
+      if (r32) r32[e] = h;
+    }
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(TT *TR) k_unpack(const T *__restrict__ src, long long N, int K, int KB,
                                                     double *__restrict__ dst) {
@@ -796,6 +834,13 @@ void pack_colmajor(const double *src, long long N, int K, int KB, int nb, T *dst
   const int Kp = KB * nb;
   const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((Kp + TT - 1) / TT));
   k_pack<T><<<count_launch(grid), dim3(TT, TR), 0, s>>>(src, N, K, KB, Kp, dst);
+}
+
+void pack_split_df(const double *src, long long N, int K, int KB, int nb, float *hi, float *lo, float *r32,
+                   cudaStream_t s) {
+  const int Kp = KB * nb;
+  const dim3 grid((unsigned)((N + TT - 1) / TT), (unsigned)((Kp + TT - 1) / TT));
+  k_pack_split_df<<<count_launch(grid), dim3(TT, TR), 0, s>>>(src, N, K, KB, Kp, hi, lo, r32);
 }
 
 void unpack_colmajor_df(const float *hi, const float *lo, long long N, int K, int KB, double *dst, cudaStream_t s) {
