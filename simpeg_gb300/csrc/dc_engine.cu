@@ -826,7 +826,9 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     // rows) (the compatible RHS), shifted so that u_0 = b_0.
     neumann_rhs(b, N, k, KB, w.B64, w.sc.rr64, s);
   }
-  CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));
+  // the host-driven mixed solve writes its first correction into x instead of adding it to zeros
+  bool first_sweep = mode != DC_MODE_FP64 && !device;
+  if (!first_sweep) CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));
   CK(cudaMemsetAsync(w.sc.loop, 0, 4 * sizeof(int), s));
   CK(cudaMemsetAsync(w.sc.status, 0, sizeof(int), s));  // read by the device-loop conditions before the first PCG
   int total_it = 0, outer = 0, status = 0;
@@ -878,7 +880,12 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
         rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
-      ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, so);
+      if (first_sweep) {
+        ir_set_df((long long)N * Kp, xh, xl, w.d32, so);
+        first_sweep = false;
+      } else {
+        ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, so);
+      }
       ir_residual_df<KB>(F, h->d_cdf_hi, h->d_cdf_lo, bh, bl, xh, xl, w.r32, nb, w.sc.active_out, w.sc.part_a, gx,
                          so);
       sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, so);
@@ -917,6 +924,7 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       }
       if (outer >= max_outer && !fixed) status = DC_ERR_NOT_CONVERGED;
     }
+    if (first_sweep) CK(cudaMemsetAsync(w.X64, 0, sizeof(double) * N * Kp, s));  // no sweep ran: x = 0
   }
   if (mode == DC_MODE_MIXED)
     unpack_colmajor_df(reinterpret_cast<const float *>(w.X64), reinterpret_cast<const float *>(w.X64) + (size_t)N * Kp,

@@ -153,6 +153,8 @@ void ir_residual_df(const Level &L, const Coef32 *ch, const Coef32 *cl, const fl
                     const float *xh, const float *xl, float *r32, int nb, const int *active, double *partial, int gx,
                     cudaStream_t s);
 void ir_accumulate_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s);
+// (xh, xl) = d: the accumulation into a zero iterate, without reading it
+void ir_set_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s);
 
 void fill_int(int *a, int n, int v, cudaStream_t s);
 // alpha = rz / (p.q) per active RHS; also zeroes *n_active for the pcg_beta of the same iteration

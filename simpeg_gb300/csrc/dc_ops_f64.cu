@@ -232,6 +232,16 @@ __global__ void __launch_bounds__(TPB) k_ir_accumulate_df(long long n, float *__
   }
 }
 
+// (xh, xl) = 0 + d: what k_ir_accumulate_df gives from a zero iterate (hi = 0 + d, lo = +0), without
+// reading the zeros
+__global__ void __launch_bounds__(TPB) k_ir_set_df(long long n, float *__restrict__ xh, float *__restrict__ xl,
+                                                   const float *__restrict__ d32) {
+  for (long long i = (long long)blockIdx.x * TPB + threadIdx.x; i < n; i += (long long)gridDim.x * TPB) {
+    xh[i] = __fadd_rn(0.0f, d32[i]);
+    xl[i] = 0.0f;
+  }
+}
+
 }  // namespace
 
 DC_OPS_INSTANTIATE(double, double)
@@ -267,6 +277,10 @@ void ir_residual_df(const Level &L, const Coef32 *ch, const Coef32 *cl, const fl
 
 void ir_accumulate_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s) {
   k_ir_accumulate_df<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(n, xh, xl, d32);
+}
+
+void ir_set_df(long long n, float *xh, float *xl, const float *d32, cudaStream_t s) {
+  k_ir_set_df<<<count_launch(grid_flat(n, g_n_sm)), TPB, 0, s>>>(n, xh, xl, d32);
 }
 
 // resident blocks per SM of the fp64 reduction kernels the mixed solve also runs
