@@ -706,7 +706,7 @@ int body_stream(dc_handle *h, int depth, cudaStream_t *out) {
 template <typename T, typename V, int KB>
 int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Scal &sc, int nb, int gx,
         const int *init_active, const double *tol2, int maxit, int total_max, int *iters, cudaStream_t s,
-        int loop = LOOP_HOST, int depth = 0) {
+        int loop = LOOP_HOST, int depth = 0, bool x_unset = false) {
   using O = Ops<T, V, KB>;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
@@ -741,15 +741,18 @@ int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Sc
   O::copy_z(N, nb, p, z, s);
   const double c0 = smoother(h->smoother_kind, F.lmax, h->cheb_ratio, h->nu_pre, h->nu_post).first;
   V *z1 = fused ? first_buffer(h, 0, z, w) : nullptr;
-  // one PCG iteration on stream st
+  // one PCG iteration on stream st.  With x_unset (host-driven loops only) x holds no value yet and the
+  // first iteration writes it (x = alpha p) instead of adding to zeros.
+  bool x_zero = x_unset && loop != LOOP_DEVICE;
   auto iteration = [&](cudaStream_t st) {
     O::apply_v(F, p, q, nb, sc.part_a, gx, st);
     pcg_alpha(Kp, KB, gx, sc.part_a, sc.rz, sc.active, sc.alpha, sc.alpha32, sc.status, sc.n_active, st);
     if (fused) {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, &F, c0, z1, scale, w.r0, st);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, &F, c0, z1, scale, w.r0, st, x_zero);
       vcycle<T, V, KB>(h, 0, rin, z, w, nb, st, true, sc.part_c, gx);
     } else {
-      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, nullptr, st);
+      O::update_xr(N, nb, x, r, p, q, sc.alpha, sc.alpha32, sc.part_b, gx, nullptr, 0.0, nullptr, nullptr, nullptr, st,
+                   x_zero);
       if (split) O::scale_to(N, nb, r, scale, w.r0, st);
       vcycle<T, V, KB>(h, 0, rin, z, w, nb, st);
       O::dot_z(N, nb, r, z, sc.part_c, gx, st);
@@ -757,6 +760,7 @@ int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Sc
     pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.beta32, sc.n_active, 0, st,
              rz_div, scale);
     O::p_update(N, nb, p, z, sc.beta, sc.beta32, st);
+    x_zero = false;
   };
   if (loop == LOOP_DEVICE) {
     int rc;
@@ -867,18 +871,21 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
                 inner_rtol * inner_rtol, kSafety2, s);
     // one refinement sweep on stream so: inner fp32 PCG, accumulate, fp64 residual, new flags
     auto sweep = [&](cudaStream_t so, int inner_cap, int *it) -> int {
-      CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
+      // the inner correction starts at zero: a host-driven PCG that runs at least one iteration writes it
+      // in its first update, otherwise it is zeroed here
+      const bool unset = !device && inner_cap >= 1;
+      if (!unset) CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, so));
       int rc;
       if (w.storage == DC_MG_FP16)
         rc = pcg<float, __half, KB>(h, w.d32, w.r32, (__half *)w.pv, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
-                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
+                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset);
       else if (w.storage == DC_MG_BF16)
         rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, (__nv_bfloat16 *)w.pv, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16, w.sc, nb,
                                            gx, w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
-                                           device ? 1 : 0);
+                                           device ? 1 : 0, unset);
       else
         rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
-                                   w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0);
+                                   w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
       if (first_sweep) {
         ir_set_df((long long)N * Kp, xh, xl, w.d32, so);
@@ -985,17 +992,20 @@ int lanes_sweep_kb(dc_handle *h, SolveWS &w, double rtol, double inner_rtol, int
   float *bh = reinterpret_cast<float *>(w.R64), *bl = bh + (size_t)N * w.Kp;
   float *xh = reinterpret_cast<float *>(w.X64), *xl = xh + (size_t)N * w.Kp;
   CK(cudaMemsetAsync(w.sc.status, 0, sizeof(int), s));
-  CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
+  // the inner correction starts at zero; with at least one iteration its first update writes it
+  const bool unset = inner_cap >= 1;
+  if (!unset) CK(cudaMemsetAsync(w.d32, 0, sizeof(float) * N * Kp, s));
   int rc;
   if (w.storage == DC_MG_FP16)
     rc = pcg<float, __half, KB>(h, w.d32, w.r32, (__half *)w.pv, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
-                                w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+                                w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s, LOOP_HOST, 0, unset);
   else if (w.storage == DC_MG_BF16)
     rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, (__nv_bfloat16 *)w.pv, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16,
-                                       w.sc, nb, gx, w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+                                       w.sc, nb, gx, w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s, LOOP_HOST, 0,
+                                       unset);
   else
     rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
-                               w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s);
+                               w.sc.active_out, w.sc.tol2, inner_cap, inner_cap, it, s, LOOP_HOST, 0, unset);
   if (rc == DC_ERR_BREAKDOWN) return rc;
   ir_accumulate_df((long long)N * Kp, xh, xl, w.d32, s);
   ir_residual_df<KB>(F, h->d_cdf_hi, h->d_cdf_lo, bh, bl, xh, xl, w.r32, nb, w.sc.active_out, w.sc.part_a, gx, s);

@@ -126,9 +126,10 @@ template <typename T, typename V, int KB> struct Ops {
   // and, when rv_out is set, rv_out = V(scale r).
   // alpha / beta per RHS in fp64 (used when T is double) and fp32 (used when T is float: no
   // per-element fp64 -> fp32 conversion, which runs at GB300's fp64 rate)
+  // x_zero: x is 0 and is written, not read (the first update of a solve from zero)
   static void update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
                         const float *alpha32, double *partial, int gx, const Level *smooth, double c0, V *z,
-                        const float *scale, V *rv_out, cudaStream_t s);
+                        const float *scale, V *rv_out, cudaStream_t s, bool x_zero = false);
   // rv_out = V(scale r)
   static void scale_to(long long N, int nb, const T *r, const float *scale, V *rv_out, cudaStream_t s);
   static void dot(long long N, int nb, const T *a, const T *b, double *partial, int gx, cudaStream_t s);

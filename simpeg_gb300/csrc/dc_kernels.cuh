@@ -768,10 +768,18 @@ __global__ void __launch_bounds__(TPB) k_update_xr(Dims d, int nb, T *__restrict
                                                    const V *__restrict__ p, const T *__restrict__ qv,
                                                    const T *__restrict__ alpha, double *__restrict__ partial,
                                                    const T *__restrict__ invd, V *__restrict__ z, T c0,
-                                                   const float *__restrict__ scale, V *__restrict__ rv_out, int gs) {
+                                                   const float *__restrict__ scale, V *__restrict__ rv_out, int gs,
+                                                   int x_zero) {
   constexpr int W = Lanes<T, KB>::W;
   sweep_reduce<T, KB, W>(d.N, nb, partial, gs, [&](int b, int n, int q, long long t, T(&acc)[W]) {
-    Vec<T, W> xv = ld<T, W>(x + t), rv = ld<T, W>(r + t);
+    // x_zero: the first update of a solve from x = 0, whose x is not read (nor zeroed beforehand)
+    Vec<T, W> xv, rv = ld<T, W>(r + t);
+    if (x_zero) {
+#pragma unroll
+      for (int e = 0; e < W; ++e) xv.a[e] = (T)0;
+    } else {
+      xv = ld<T, W>(x + t);
+    }
     const Vec<T, W> pv = ld<T, W>(p + t), qq = ld<T, W>(qv + t);
     const Vec<T, W> av = lane_par<T, W>(alpha + b * KB + q * W);
 #pragma unroll
@@ -1081,15 +1089,15 @@ inline const float *param_of<float>(const double *, const float *f) {
 template <typename T, typename V, int KB>
 void Ops<T, V, KB>::update_xr(long long N, int nb, T *x, T *r, const V *p, const T *q, const double *alpha,
                               const float *alpha32, double *partial, int gx, const Level *smooth, double c0, V *z,
-                              const float *scale, V *rv_out, cudaStream_t s) {
+                              const float *scale, V *rv_out, cudaStream_t s, bool x_zero) {
   const Dims dd = flat_dims(N);
   const T *a = param_of<T>(alpha, alpha32);
   if (smooth)
     k_update_xr<T, V, KB, true><<<RED_GRID(N, (k_update_xr<T, V, KB, true>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
-        dd, nb, x, r, p, q, a, partial, invd_ptr<T>(*smooth), z, (T)c0, scale, rv_out, gx);
+        dd, nb, x, r, p, q, a, partial, invd_ptr<T>(*smooth), z, (T)c0, scale, rv_out, gx, x_zero ? 1 : 0);
   else
     k_update_xr<T, V, KB, false><<<RED_GRID(N, (k_update_xr<T, V, KB, false>), (Lanes<T, KB>::LPN)), TPB, 0, s>>>(
-        dd, nb, x, r, p, q, a, partial, nullptr, nullptr, (T)0, nullptr, nullptr, gx);
+        dd, nb, x, r, p, q, a, partial, nullptr, nullptr, (T)0, nullptr, nullptr, gx, x_zero ? 1 : 0);
 }
 
 template <typename T, typename V, int KB>
