@@ -363,6 +363,11 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# Algorithmic bytes per (node x RHS lane) of each kind of fine-level Chebyshev step with fp16 lanes:
+# momentum kinds read r, x_k, x_{k-1} and write x_{k+1}; the others read r, x_k and write x_{k+1}.
+STEP_LANE_BYTES = {"plain": 6.0, "zero_start": 6.0, "momentum": 8.0, "momentum_rz": 8.0}
+
+
 def _traffic_by_kind():
     """DRAM bytes per (node x RHS) of each kind of fine-level Chebyshev step (fp16 multigrid storage),
     from the committed ncu summary (lines ``dram_bytes_per_node_rhs[<kind>]: <value>``)."""
@@ -589,11 +594,10 @@ def _stencil_roofline(ms, n, alg_bytes, kinds=None, what="fine-level Chebyshev s
                               "frac": b / (t * 1e-3) / 1e9 / peak} for k, (c, t, b) in kinds.items()}
         if scaled_traffic:
             # DRAM bytes over algorithmic bytes of each kind in the profiled 1M-node, 256-RHS solve (fp16 lanes:
-            # 8 B per node-RHS with the momentum term, 6 B without, plus 20 B per node), applied to this run's
-            # algorithmic bytes of that kind
+            # STEP_LANE_BYTES per node-RHS plus 20 B per node), applied to this run's algorithmic bytes of that kind
             tbk = _traffic_by_kind()
             if all(k in tbk for k in kinds):
-                alg_nr = {k: ((8.0 if k.startswith("momentum") else 6.0) * 256 + 20.0) / 256 for k in kinds}
+                alg_nr = {k: (STEP_LANE_BYTES[k] * 256 + 20.0) / 256 for k in kinds}
                 out["traffic"] = sum(b * tbk[k] / alg_nr[k] for k, (_, _, b) in kinds.items()) / n
                 out["traffic_source"] = ("ncu DRAM bytes / algorithmic bytes of each kind of step in the profiled "
                                          "1M-node 256-RHS solve (profiles/cheb_step_fp16_dc3d.md), times this run's "

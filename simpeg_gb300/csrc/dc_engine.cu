@@ -293,6 +293,7 @@ void free_level(Level &L, bool own_geometry) {
   cudaFree(L.d_coef32);
   cudaFree(L.d_invd64);
   cudaFree(L.d_invd32);
+  cudaFree(L.d_rows32);
 }
 
 int build_hierarchy(dc_handle *h) {
@@ -344,6 +345,7 @@ int build_hierarchy(dc_handle *h) {
     if ((rc = dalloc(&L.d_coef32, L.dims.N))) return rc;
     if ((rc = dalloc(&L.d_invd64, L.dims.N))) return rc;
     if ((rc = dalloc(&L.d_invd32, L.dims.N))) return rc;
+    if (&L != &h->lv[0] && L.has_coarse && (rc = dalloc(&L.d_rows32, L.dims.N))) return rc;
     if (L.has_coarse) {
       std::vector<int> pl, rfi;
       std::vector<double> pw, rwl, rwr;
@@ -565,14 +567,14 @@ const double *ainv<double>(const dc_handle *h) { return h->d_Ainv64; }
 // stencil timing is on (dc_stencil_timing).
 template <typename T, typename V, int KB>
 void timed_cheb(const dc_handle *hc, int l, const Level &F, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb,
-                double c1, double c2, double *partial, int gx, int *status, cudaStream_t s) {
+                double c1, double c2, double *partial, int gx, int *status, cudaStream_t s, double c0 = 0.0) {
   dc_handle *h = const_cast<dc_handle *>(hc);
   const bool rec = h->prof && l == 0 && sizeof(T) == 4 && h->prof_used + 2 <= (int)h->prof_ev.size();
   if (rec) cudaEventRecord(h->prof_ev[h->prof_used], s);
   // finest level, 16-bit storage, no partials: x_k staged in shared memory by bulk copies
   const bool staged = h->bulk_staging && l == 0 && !partial && r.part && sizeof(V) == 2 &&
                       Ops<T, V, KB>::cheb_bulk(F, r.part, zin, zout, prev, nb, c1, c2, status, h->bulk_shape, s);
-  if (!staged) Ops<T, V, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s);
+  if (!staged) Ops<T, V, KB>::cheb_step(F, r, zin, zout, prev, nb, c1, c2, partial, gx, s, c0);
   if (rec) {
     cudaEventRecord(h->prof_ev[h->prof_used + 1], s);
     // algorithmic bytes: r (T, or V when stored narrow) and x_k (+ x_{k-1}) (V) read, x_{k+1} (V) written;
@@ -592,6 +594,20 @@ template <typename V>
 V *first_buffer(const dc_handle *h, int l, V *z, const MGWork<V> &w) {
   const int steps = (h->nu_pre - 1) + h->nu_post;
   return (steps % 2) ? w.z2[l] : z;
+}
+
+// Whether level l's first pre-smoothing step x_1 = c0 D^-1 r is folded into
+// the next two (never stored): the second forms A x_1 from r and the rows of
+// A D^-1 (prev 3), the third forms its x_{k-1} = x_1 from r at the node
+// (prev 4).  This saves a pass (k_cheb_first) on the coarse levels.  On the
+// finest level the fused x, r update (k_update_xr) already writes x_1, and
+// the folded step, with one vector stream in flight instead of two, measured
+// slower than the plain zero-start step (440 vs 368 us at 1M nodes x 256 RHS,
+// long-scoreboard stalls 7.5 vs 5.3 per issue), so it is not folded there.
+// fp32 arithmetic only (the rows are fp32); not with a single pre-smoothing
+// step (x_1 is then the residual's operand).
+bool folds_first(const dc_handle *h, int l, bool fp32) {
+  return fp32 && l > 0 && h->nu_pre >= 2 && h->lv[l].d_rows32;
 }
 
 // One V-cycle z = M r from level l.  r is the PCG residual (type T, scaled per
@@ -617,11 +633,14 @@ void vcycle(const dc_handle *h, int l, Rhs<T, V> r, V *z, const MGWork<V> &w, in
   V *cur = first_buffer(h, l, z, w);
   auto other = [&](V *c) { return c == z ? w.z2[l] : z; };
   // pre-smoothing from zero
-  if (!pre_done) O::cheb_first(F, r, cur, nb, sm.first, s);
+  const bool fold = folds_first(h, l, sizeof(T) == 4);
+  if (!pre_done && !fold) O::cheb_first(F, r, cur, nb, sm.first, s);
   for (int it = 1; it < h->nu_pre; ++it) {
     V *out = other(cur);
     const SmoothStep &st = sm.pre[it];
-    timed_cheb<T, V, KB>(h, l, F, r, cur, out, st.prev, nb, st.c1, st.c2, nullptr, 0, w.status, s);
+    // folded: x_1 is formed from r by the second step (prev 3) and by the third (prev 4, its x_{k-1})
+    const int prev = fold && it <= 2 ? it + 2 : st.prev;
+    timed_cheb<T, V, KB>(h, l, F, r, cur, out, prev, nb, st.c1, st.c2, nullptr, 0, w.status, s, sm.first);
     cur = out;
   }
   // coarse-grid correction
@@ -1229,6 +1248,7 @@ static int set_model_impl(dc_handle *h, const double *sigma_dev, const CCFine *c
     if (!(lm > 0.0) || !std::isfinite(lm)) return fail(DC_ERR_ARG, "conductivity must be positive and finite");
     h->lv[l].lmax = lm;
   }
+  for (size_t l = 1; l + 1 < nl; ++l) rows_dinv(h->lv[l], s);
   if (!h->d_cdf_hi) {
     int rc;
     if ((rc = dalloc(&h->d_cdf_hi, L0.dims.N))) return rc;

@@ -25,6 +25,9 @@ namespace dc {
 
 struct alignas(32) Coef64 { double cx, cy, cz, d; };
 struct alignas(16) Coef32 { float cx, cy, cz, d; };
+// Row n of A D^-1 in fp32: d_n / d_n and each coupling times the inverse
+// diagonal of the node it reaches (0 for an off-mesh neighbour).
+struct alignas(32) RowDinv32 { float d, xp, xm, yp, ym, zp, zm, pad; };
 
 struct Dims {
   int Nx, Ny, Nz;    // nodes per axis
@@ -61,6 +64,7 @@ struct Level {
   Coef32 *d_coef32 = nullptr;
   double *d_invd64 = nullptr;       // 1/diag
   float *d_invd32 = nullptr;
+  RowDinv32 *d_rows32 = nullptr;    // rows of A D^-1 (coarse levels with a coarser one): folded first step
   double lmax = 2.0;                // Gershgorin bound of D^-1 A
   // transfer to the next coarser level (valid when has_coarse)
   bool has_coarse = false;
@@ -110,10 +114,12 @@ template <typename T, typename V, int KB> struct Ops {
   static void residual(const Level &L, Rhs<T, V> r, const V *z, V *res, int nb, cudaStream_t s);
   // z = c0 D^-1 r (first Chebyshev step from zero)
   static void cheb_first(const Level &L, Rhs<T, V> r, V *z, int nb, double c0, cudaStream_t s);
-  // zout = zin + c1 (zin - prev) + c2 D^-1 (r - A zin); prev: 0 none, 1 = zout's old content, 2 = zero.
+  // zout = zin + c1 (zin - prev) + c2 D^-1 (r - A zin); prev: 0 none, 1 = zout's old content, 2 = zero;
+  // 3 = zero with zin = c0 D^-1 r formed from r and the rows of A D^-1 (zin not read); 4 = prev formed as
+  // c0 D^-1 r (zout's old content not read).  3 and 4: fp32 arithmetic, no partials.
   // With partial (finest level only): also per-block partials of r . zout.
   static void cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb, double c1,
-                        double c2, double *partial, int gx, cudaStream_t s);
+                        double c2, double *partial, int gx, cudaStream_t s, double c0 = 0.0);
   // The same step (no partials) with x_k staged in shared memory by bulk asynchronous copies, for r and
   // the iterates in V; false when it does not apply (then use cheb_step).  Copy timeouts set bit 8 of *status.
   // shape = 10 * slab rows + copy depth to force one layout (0: automatic).
@@ -181,6 +187,8 @@ void outer_loop_cond(cudaGraphConditionalHandle hc, int init, const int *n_activ
 
 
 void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cudaStream_t s);
+// L.d_rows32 from L's fp32 coefficients and inverse diagonal
+void rows_dinv(const Level &L, cudaStream_t s);
 void coarsen_sigma(const Level &f, const Level &c, cudaStream_t s);
 // Coarse level c's operator from the finer level f's coefficients (mode 1: collapsed Galerkin product with
 // the linear prolongation; mode 2: fine couplings in series along each coarse edge).

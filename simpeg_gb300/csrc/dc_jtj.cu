@@ -24,6 +24,7 @@
 #include "../../include/dcgpu.h"
 #include "dc_internal.h"
 
+#include <mutex>
 #include <string>
 
 namespace dc {
@@ -212,10 +213,25 @@ int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD
                    std::to_string((maxsm - static_smem) / (sizeof(double) + 28 * sizeof(float))) + ")";
     return DC_ERR_ARG;
   }
-  cudaError_t e = cudaFuncSetAttribute(k_jtj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) {
-    last_error() = std::string("dc_jtj_diag: ") + cudaGetErrorString(e);
-    return DC_ERR_CUDA;
+  // The dynamic shared-memory limit is raised once per device, to the largest tile the check above admits:
+  // set per call, a concurrent call with a smaller tile could lower it between another's set and launch.
+  {
+    static std::mutex mu;
+    static unsigned long long raised = 0;  // bit per device
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 64) {
+      last_error() = "dc_jtj_diag: device ordinal above 63";
+      return DC_ERR_ARG;
+    }
+    if (!(raised >> dev & 1ull)) {
+      const cudaError_t e = cudaFuncSetAttribute(k_jtj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)((size_t)maxsm - static_smem));
+      if (e != cudaSuccess) {
+        last_error() = std::string("dc_jtj_diag: ") + cudaGetErrorString(e);
+        return DC_ERR_CUDA;
+      }
+      raised |= 1ull << dev;
+    }
   }
   float *w32 = nullptr;
   if (cudaMallocAsync((void **)&w32, sizeof(float) * 5 * (size_t)(nD > 0 ? nD : 1), stream) != cudaSuccess) {
@@ -229,7 +245,7 @@ int jtj_diag_launch(const Level &L, int robin, const double *phi, int nE, int nD
       phi, nE, L.dims.N, L.nx, L.ny, L.nz, L.d_h, robin ? L.d_bface : nullptr, L.bface_off[0], L.bface_off[1],
       L.bface_off[2], L.bface_off[3], L.bface_off[4], L.bface_off[5], dsig, D, diag);
   cudaFreeAsync(w32, stream);
-  e = cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     last_error() = std::string("dc_jtj_diag: ") + cudaGetErrorString(e);
     return DC_ERR_CUDA;

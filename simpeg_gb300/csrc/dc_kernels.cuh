@@ -185,6 +185,29 @@ __device__ __forceinline__ Vec<T, W> stencil_vec(const typename CoefT<T>::type *
                                    pz ? c.cz : (T)0, hz ? wzm : (T)0, v0, vxp, vxm, vyp, vym, vzp, vzm);
 }
 
+// A (c0 D^-1 v) at element t of node n for the W lanes (v stored as S), from
+// the rows of A D^-1: two 16-byte loads per node instead of the coefficient
+// and seven inverse-diagonal loads, the seven neighbour loads as above.
+template <typename T, int KB, int W, typename S>
+__device__ __forceinline__ Vec<T, W> stencil_rows(const RowDinv32 *__restrict__ rows, const S *__restrict__ x,
+                                                   long long t, int n, int i, int j, int k, const Dims &d, T c0) {
+  static_assert(sizeof(T) == 4, "the rows of A D^-1 are fp32");
+  const int sxn = 1, syn = d.Nx, szn = d.Nx * d.Ny;
+  const bool hx = i > 0, hy = j > 0, hz = k > 0;
+  const bool px = i + 1 < d.Nx, py = j + 1 < d.Ny, pz = k + 1 < d.Nz;
+  const float4 *rp = reinterpret_cast<const float4 *>(rows + n);
+  const float4 ra = __ldg(rp), rb = __ldg(rp + 1);  // (d, xp, xm, yp), (ym, zp, zm, 0)
+  const Vec<T, W> v0 = ld<T, W>(x + t);
+  const Vec<T, W> vxp = ld<T, W>(x + t + (px ? (long long)sxn * KB : 0));
+  const Vec<T, W> vxm = ld<T, W>(x + t - (hx ? (long long)sxn * KB : 0));
+  const Vec<T, W> vyp = ld<T, W>(x + t + (py ? (long long)syn * KB : 0));
+  const Vec<T, W> vym = ld<T, W>(x + t - (hy ? (long long)syn * KB : 0));
+  const Vec<T, W> vzp = ld<T, W>(x + t + (pz ? (long long)szn * KB : 0));
+  const Vec<T, W> vzm = ld<T, W>(x + t - (hz ? (long long)szn * KB : 0));
+  return stencil_terms<T, W, true>(c0 * ra.x, c0 * ra.y, c0 * ra.z, c0 * ra.w, c0 * rb.x, c0 * rb.y, c0 * rb.z, v0,
+                                   vxp, vxm, vyp, vym, vzp, vzm);
+}
+
 // Right-hand side r (type R) of a smoothing kernel at element t, times the
 // per-lane scale when given (the finest level's PCG residual, see Rhs).
 // The W per-RHS parameters (alpha, beta, scale) of one thread's lanes, p
@@ -410,6 +433,11 @@ __global__ void __launch_bounds__(TPB) k_cheb_first(const T *__restrict__ invd, 
 //   PREV = 0: no momentum term (first step from a nonzero start, c1 = 0)
 //   PREV = 1: x_{k-1} read from zout (overwritten in place with x_{k+1})
 //   PREV = 2: x_{k-1} = 0 (second step of a zero-start sequence)
+//   PREV = 3: the second step of a zero start with x_1 = c0 D^-1 r formed from r
+//             on the fly (zin unused): the first step is never stored, and
+//             the step streams r and x_2 only
+//   PREV = 4: the third step of that sequence: momentum with x_{k-1} = x_1 =
+//             c0 D^-1 r formed pointwise from r (zout's old content not read)
 // Four streams per RHS lane (x_k, r, x_{k-1} read; x_{k+1} write) instead of the
 // five of the d-vector form.  With DOT (finest level), also per-block partials
 // of r . x_{k+1} with the unscaled PCG residual r.
@@ -417,8 +445,10 @@ template <typename T, typename V, typename R, int KB, bool DOT, int PREV>
 __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, const T *__restrict__ invd,
                                                    const R *__restrict__ r, const float *__restrict__ scale,
                                                    const V *__restrict__ zin, V *zout, Dims d, int nb, T c1, T c2,
-                                                   double *__restrict__ partial, int gs) {
+                                                   double *__restrict__ partial, int gs, T c0) {
   constexpr int W = Lanes<V, KB>::W;
+  static_assert(!(DOT && PREV >= 3), "the r.z partials belong to the last post-smoothing step");
+  // PREV 3: cf holds the rows of A D^-1 (RowDinv32), not the coefficients
   const auto *coef = coef_of<T, KB>(cf);
   auto body = [&](int b, int n, int q, long long t, T(&acc)[W]) {
     int i, j, k;
@@ -428,17 +458,29 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
     // the compiler (64, 4 blocks of TPB per SM): at 1M nodes x 256 RHS this
     // measured faster than 48 registers at 5 blocks, and than the zero-start
     // step as one r - A x chain of two-lane FMAs (405 -> 384 us per launch).
-    const Vec<T, W> az = stencil_vec<T, KB, W, V, !DOT || DOT_SMEM>(coef, zin, t, n, i, j, k, d);
+    Vec<T, W> az, zc, zo;
+    if constexpr (PREV == 3)
+      az = stencil_rows<T, KB, W, R>(static_cast<const RowDinv32 *>(cf), r, t, n, i, j, k, d, c0);
+    else
+      az = stencil_vec<T, KB, W, V, !DOT || DOT_SMEM>(coef, zin, t, n, i, j, k, d);
     const Vec<T, W> rv = ld<T, W>(r + t);
-    const Vec<T, W> zc = ld<T, W>(zin + t);
-    Vec<T, W> zo;
+    if constexpr (PREV != 3) zc = ld<T, W>(zin + t);
     if (PREV == 1) zo = ld<T, W>(zout + t);
-    const T s = c2 * invd[n];
+    const T dn = invd[n];
+    const T s = c2 * dn;
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const T mom = PREV == 1 ? c1 * (zc.a[e] - zo.a[e]) : (PREV == 2 ? c1 * zc.a[e] : (T)0);
       const T re = scale ? rv.a[e] * (T)scale[b * KB + q * W + e] : rv.a[e];
-      zo.a[e] = zc.a[e] + mom + s * (re - az.a[e]);
+      T ae = az.a[e];
+      if constexpr (PREV == 3) {
+        // x_1 = c0 D^-1 (scale r); the per-lane scale factors out of A x_1
+        zc.a[e] = (c0 * dn) * re;
+        if (scale) ae *= (T)scale[b * KB + q * W + e];
+      }
+      if constexpr (PREV == 4) zo.a[e] = (c0 * dn) * re;  // x_{k-1} = x_1
+      const T mom = (PREV == 1 || PREV == 4) ? c1 * (zc.a[e] - zo.a[e])
+                                             : ((PREV == 2 || PREV == 3) ? c1 * zc.a[e] : (T)0);
+      zo.a[e] = zc.a[e] + mom + s * (re - ae);
     }
     st<T, W>(zout + t, zo);
     if constexpr (DOT) {
@@ -450,7 +492,7 @@ __global__ void __launch_bounds__(TPB) k_cheb_step(const void *__restrict__ cf, 
   };
   auto pf = [&](long long tn) {
     if constexpr (sizeof(T) == 4) {
-      pf_line(zin, tn);
+      if (PREV != 3) pf_line(zin, tn);
       pf_line(r, tn);
       if (PREV == 1) pf_line(zout, tn);
     }
@@ -960,16 +1002,29 @@ void Ops<T, V, KB>::cheb_first(const Level &L, Rhs<T, V> r, V *z, int nb, double
 
 template <typename T, typename V, int KB, typename R, bool DOT, int PREV>
 static void cheb_launch(const Level &L, const R *r, const float *scale, const V *zin, V *zout, int nb, double c1,
-                        double c2, double *partial, int gx, cudaStream_t s) {
+                        double c2, double *partial, int gx, cudaStream_t s, double c0 = 0.0) {
   const dim3 g = DOT ? RED_GRID(L.dims.N, (k_cheb_step<T, V, R, KB, DOT, PREV>), (Lanes<V, KB>::LPN))
                      : GRID_K(L.dims.N, (k_cheb_step<T, V, R, KB, DOT, PREV>));
-  k_cheb_step<T, V, R, KB, DOT, PREV><<<g, TPB, 0, s>>>(coef_ptr<T>(L), invd_ptr<T>(L), r, scale, zin, zout, L.dims,
-                                                        nb, (T)c1, (T)c2, partial, gx);
+  const void *cf = PREV == 3 ? (const void *)L.d_rows32 : (const void *)coef_ptr<T>(L);
+  k_cheb_step<T, V, R, KB, DOT, PREV><<<g, TPB, 0, s>>>(cf, invd_ptr<T>(L), r, scale, zin, zout, L.dims, nb, (T)c1,
+                                                        (T)c2, partial, gx, (T)c0);
 }
 
 template <typename T, typename V, int KB>
 void Ops<T, V, KB>::cheb_step(const Level &L, Rhs<T, V> r, const V *zin, V *zout, int prev, int nb, double c1,
-                              double c2, double *partial, int gx, cudaStream_t s) {
+                              double c2, double *partial, int gx, cudaStream_t s, double c0) {
+  if constexpr (sizeof(T) == 4) {
+    if (prev == 3 && !partial) {
+      if (r.full) cheb_launch<T, V, KB, T, false, 3>(L, r.full, r.scale, nullptr, zout, nb, c1, c2, nullptr, gx, s, c0);
+      else cheb_launch<T, V, KB, V, false, 3>(L, r.part, nullptr, nullptr, zout, nb, c1, c2, nullptr, gx, s, c0);
+      return;
+    }
+    if (prev == 4 && !partial) {
+      if (r.full) cheb_launch<T, V, KB, T, false, 4>(L, r.full, r.scale, zin, zout, nb, c1, c2, nullptr, gx, s, c0);
+      else cheb_launch<T, V, KB, V, false, 4>(L, r.part, nullptr, zin, zout, nb, c1, c2, nullptr, gx, s, c0);
+      return;
+    }
+  }
   if (r.full) {
     const T *rp = r.full;
     const float *sc = r.scale;

@@ -784,6 +784,33 @@ void coef_build(const Level &L, int robin, unsigned long long *d_lmax_bits, cuda
                                                             d_lmax_bits);
 }
 
+// Rows of A D^-1: the couplings of row n scaled by the inverse diagonal of
+// the neighbour they multiply, so that A (c0 D^-1 r) needs r and one 32-byte
+// row per node (the folded first Chebyshev step).
+__global__ void k_rows_dinv(const Coef32 *__restrict__ c, const float *__restrict__ invd, Dims d,
+                            RowDinv32 *__restrict__ rows) {
+  const long long sy = d.Nx, sz = (long long)d.Nx * d.Ny;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < d.N; n += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    node_ijk((int)n, d, i, j, k);
+    const Coef32 cn = c[n];
+    RowDinv32 w;
+    w.d = cn.d * invd[n];
+    w.xp = i + 1 < d.Nx ? cn.cx * invd[n + 1] : 0.f;
+    w.xm = i > 0 ? c[n - 1].cx * invd[n - 1] : 0.f;
+    w.yp = j + 1 < d.Ny ? cn.cy * invd[n + sy] : 0.f;
+    w.ym = j > 0 ? c[n - sy].cy * invd[n - sy] : 0.f;
+    w.zp = k + 1 < d.Nz ? cn.cz * invd[n + sz] : 0.f;
+    w.zm = k > 0 ? c[n - sz].cz * invd[n - sz] : 0.f;
+    w.pad = 0.f;
+    rows[n] = w;
+  }
+}
+
+void rows_dinv(const Level &L, cudaStream_t s) {
+  k_rows_dinv<<<count_launch(grid_flat(L.dims.N, g_n_sm)), TPB, 0, s>>>(L.d_coef32, L.d_invd32, L.dims, L.d_rows32);
+}
+
 void coef_galerkin(const Level &f, const Level &c, int mode, unsigned long long *d_lmax_bits, cudaStream_t s) {
   AxisTab t;
   t.fi = f.d_r_fi;

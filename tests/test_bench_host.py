@@ -23,9 +23,9 @@ def bench():
 def test_traffic_by_kind_covers_every_step_kind(bench):
     tbk = bench._traffic_by_kind()
     assert set(tbk) == {"zero_start", "momentum", "plain", "momentum_rz"}
-    # fp16 lanes: 6 or 8 algorithmic bytes per node-RHS plus the coefficient re-reads
+    # fp16 lanes: 4, 6 or 8 algorithmic bytes per node-RHS plus the coefficient re-reads
     for k, v in tbk.items():
-        alg = 8.0 if k.startswith("momentum") else 6.0
+        alg = bench.STEP_LANE_BYTES[k]
         assert alg < v < 1.2 * alg
 
 
@@ -42,7 +42,7 @@ def test_stencil_roofline_arithmetic(bench):
     assert r["by_kind"]["momentum"]["achieved"] == pytest.approx(3.0e9 / 1e-3 / 1e9)
     # scaled traffic: each kind's algorithmic bytes times its measured DRAM/algorithmic ratio
     tbk = bench._traffic_by_kind()
-    ratio = {k: tbk[k] / (((8.0 if k.startswith("momentum") else 6.0) * 256 + 20.0) / 256) for k in kinds}
+    ratio = {k: tbk[k] / ((bench.STEP_LANE_BYTES[k] * 256 + 20.0) / 256) for k in kinds}
     want = (2.0e9 * ratio["plain"] + 3.0e9 * ratio["momentum"]) / n
     assert r["traffic"] == pytest.approx(want)
     assert bench._stencil_roofline(1.0, 0, 1.0) is None
