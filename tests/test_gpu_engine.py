@@ -185,6 +185,31 @@ def test_mixed_solve_every_multigrid_storage(cuda, storage, k):
     assert err.max() < 1e-8, (storage, err.max(), info)
 
 
+@pytest.mark.parametrize("nu,kind", [(1, 1), (2, 1), (3, 1), (4, 1), (2, 4), (3, 4)])
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_smoother_degrees_and_kinds_reach_the_direct_solution(cuda, nu, kind, mode):
+    """Every smoother degree and kind gives a V-cycle that PCG converges with: degree 1 (the first step
+    alone), 2 (its second step forms x_1 from r on the coarse levels), 3-4 (the third step forms its
+    previous iterate from r too), fourth-kind polynomials; fp64 runs the unfolded steps."""
+    import torch
+
+    from simpeg_gb300.engine import DCEngine
+
+    mesh = _mesh("padded")
+    sigma = _sigma(mesh, seed=13)
+    A = _oracle(mesh, sigma).getA().tocsc()
+    eng = DCEngine(mesh.h, robin_face_weights(mesh), nu_pre=nu, nu_post=nu, coarse_max=64, smoother=kind)
+    eng.set_model(torch.from_numpy(sigma).to(cuda))
+    rng = np.random.default_rng(17)
+    B = rng.standard_normal((40, mesh.n_nodes))
+    X, info = eng.solve(torch.from_numpy(B).to(cuda), mode=mode, rtol=1e-11)
+    X0 = spla.splu(A).solve(B.T).T
+    assert info.status == 0 and info.max_rel_res <= 1e-11
+    assert info.n_levels > 2  # coarse levels with smoothing
+    err = np.linalg.norm(X.cpu().numpy() - X0, axis=1) / np.linalg.norm(X0, axis=1)
+    assert err.max() < 1e-8, (nu, kind, mode, err.max(), info)
+
+
 @pytest.mark.parametrize("k", [32, 40, 16])
 def test_staged_smoothing_matches_direct_loads(cuda, k):
     """The shared-memory staged finest-level smoothing (bulk asynchronous
