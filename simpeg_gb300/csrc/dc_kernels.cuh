@@ -396,22 +396,33 @@ __global__ void __launch_bounds__(TPB, (DOT && sizeof(T) == 4 && sizeof(S) == 2)
     sweep_flat<T, KB, W>(d.N, d.mn, nb, body, pf);
 }
 
-// res = r - A z
+// res = r - A z (two-lane stencil and next-iteration L2 prefetch like the
+// Chebyshev steps: 367 -> 355 us per fine-level launch at 1M nodes x 256 RHS;
+// the same prefetch in k_prolong_add made it slower, 299 -> 315 us)
 template <typename T, typename V, typename R, int KB>
 __global__ void __launch_bounds__(TPB) k_residual(const void *__restrict__ cf, const R *__restrict__ r,
                                                   const float *__restrict__ scale, const V *__restrict__ z,
                                                   V *__restrict__ res, Dims d, int nb) {
   constexpr int W = Lanes<V, KB>::W;
   const auto *coef = coef_of<T, KB>(cf);
-  sweep_flat<T, KB, W>(d.N, d.mn, nb, [&](int b, int n, int q, long long t, T(&)[W]) {
-    int i, j, k;
-    node_ijk(n, d, i, j, k);
-    const Vec<T, W> az = stencil_vec<T, KB, W, V, false>(coef, z, t, n, i, j, k, d);
-    Vec<T, W> rv = rhs_at<T, KB, W>(r, scale, t, b, q);
+  auto pf = [&](long long tn) {
+    if constexpr (sizeof(T) == 4) {
+      pf_line(z, tn);
+      pf_line(r, tn);
+    }
+  };
+  sweep_flat<T, KB, W>(
+      d.N, d.mn, nb,
+      [&](int b, int n, int q, long long t, T(&)[W]) {
+        int i, j, k;
+        node_ijk(n, d, i, j, k);
+        const Vec<T, W> az = stencil_vec<T, KB, W, V>(coef, z, t, n, i, j, k, d);
+        Vec<T, W> rv = rhs_at<T, KB, W>(r, scale, t, b, q);
 #pragma unroll
-    for (int e = 0; e < W; ++e) rv.a[e] -= az.a[e];
-    st<T, W>(res + t, rv);
-  });
+        for (int e = 0; e < W; ++e) rv.a[e] -= az.a[e];
+        st<T, W>(res + t, rv);
+      },
+      pf);
 }
 
 // First Chebyshev step from z = 0: z = c0 * D^-1 r.
