@@ -722,10 +722,12 @@ int body_stream(dc_handle *h, int depth, cudaStream_t *out) {
 // init_active (nullable): RHS with init_active[r] == 0 are left untouched.
 // `depth` selects the body stream of a LOOP_DEVICE loop (0 unless nested in a
 // refinement loop); total_max caps the iterations summed over sweeps.
+// rr_part (nullable): per-block partials of |r|^2 (stride gx) left by the
+// kernel that wrote r; without them they are computed here.
 template <typename T, typename V, int KB>
 int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Scal &sc, int nb, int gx,
         const int *init_active, const double *tol2, int maxit, int total_max, int *iters, cudaStream_t s,
-        int loop = LOOP_HOST, int depth = 0, bool x_unset = false) {
+        int loop = LOOP_HOST, int depth = 0, bool x_unset = false, const double *rr_part = nullptr) {
   using O = Ops<T, V, KB>;
   const Level &F = h->lv[0];
   const long long N = F.dims.N;
@@ -749,13 +751,17 @@ int pcg(dc_handle *h, T *x, T *r, V *p, T *q, V *z, const MGWork<V> &w, const Sc
   else
     fill_int(sc.active, Kp, 1, s);
   CK(cudaMemsetAsync(sc.status, 0, sizeof(int), s));
-  O::dot(N, nb, r, r, sc.part_b, gx, s);
-  sum_partials(Kp, KB, gx, sc.part_b, sc.bb, s, scale);
+  const double *rrp = rr_part;
+  if (!rrp) {
+    O::dot(N, nb, r, r, sc.part_b, gx, s);
+    rrp = sc.part_b;
+  }
+  sum_partials(Kp, KB, gx, rrp, sc.bb, s, scale);
   if (split) O::scale_to(N, nb, r, scale, w.r0, s);
   vcycle<T, V, KB>(h, 0, rin, z, w, nb, s, false, sc.part_c, gx);
   if (!fused) O::dot_z(N, nb, r, z, sc.part_c, gx, s);
   CK(cudaMemsetAsync(sc.n_active, 0, sizeof(int), s));
-  pcg_beta(Kp, KB, gx, sc.part_c, sc.part_b, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.beta32, sc.n_active, 1, s,
+  pcg_beta(Kp, KB, gx, sc.part_c, rrp, sc.rz, sc.rr, sc.bb, tol2, sc.active, sc.beta, sc.beta32, sc.n_active, 1, s,
            rz_div, scale);
   O::copy_z(N, nb, p, z, s);
   const double c0 = smoother(h->smoother_kind, F.lmax, h->cheb_ratio, h->nu_pre, h->nu_post).first;
@@ -882,10 +888,11 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
     else
       split_df(w.B64, (long long)N * Kp, bh, bl, w.r32, s);
     // |b|^2 from the fp32 copy of b (the stopping test needs it to ~1e-6 relatively; an fp64 dot runs at
-    // the fp64 rate), initial outer flags
-    Ops<float, float, KB>::dot(N, nb, w.r32, w.r32, w.sc.part_b, gx, s);
-    sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.bb64, s);
-    sum_partials(Kp, KB, gx, w.sc.part_b, w.sc.rr64, s);
+    // the fp64 rate), initial outer flags.  part_a holds the |r32|^2 partials at the start of every sweep
+    // (from here, then from the residual kernel), and the inner PCG starts from them.
+    Ops<float, float, KB>::dot(N, nb, w.r32, w.r32, w.sc.part_a, gx, s);
+    sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.bb64, s);
+    sum_partials(Kp, KB, gx, w.sc.part_a, w.sc.rr64, s);
     outer_check(Kp, w.sc.rr64, w.sc.bb64, rtol * rtol, w.sc.active_out, w.sc.n_active_out, w.sc.maxrel, w.sc.tol2,
                 inner_rtol * inner_rtol, kSafety2, s);
     // one refinement sweep on stream so: inner fp32 PCG, accumulate, fp64 residual, new flags
@@ -897,14 +904,16 @@ int solve_kb(dc_handle *h, int mode, const double *b, double *x, int k, double r
       int rc;
       if (w.storage == DC_MG_FP16)
         rc = pcg<float, __half, KB>(h, w.d32, w.r32, (__half *)w.pv, w.q32, (__half *)w.zv, w.mg16, w.sc, nb, gx,
-                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset);
+                                    w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset,
+                                    w.sc.part_a);
       else if (w.storage == DC_MG_BF16)
         rc = pcg<float, __nv_bfloat16, KB>(h, w.d32, w.r32, (__nv_bfloat16 *)w.pv, w.q32, (__nv_bfloat16 *)w.zv, w.mgb16, w.sc, nb,
                                            gx, w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop,
-                                           device ? 1 : 0, unset);
+                                           device ? 1 : 0, unset, w.sc.part_a);
       else
         rc = pcg<float, float, KB>(h, w.d32, w.r32, (float *)w.pv, w.q32, (float *)w.zv, w.mg32, w.sc, nb, gx,
-                                   w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset);
+                                   w.sc.active_out, w.sc.tol2, inner_cap, maxit, it, so, loop, device ? 1 : 0, unset,
+                                   w.sc.part_a);
       if (rc == DC_ERR_BREAKDOWN || (device && rc)) return rc;
       if (first_sweep) {
         ir_set_df((long long)N * Kp, xh, xl, w.d32, so);
