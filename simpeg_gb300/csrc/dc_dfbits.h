@@ -75,4 +75,62 @@ DC_HD bool widen_bits(float f, double &d) {
   return true;
 }
 
+// d = (double)hi + (double)lo rounded to nearest even, as the fp64 addition
+// rounds it, by integer operations, for a normalised double-float pair: hi
+// normal and lo zero, or lo normal at least 24 binades below hi (exponent gap
+// g >= 24, which |lo| <= ulp(hi) / 2 implies).  In units of 2^-52 of hi's
+// binade hi is the 53-bit integer m = (hi's significand) << 29 and lo is
+// (lo's significand) * 2^(29 - g): an integer for g <= 29, added exactly
+// (below 2^53); for g >= 30 its integer part is added and the shifted-out
+// bits round the sum.  False for what is left to the fp64 addition: hi zero
+// (unless lo is zero too), denormal, inf or nan; lo denormal, inf or nan;
+// g < 24; hi a power of two with lo of the opposite sign and g >= 30 (the sum
+// falls into the binade below, where the rounding point moves).
+DC_HD bool df_sum_bits(float hi, float lo, double &d) {
+  const uint32_t bh = bits32(hi), bl = bits32(lo);
+  const uint32_t eh = (bh >> 23) & 0xff;
+  if ((bh << 1) == 0 && (bl << 1) == 0) {  // +-0 + +-0: -0 only when both are -0
+    d = from_bits64((uint64_t)(bh & bl & 0x80000000u) << 32);
+    return true;
+  }
+  if (eh == 0 || eh == 255) return false;
+  uint64_t m = (uint64_t)((bh & 0x7FFFFFu) | 0x800000u) << 29;
+  uint32_t ed = eh + 896;  // fp64 biased exponent of hi
+  if ((bl << 1) != 0) {
+    const uint32_t el = (bl >> 23) & 0xff;
+    if (el == 0 || el == 255) return false;
+    const int g = (int)eh - (int)el;
+    if (g < 24) return false;
+    const uint64_t ml = (bl & 0x7FFFFFu) | 0x800000u;
+    const bool same = (bh >> 31) == (bl >> 31);
+    if (g <= 29) {
+      const uint64_t t = ml << (29 - g);
+      m = same ? m + t : m - t;  // exact: below 2^53, and above 2^51 after a subtraction
+      if (m < (1ull << 52)) {    // hi a power of two, lo subtracted: one binade down, exactly
+        m <<= 1;
+        --ed;
+      }
+    } else {
+      if (!same && m == (1ull << 52)) return false;
+      const int sh = g - 29;
+      if (sh <= 24) {  // for larger gaps |lo| is below half a unit: the sum rounds to hi
+        const uint64_t q = ml >> sh, rem = ml & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (same) {
+          m += q;
+          if (rem > half || (rem == half && (m & 1))) ++m;
+        } else {
+          m -= q;
+          if (rem) {  // m - q - rem / 2^sh = (m - q - 1) + (2^sh - rem) / 2^sh
+            const uint64_t f = (1ull << sh) - rem;
+            --m;
+            if (f > half || (f == half && (m & 1))) ++m;
+          }
+        }
+      }
+    }
+  }
+  d = from_bits64(((uint64_t)(bh >> 31) << 63) | ((uint64_t)ed << 52) | (m & 0xFFFFFFFFFFFFFull));
+  return true;
+}
+
 }  // namespace dc

@@ -26,8 +26,8 @@ __device__ __forceinline__ long long lane_elem(int lane, long long node, long lo
   return ((long long)(lane / KB) * N + node) * KB + lane % KB;
 }
 
-// fp64 instructions only outside the normal fp32 range, in calls of their own
-__device__ __noinline__ double widen_slow(float f) { return (double)f; }
+// fp64 instructions only where the bit routines do not cover the value, in calls of their own
+__device__ __noinline__ double sum_slow(float h, float l) { return (double)h + (double)l; }
 __device__ __noinline__ void split_slow(double v, float &h, float &l) {
   h = (float)v;
   l = (float)(v - (double)h);
@@ -79,10 +79,10 @@ __global__ void k_lanes_fetch(const float *__restrict__ xh, const float *__restr
     const int i = (int)(t / N);
     const long long node = t - (long long)i * N;
     const long long e = lane_elem(lanes[i], node, N, KB);
-    double h, l;
-    if (__builtin_expect(!widen_bits(xh[e], h), 0)) h = widen_slow(xh[e]);
-    if (__builtin_expect(!widen_bits(xl[e], l), 0)) l = widen_slow(xl[e]);
-    x[t] = h + l;
+    const float fh = xh[e], fl = xl[e];
+    double v;
+    if (__builtin_expect(!df_sum_bits(fh, fl, v), 0)) v = sum_slow(fh, fl);
+    x[t] = v;
   }
 }
 

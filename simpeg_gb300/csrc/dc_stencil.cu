@@ -671,12 +671,16 @@ __global__ void __launch_bounds__(TT *TR) k_unpack(const T *__restrict__ src, lo
   }
 }
 
-// (double)f with the fp64 conversion instruction, in a call of its own (kept out
-// of the common path of k_unpack_df).
-__device__ __noinline__ double widen_fp64(float f) { return (double)f; }
+// (double)h + (double)l with the fp64 instructions, in a call of its own (kept
+// out of the common path of k_unpack_df).
+__device__ __noinline__ double df_sum_fp64(float h, float l) { return (double)h + (double)l; }
 
-// The same transpose for a double-float (hi, lo) blocked array: dst = hi + lo in fp64
-// (each fp32 widened by bits where that covers it, one fp64 add).
+// The same transpose for a double-float (hi, lo) blocked array: dst = hi + lo in
+// fp64, rounded as the fp64 addition rounds it, by integer operations for
+// normalised pairs (df_sum_bits) and the fp64 instructions otherwise.  With one
+// fp64 add per element the transpose ran at GB300's fp64 rate (1.34 ms at 1M
+// nodes x 256 RHS; 1.21 ms by bits.  Tiles of 32 x 128 instead of 32 x 32
+// measured slower, 1.45 ms).
 __global__ void __launch_bounds__(TT *TR) k_unpack_df(const float *__restrict__ hi, const float *__restrict__ lo,
                                                      long long N, int K, int KB, double *__restrict__ dst) {
   __shared__ double tile[TT][TT + 1];
@@ -689,10 +693,10 @@ __global__ void __launch_bounds__(TT *TR) k_unpack_df(const float *__restrict__ 
       const long long n = n0 + j;
       if (r < K && n < N) {
         const long long e = ((long long)b * N + n) * KB + l;
-        double h, l;
-        if (__builtin_expect(!widen_bits(hi[e], h), 0)) h = widen_fp64(hi[e]);
-        if (__builtin_expect(!widen_bits(lo[e], l), 0)) l = widen_fp64(lo[e]);
-        tile[threadIdx.x][j] = h + l;
+        const float fh = hi[e], fl = lo[e];
+        double v;
+        if (__builtin_expect(!df_sum_bits(fh, fl, v), 0)) v = df_sum_fp64(fh, fl);
+        tile[threadIdx.x][j] = v;
       }
     }
   }

@@ -220,9 +220,10 @@ def test_device_map_transforms_match_host():
 
 
 def test_double_float_bit_routines(tmp_path):
-    """The bit-level double-float split and widening (csrc/dc_dfbits.h), compiled for
+    """The bit-level double-float split, widening and sum (csrc/dc_dfbits.h), compiled for
     the host: truncation split exact to 2^-48, widening equal to the fp32 -> fp64
-    conversion, out-of-range values rejected (they take the fp64 instructions)."""
+    conversion, the pair sum equal to the fp64 addition bit for bit, out-of-range
+    values rejected (they take the fp64 instructions)."""
     import shutil
     import subprocess
 
