@@ -153,3 +153,45 @@ def test_gpu_solver_neumann_pinned(cuda):
     assert _rel(X, X0) < 1e-9
     assert _rel(Ainv * B[:, 0], X0[:, 0]) < 1e-9
     Ainv.clean()
+
+
+def test_jtj_diag_concurrent_calls_with_different_tiles(cuda):
+    """getJtJdiag of four simulations from four threads at once, on surveys with different
+    electrode counts (different shared-memory tiles of the reciprocity kernel): every call
+    succeeds and equals the simulation's serial result."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import torch
+
+    mesh = TensorMesh([[(10.0, 12)], [(10.0, 10)], [(10.0, 8)]], origin="CCN")
+    xs = -50.0 + 10.0 * np.arange(11)
+
+    def survey(n_src):
+        src = []
+        for i in range(n_src):
+            rx = receivers.Dipole(np.c_[xs[i + 3:i + 6], np.zeros(3), np.zeros(3)],
+                                  np.c_[xs[i + 4:i + 7], np.zeros(3), np.zeros(3)])
+            src.append(sources.Dipole([rx], np.r_[xs[i], 0.0, 0.0], np.r_[xs[i + 1], 0.0, 0.0]))
+        return Survey(src)
+
+    rng = np.random.default_rng(21)
+    m = np.log(10 ** rng.uniform(-2.5, -1.5, mesh.n_cells))
+    sims = [Simulation3DNodal(mesh, survey=survey(n), sigmaMap=maps.ExpMap(mesh), precision="fp64", rtol=1e-11)
+            for n in (2, 4, 2, 4)]
+    serial = [s.getJtJdiag(m).copy() for s in sims]
+
+    def run(i):
+        s = sims[i]
+        out = []
+        with torch.cuda.stream(torch.cuda.Stream()):
+            for _ in range(5):
+                s._gtgdiag = None
+                out.append(s.getJtJdiag(m).copy())
+            torch.cuda.current_stream().synchronize()
+        return out
+
+    with ThreadPoolExecutor(len(sims)) as ex:
+        results = list(ex.map(run, range(len(sims))))
+    for i, outs in enumerate(results):
+        for d in outs:
+            assert _rel(d, serial[i]) < 1e-12
